@@ -1,0 +1,167 @@
+"""ctypes mirror of include/doma_gb300.h and the loader of the native library.
+
+The native library (``doma_gb300/_lib/libdoma_gb300.so``) is the product: CUDA
+kernels for sm_103a plus the C ABI.  This module only binds it.  There is no
+fallback: if the library is missing or a call needs a GPU that is not there,
+the call fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_DIR = PKG_DIR / "_lib"
+LIB_PATH = LIB_DIR / "libdoma_gb300.so"
+
+DOMA_OK = 0
+DOMA_NOT_CONVERGED = 1
+DOMA_BAD_INPUT = 2
+DOMA_CUDA_ERROR = 3
+DOMA_DEVICE_WAIT_TIMEOUT = 4
+DOMA_NO_DEVICE = 5
+DOMA_NUMERIC_ERROR = 6
+
+STATUS_NAMES = {
+    0: "DOMA_OK",
+    1: "DOMA_NOT_CONVERGED",
+    2: "DOMA_BAD_INPUT",
+    3: "DOMA_CUDA_ERROR",
+    4: "DOMA_DEVICE_WAIT_TIMEOUT",
+    5: "DOMA_NO_DEVICE",
+    6: "DOMA_NUMERIC_ERROR",
+}
+
+DOMA_SCHEME_DD = 0
+DOMA_SCHEME_TW_DD = 1
+DOMA_PREC_FP64 = 0
+DOMA_PREC_FP32 = 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+class DomaProblem(ctypes.Structure):
+    _fields_ = [
+        ("num_dims", ctypes.c_uint32),
+        ("nx", ctypes.c_uint32),
+        ("ny", ctypes.c_uint32),
+        ("nz", ctypes.c_uint32),
+        ("dx", _dp),
+        ("dy", _dp),
+        ("dz", _dp),
+        ("num_groups", ctypes.c_uint32),
+        ("num_materials", ctypes.c_uint32),
+        ("cell_material", _u32p),
+        ("total", _dp),
+        ("scatter", _dp),
+        ("source", _dp),
+        ("has_fission", _u8p),
+        ("chi_p", _dp),
+        ("nu_sigma_f", _dp),
+        ("num_polar", ctypes.c_uint32),
+        ("num_azimuthal", ctypes.c_uint32),
+    ]
+
+
+class DomaOptions(ctypes.Structure):
+    _fields_ = [
+        ("scheme", ctypes.c_uint32),
+        ("theta", ctypes.c_double),
+        ("precision", ctypes.c_uint32),
+        ("fs_tol", ctypes.c_double),
+        ("fs_max_it", ctypes.c_uint32),
+        ("mg_tol", ctypes.c_double),
+        ("mg_max_it", ctypes.c_uint32),
+        ("verbose", ctypes.c_uint32),
+        ("tile_x", ctypes.c_uint32),
+        ("tile_y", ctypes.c_uint32),
+        ("tile_z", ctypes.c_uint32),
+    ]
+
+
+class DomaReport(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_uint32),
+        ("mg_iterations", ctypes.c_uint32),
+        ("si_iterations", ctypes.c_uint64),
+        ("updates", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("mg_residual", ctypes.c_double),
+        ("si_residual", ctypes.c_double),
+        ("solve_ms", ctypes.c_double),
+        ("si_counts", _u32p),
+        ("si_counts_capacity", ctypes.c_size_t),
+        ("si_counts_len", ctypes.c_size_t),
+    ]
+
+
+# Every entry point declared in include/doma_gb300.h: name -> (restype, argtypes).
+SIGNATURES = {
+    "doma_default_options": (None, [ctypes.POINTER(DomaOptions)]),
+    "doma_last_error": (ctypes.c_char_p, []),
+    "doma_abi_version": (ctypes.c_uint32, []),
+    "doma_quadrature": (
+        ctypes.c_int,
+        [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _dp, _dp, _dp, _dp, _u32p],
+    ),
+    "doma_solver_create": (
+        ctypes.c_int,
+        [ctypes.POINTER(DomaProblem), ctypes.POINTER(DomaOptions), ctypes.POINTER(ctypes.c_void_p)],
+    ),
+    "doma_solver_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "doma_solver_solve_fixed_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport)]),
+    "doma_solver_get_scalar_flux": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_size_t]),
+    "doma_solver_source_iterations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
+    "doma_solver_sweeps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
+    "doma_solver_describe": (
+        ctypes.c_int,
+        [ctypes.c_void_p, _u32p, _u32p, ctypes.POINTER(ctypes.c_uint64)],
+    ),
+    "doma_solver_destroy": (None, [ctypes.c_void_p]),
+}
+
+_LIB = None
+
+
+class DomaError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str = ""):
+        self.status = status
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} {message}".strip())
+
+
+def load_library(path: os.PathLike | str | None = None) -> ctypes.CDLL:
+    """Load the native library and bind every declared symbol (raises if absent)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"native library {p} is missing; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)"
+        )
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.doma_abi_version() != 1:
+        raise RuntimeError("doma_gb300 ABI version mismatch")
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def last_error(lib: ctypes.CDLL | None = None) -> str:
+    lib = lib or load_library()
+    msg = lib.doma_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(status: int, where: str, lib: ctypes.CDLL | None = None, allow=(DOMA_OK,)) -> int:
+    if status not in allow:
+        raise DomaError(status, where, last_error(lib))
+    return status

@@ -1,0 +1,182 @@
+/*
+ * doma_gb300.h -- C ABI of the GB300 fixed-source discrete-ordinates solver.
+ *
+ * The library replaces DOMA's fixed-source hot path: the Gauss-Seidel loop
+ * over energy groups, the within-group scattering-source iteration (increment
+ * form) and the octant-by-octant transport sweep with diamond-difference (DD)
+ * or theta-weighted diamond-difference (TW-DD) cell solves.  Everything
+ * crosses this boundary as plain C: pointers, sizes and status codes.  No C++
+ * or torch types appear here, so a C++ shim, ctypes or any other FFI can bind
+ * it directly.
+ *
+ * Reference interfaces replaced (paths inside the DOMA source tree):
+ *   doma_solver_create                 TransportSolver3D<T>::TransportSolver3D
+ *                                      (src/TransportSolver3D.cpp:5-27) and
+ *                                      TransportSolver2D<T>::TransportSolver2D
+ *                                      (src/TransportSolver2D.cpp:5-27), plus the
+ *                                      mesh set-up of BrickMesh3D/2D
+ *                                      (src/BrickMesh3D.cpp:8-184)
+ *   doma_solver_solve_fixed_source     TransportSolver3D<T>::solveFixedSource
+ *                                      (src/TransportSolver3D.cpp:262-316) and the
+ *                                      2D twin (src/TransportSolver2D.cpp:264-316)
+ *   doma_solver_get_scalar_flux        read-back of CartesianCell3D::_total_scalar_flux
+ *                                      (include/CartesianCell3D.h:99), as used by
+ *                                      BrickMesh3D::dumpToTextFile / fluxAtPoint
+ *   doma_quadrature                    GCAngularQuadrature::GCAngularQuadrature,
+ *                                      order/direction/weight
+ *                                      (src/GCAngularQuadrature.cpp:9-75)
+ *   doma_solver_source_iterations,     single steps of TransportSolver3D::sourceIteration
+ *   doma_solver_sweeps                 (src/TransportSolver3D.cpp:458-497) and ::sweep
+ *                                      (src/TransportSolver3D.cpp:565-622), exposed so a
+ *                                      caller can time the hot loop on resident data
+ *
+ * Status codes replace the reference's std::exit(1) on bad input and its
+ * `false` return on non-convergence; the library never exits the process.
+ */
+#ifndef DOMA_GB300_H
+#define DOMA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DOMA_ABI_VERSION 1u
+
+/* Status codes returned by every entry point. */
+typedef enum doma_status {
+  DOMA_OK = 0,
+  DOMA_NOT_CONVERGED = 1,        /* iteration cap reached (reference returns false) */
+  DOMA_BAD_INPUT = 2,            /* invalid problem or options (reference exits) */
+  DOMA_CUDA_ERROR = 3,           /* a CUDA runtime call failed */
+  DOMA_DEVICE_WAIT_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+  DOMA_NO_DEVICE = 5,            /* no CUDA device is visible */
+  DOMA_NUMERIC_ERROR = 6         /* a residual norm became NaN or Inf */
+} doma_status;
+
+/* Cell-balance scheme: EquationType DD / TW_DD (include/TransportBase.h:45-49). */
+enum { DOMA_SCHEME_DD = 0, DOMA_SCHEME_TW_DD = 1 };
+
+/* Arithmetic of the sweep.
+ *   DOMA_PREC_FP64: reference drop-in.  Every cell solve uses the reference's
+ *     operation order with round-to-nearest IEEE double and no fused
+ *     multiply-add; the scalar flux is accumulated over directions in the
+ *     reference's single-thread order (octant PPP..MMM, then ordinate).
+ *   DOMA_PREC_FP32: single-precision sweep with compensated angular sums;
+ *     sources, scalar flux, residual and convergence norms stay double. */
+enum { DOMA_PREC_FP64 = 0, DOMA_PREC_FP32 = 1 };
+
+/* A fixed-source problem on a tensor-product Cartesian mesh.
+ * Cells are numbered x fastest, then y, then z (src/BrickMesh3D.cpp:83-102).
+ * Materials play the role of DOMA's block ids (include/InputParameters.h:24-48). */
+typedef struct doma_problem {
+  uint32_t num_dims;              /* 2 or 3 */
+  uint32_t nx, ny, nz;            /* cells per axis; nz must be 1 when num_dims == 2 */
+  const double *dx;               /* [nx] cell widths along x (cm) */
+  const double *dy;               /* [ny] cell widths along y (cm) */
+  const double *dz;               /* [nz] cell widths along z (cm); ignored in 2D */
+  uint32_t num_groups;            /* G */
+  uint32_t num_materials;         /* M */
+  const uint32_t *cell_material;  /* [nx*ny*nz] material index of every cell */
+  const double *total;            /* [M][G] total cross section */
+  const double *scatter;          /* [M][G][G] row-major [to*G + from] */
+  const double *source;           /* [M][G] isotropic external source, or NULL */
+  const uint8_t *has_fission;     /* [M] nonzero: material carries a prompt
+                                     fission spectrum, or NULL for none */
+  const double *chi_p;            /* [M][G] prompt fission spectrum, or NULL */
+  const double *nu_sigma_f;       /* [M][G] fission production, or NULL */
+  uint32_t num_polar;             /* np of <angular_quad>: 2*np Legendre roots */
+  uint32_t num_azimuthal;         /* na of <angular_quad>: 2*na Chebyshev roots */
+} doma_problem;
+
+/* Solver options (the <solver> block of a DOMA deck plus GPU choices). */
+typedef struct doma_options {
+  uint32_t scheme;      /* DOMA_SCHEME_DD or DOMA_SCHEME_TW_DD */
+  double theta;         /* TW-DD theta (= theta_s); DOMA uses 0.9 */
+  uint32_t precision;   /* DOMA_PREC_FP64 or DOMA_PREC_FP32 */
+  double fs_tol;        /* source-iteration tolerance (relative L2 of the increment) */
+  uint32_t fs_max_it;   /* source-iteration cap */
+  double mg_tol;        /* Gauss-Seidel tolerance (relative L2 of the group change) */
+  uint32_t mg_max_it;   /* Gauss-Seidel cap */
+  uint32_t verbose;     /* 0: silent, 1: the reference's progress lines on stdout,
+                           2: also every SI residual (the reference's --verbose) */
+  uint32_t tile_x, tile_y, tile_z;   /* sweep block shape in cells; 0 = pick */
+} doma_options;
+
+/* Filled by doma_solver_solve_fixed_source. */
+typedef struct doma_report {
+  uint32_t status;            /* doma_status of the solve */
+  uint32_t mg_iterations;     /* Gauss-Seidel iterations performed */
+  uint64_t si_iterations;     /* source iterations (= sweeps) over all groups */
+  uint64_t updates;           /* cell * direction * group updates swept */
+  uint64_t kernel_launches;   /* CUDA kernel launches issued by the solve */
+  double mg_residual;         /* last Gauss-Seidel residual */
+  double si_residual;         /* last source-iteration residual */
+  double solve_ms;            /* host wall time of the solve */
+  uint32_t *si_counts;        /* optional caller buffer: SI count of every
+                                 (MG iteration, group) pair, in solve order */
+  size_t si_counts_capacity;  /* entries available in si_counts */
+  size_t si_counts_len;       /* entries written (may exceed capacity: the
+                                 rest were dropped) */
+} doma_report;
+
+typedef struct doma_solver doma_solver;
+
+/* Default options: DD, theta 0.9, FP64, tolerances 1e-8, caps 1000/100. */
+void doma_default_options(doma_options *opts);
+
+/* Last error message of the calling thread ("" if none). */
+const char *doma_last_error(void);
+
+/* ABI version of the loaded library (DOMA_ABI_VERSION). */
+uint32_t doma_abi_version(void);
+
+/* Gauss-Chebyshev product quadrature binned by octant, exactly as
+ * GCAngularQuadrature(2*na, 2*np, num_dims) builds it.  Outputs are sized
+ * 8*np*na (3D) or 4*np*na (2D) and ordered octant-major (PPP, PPM, PMP, PMM,
+ * MPP, MPM, MMP, MMM), then by ordinate; counts[8] gets the per-octant sizes.
+ * Host-only: needs no GPU. */
+doma_status doma_quadrature(uint32_t num_polar, uint32_t num_azimuthal, uint32_t num_dims,
+                            double *mu, double *eta, double *xi, double *weight,
+                            uint32_t counts[8]);
+
+/* Validate the problem, build the quadrature and upload everything to the
+ * current CUDA device.  The problem arrays are copied; the caller may free
+ * them after this returns. */
+doma_status doma_solver_create(const doma_problem *problem, const doma_options *opts,
+                               doma_solver **out);
+
+/* Launch all work of this solver on `stream` (a cudaStream_t; NULL = the
+ * solver's own stream). */
+doma_status doma_solver_set_stream(doma_solver *solver, void *stream);
+
+/* Zero the scalar flux and run the Gauss-Seidel / source-iteration solve.
+ * Returns DOMA_OK, or DOMA_NOT_CONVERGED when an iteration cap was hit (the
+ * flux of the last iterate is kept, as in the reference). */
+doma_status doma_solver_solve_fixed_source(doma_solver *solver, doma_report *report);
+
+/* Copy the scalar flux to host memory: out[g*N + cell], N = nx*ny*nz. */
+doma_status doma_solver_get_scalar_flux(doma_solver *solver, double *out, size_t count);
+
+/* Set up the group-g source (external + in-scatter + fission) from the
+ * current flux, then run `count` source iterations (sweep, residual, source
+ * update) without a convergence test.  Stream-ordered; does not synchronise. */
+doma_status doma_solver_source_iterations(doma_solver *solver, uint32_t group, uint32_t count);
+
+/* Run `count` bare sweeps of group g on the current iteration source (no
+ * residual, no update).  Stream-ordered; for timing the sweep kernels. */
+doma_status doma_solver_sweeps(doma_solver *solver, uint32_t group, uint32_t count);
+
+/* Sweep block shape and launch counts actually in use (for reports). */
+doma_status doma_solver_describe(const doma_solver *solver, uint32_t tile[3],
+                                 uint32_t *launches_per_sweep, uint64_t *kernel_launches);
+
+void doma_solver_destroy(doma_solver *solver);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* DOMA_GB300_H */

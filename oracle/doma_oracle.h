@@ -1,0 +1,47 @@
+/*
+ * doma_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, CPU restatement of DOMA's 2D/3D fixed-source path, used as the
+ * checker for the GPU library (tests, the smoke check and the CPU-baseline leg
+ * of the benchmark).  The product never links it.  Parity of this restatement
+ * with DOMA itself is pinned two ways: bit-for-bit against the committed
+ * golden fixtures (tests/golden/, produced by running DOMA's own code through
+ * oracle/ref_harness.cpp), and live against oracle/_ref/libdoma_ref.so where
+ * the DOMA sources are present.
+ */
+#ifndef DOMA_ORACLE_H
+#define DOMA_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../include/doma_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Quadrature binned by octant; returns the total order, or -1 on bad input. */
+int oracle_quadrature(uint32_t np, uint32_t na, uint32_t dims, double *mu, double *eta,
+                      double *xi, double *w, uint32_t counts[8]);
+
+/* Full fixed-source solve.  phi_out: [G][N].  si_counts receives the SI count
+ * of each (MG iteration, group) pair (up to si_cap entries; *si_len gets the
+ * total).  Returns 1 converged, 0 cap reached, -1 bad input. */
+int oracle_solve(const doma_problem *p, const doma_options *o, uint32_t num_threads,
+                 double *phi_out, uint32_t *si_counts, size_t si_cap, size_t *si_len,
+                 uint32_t *mg_iterations, double *mg_residual);
+
+/* From a zero flux: set up group g's source, then run `count` source
+ * iterations (sweep, residual, update) with no convergence test.  phi_out
+ * ([G][N]) gets the flux afterwards; residuals ([count]) the SI residuals.
+ * This is the bounded CPU-baseline sample.  Returns 0, or -1 on bad input. */
+int oracle_source_iterations(const doma_problem *p, const doma_options *o,
+                             uint32_t num_threads, uint32_t group, uint32_t count,
+                             double *phi_out, double *residuals);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,210 @@
+// ref_harness.cpp -- test infrastructure only.
+//
+// Drives DOMA's own fixed-source solver (the reference, compiled from its
+// unmodified sources by oracle/Makefile into oracle/_ref/libdoma_ref.so) from
+// a doma_problem description, so that the CPU restatement in oracle/ and the
+// GPU library can be pinned against the reference itself.  The product never
+// links or loads this file.
+//
+// What it follows in the reference:
+//   * InputParameters is filled in code instead of from XML
+//     (include/InputParameters.h:50-117), because the XML reader needs pugixml,
+//     which is not available: one x/y/z interval per cell, one block per cell,
+//     block id = material index.
+//   * BrickMesh3D/2D + {DD,TWDD}TransportSolver3D/2D are built exactly as
+//     src/main.cpp:106-292 does, with omp_set_num_threads(T) equal to the T
+//     handed to mesh and solver (src/main.cpp:47).
+//   * The scalar flux is read through TransportSolver3D<OracleTap> /
+//     TransportSolver2D<OracleTap>, explicit specialisations that the mesh and
+//     cell classes befriend (include/BrickMesh3D.h:46-47,
+//     include/CartesianCell3D.h:114-115).
+//   * stdout of the solve (SI/MGI progress lines) is captured and returned.
+
+#include <cstdint>
+#include <cstring>
+#include <iostream>
+#include <sstream>
+#include <string>
+
+#include <omp.h>
+
+#include "TransportSolver2D.h"
+#include "TransportSolver3D.h"
+
+#include "../include/doma_gb300.h"
+
+struct OracleTap {};
+
+template <>
+class TransportSolver3D<OracleTap>
+{
+public:
+  static void readFlux(const BrickMesh3D & mesh, unsigned int G, double * out)
+  {
+    const std::size_t N = mesh._cells.size();
+    for (std::size_t c = 0; c < N; ++c)
+      for (unsigned int g = 0; g < G; ++g)
+        out[g * N + c] = mesh._cells[c]._total_scalar_flux[g];
+  }
+};
+
+template <>
+class TransportSolver2D<OracleTap>
+{
+public:
+  static void readFlux(const BrickMesh2D & mesh, unsigned int G, double * out)
+  {
+    const std::size_t N = mesh._cells.size();
+    for (std::size_t c = 0; c < N; ++c)
+      for (unsigned int g = 0; g < G; ++g)
+        out[g * N + c] = mesh._cells[c]._total_scalar_flux[g];
+  }
+};
+
+namespace
+{
+InputParameters
+makeParams(const doma_problem * p, const doma_options * o)
+{
+  InputParameters params;
+  params._mode = RunMode::FixedSrc;
+  params._num_e_groups = p->num_groups;
+  params._t0 = 0.0;
+  params._t1 = 1.0;
+  params._num_steps = 1u;
+  params._ic = TransientIC::Zero;
+  params._src_it_tol = o->fs_tol;
+  params._gs_tol = o->mg_tol;
+  params._k_tol = 1e-5;
+  params._dsa = false;
+  params._num_src_it = o->fs_max_it;
+  params._num_mg_it = o->mg_max_it;
+  params._num_polar = p->num_polar;
+  params._num_azimuthal = p->num_azimuthal;
+  params._eq_type = o->scheme == DOMA_SCHEME_TW_DD ? EquationType::TW_DD : EquationType::DD;
+  params._num_dims = p->num_dims;
+  params._refinement = 0u;
+
+  params._x_intervals.assign(p->nx, 1u);
+  params._y_intervals.assign(p->ny, 1u);
+  params._dx.assign(p->dx, p->dx + p->nx);
+  params._dy.assign(p->dy, p->dy + p->ny);
+  std::size_t N = std::size_t(p->nx) * p->ny;
+  if (p->num_dims == 3)
+  {
+    params._z_intervals.assign(p->nz, 1u);
+    params._dz.assign(p->dz, p->dz + p->nz);
+    N *= p->nz;
+  }
+  params._blocks.assign(p->cell_material, p->cell_material + N);
+
+  const unsigned int G = p->num_groups;
+  for (unsigned int m = 0; m < p->num_materials; ++m)
+  {
+    MaterialProps mp;
+    mp._num_d_groups = 0u;
+    mp._g_total.assign(p->total + m * G, p->total + (m + 1) * G);
+    mp._g_g_scatter_mat.assign(p->scatter + m * G * G, p->scatter + (m + 1) * G * G);
+    if (p->source)
+      mp._g_src.assign(p->source + m * G, p->source + (m + 1) * G);
+    if (p->has_fission && p->has_fission[m])
+    {
+      mp._g_chi_p.assign(p->chi_p + m * G, p->chi_p + (m + 1) * G);
+      mp._g_prod.assign(p->nu_sigma_f + m * G, p->nu_sigma_f + (m + 1) * G);
+    }
+    params._block_mat_info.emplace(m, mp);
+  }
+  return params;
+}
+
+void
+copyLog(const std::string & s, char * log, std::size_t cap)
+{
+  if (!log || cap == 0)
+    return;
+  const std::size_t n = s.size() < cap - 1 ? s.size() : cap - 1;
+  std::memcpy(log, s.data(), n);
+  log[n] = '\0';
+}
+} // namespace
+
+extern "C" {
+
+// Solve with the reference.  Returns 1 if solveFixedSource returned true, 0 if
+// it returned false.  phi_out receives [G][N].  If out_base is non-empty the
+// reference also writes its text output (BrickMesh3D::dumpToTextFile).
+int
+ref_solve(const doma_problem * p, const doma_options * o, unsigned int num_threads,
+          double * phi_out, char * log, std::size_t log_cap, const char * out_base)
+{
+  omp_set_num_threads(static_cast<int>(num_threads));
+  const InputParameters params = makeParams(p, o);
+  const bool verbose = o->verbose >= 2;
+  const std::string base = out_base ? std::string(out_base) : std::string();
+
+  std::ostringstream captured;
+  std::streambuf * old = std::cout.rdbuf(captured.rdbuf());
+  bool ok = false;
+  if (p->num_dims == 3)
+  {
+    std::array<BoundaryCondition, 6u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh3D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver3D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveFixedSource(base);
+    }
+    else
+    {
+      TWDDTransportSolver3D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveFixedSource(base);
+    }
+    TransportSolver3D<OracleTap>::readFlux(mesh, p->num_groups, phi_out);
+  }
+  else
+  {
+    std::array<BoundaryCondition, 4u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh2D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver2D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveFixedSource(base);
+    }
+    else
+    {
+      TWDDTransportSolver2D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveFixedSource(base);
+    }
+    TransportSolver2D<OracleTap>::readFlux(mesh, p->num_groups, phi_out);
+  }
+  std::cout.rdbuf(old);
+  copyLog(captured.str(), log, log_cap);
+  return ok ? 1 : 0;
+}
+
+// The reference's quadrature, binned by octant: out arrays sized to the total
+// order, octant-major; counts[8] per octant.
+int
+ref_quadrature(unsigned int np, unsigned int na, unsigned int dims, double * mu, double * eta,
+               double * xi, double * w, unsigned int * counts)
+{
+  GCAngularQuadrature q(2u * na, 2u * np, dims);
+  std::size_t k = 0;
+  for (unsigned int o = 0; o < 8u; ++o)
+  {
+    const Octant oct = static_cast<Octant>(o);
+    counts[o] = q.order(oct);
+    for (unsigned int n = 0; n < q.order(oct); ++n, ++k)
+    {
+      q.direction(oct, n, mu[k], eta[k], xi[k]);
+      w[k] = q.weight(oct, n);
+    }
+  }
+  return static_cast<int>(k);
+}
+
+} // extern "C"

@@ -1,0 +1,109 @@
+"""Generate the golden fixtures by running DOMA's own code.
+
+Run from the repository root where the DOMA source tree is present:
+
+    make -C oracle ref        # builds oracle/_ref/libdoma_ref.so from DOMA's sources
+    python tests/golden/make_golden.py
+
+Each case is a seeded synthetic problem (doma_gb300.problems) solved by DOMA
+(single thread, the bit-reproducible order).  A fixture stores the generator
+call, the SHA-256 digest of the regenerated inputs, the options, DOMA's scalar
+flux, its return value and the source-iteration counts it printed.  The
+quadrature file stores DOMA's direction cosines and weights.
+"""
+from __future__ import annotations
+
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+import oracle_lib as ol  # noqa: E402
+from doma_gb300 import problems as P  # noqa: E402
+
+HERE = Path(__file__).resolve().parent
+
+# name -> (generator, kwargs, options kwargs)
+CASES = {
+    "small_cube_dd": ("small_cube", {"seed": 0, "n": 20}, {"scheme": "dd"}),
+    "small_cube_twdd": ("small_cube", {"seed": 0, "n": 20}, {"scheme": "tw_dd", "theta": 0.9}),
+    "random3d_fission_dd": ("random_problem",
+                            {"seed": 3, "dims": 3, "nx": 7, "ny": 6, "nz": 5, "groups": 3,
+                             "np_": 2, "na": 2, "materials": 4, "fission": True},
+                            {"scheme": "dd", "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    "random3d_fission_twdd": ("random_problem",
+                              {"seed": 3, "dims": 3, "nx": 7, "ny": 6, "nz": 5, "groups": 3,
+                               "np_": 2, "na": 2, "materials": 4, "fission": True},
+                              {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-10,
+                               "mg_tol": 1e-10}),
+    "random2d_dd": ("random_problem",
+                    {"seed": 5, "dims": 2, "nx": 9, "ny": 7, "groups": 3, "np_": 2, "na": 3,
+                     "materials": 3, "fission": True},
+                    {"scheme": "dd", "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    "random2d_twdd": ("random_problem",
+                      {"seed": 5, "dims": 2, "nx": 9, "ny": 7, "groups": 3, "np_": 2, "na": 3,
+                       "materials": 3, "fission": True},
+                      {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    "square2d_dd": ("square_2d", {"seed": 1, "n": 24, "groups": 2}, {"scheme": "dd"}),
+    "square2d_twdd": ("square_2d", {"seed": 1, "n": 24, "groups": 2},
+                      {"scheme": "tw_dd", "theta": 0.9}),
+    "checkerboard_n16_twdd": ("checkerboard",
+                              {"seed": 0, "n": 16, "groups": 8, "np_": 4, "na": 4, "block": 4},
+                              {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-6,
+                               "mg_tol": 1e-6}),
+    "checkerboard_n16_dd": ("checkerboard",
+                            {"seed": 0, "n": 16, "groups": 8, "np_": 4, "na": 4, "block": 4},
+                            {"scheme": "dd", "fs_tol": 1e-6, "mg_tol": 1e-6}),
+    "streaming_n24_dd": ("streaming_duct",
+                         {"seed": 0, "n": 24, "np_": 3, "na": 3, "width": 4, "src": 4},
+                         {"scheme": "dd", "fs_tol": 1e-8, "mg_tol": 1e-8}),
+    "capped_si_twdd": ("small_cube", {"seed": 2, "n": 12},
+                       {"scheme": "tw_dd", "theta": 0.9, "fs_max_it": 3}),
+    "capped_mg_dd": ("random_problem",
+                     {"seed": 7, "dims": 3, "nx": 6, "ny": 5, "nz": 4, "groups": 4, "np_": 1,
+                      "na": 2, "materials": 3},
+                     {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-12, "mg_max_it": 2}),
+}
+
+QUAD_SETS = [(dims, np_, na) for dims in (2, 3)
+             for (np_, na) in [(1, 1), (2, 2), (3, 3), (4, 4), (6, 6), (2, 5), (5, 2)]]
+
+
+def make_problem(gen: str, kwargs: dict) -> P.Problem:
+    return getattr(P, gen)(**kwargs)
+
+
+def main() -> None:
+    if not ol.ref_available():
+        raise SystemExit("oracle/_ref/libdoma_ref.so is missing: run `make -C oracle ref` first")
+    quad = {}
+    for dims, np_, na in QUAD_SETS:
+        mu, eta, xi, w, counts = ol.ref_quadrature(np_, na, dims)
+        key = f"d{dims}_np{np_}_na{na}"
+        quad[key + "_mu"], quad[key + "_eta"], quad[key + "_xi"] = mu, eta, xi
+        quad[key + "_w"], quad[key + "_counts"] = w, counts
+    np.savez_compressed(HERE / "quadrature.npz", **quad)
+    print("quadrature.npz", len(QUAD_SETS), "sets")
+
+    for name, (gen, kw, okw) in CASES.items():
+        p = make_problem(gen, kw)
+        opts = P.make_options(**okw)
+        t0 = time.time()
+        phi, ok, si, mg, _log = ol.ref_solve(p, opts, threads=1)
+        dt = time.time() - t0
+        meta = {"generator": gen, "kwargs": kw, "options": okw, "digest": p.digest(),
+                "converged": ok, "mg_iterations": mg, "reference_seconds": round(dt, 3)}
+        np.savez_compressed(HERE / f"{name}.npz", phi=phi, si_counts=si,
+                            meta=np.array(json.dumps(meta)))
+        print(f"{name:28s} converged={ok} mg={mg} si={list(map(int, si))[:8]}... "
+              f"{dt:.2f}s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,39 @@
+"""Loading of the committed golden fixtures (tests/golden/*.npz)."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+from doma_gb300 import problems as P
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def case_names():
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "quadrature")
+
+
+def load_case(name: str):
+    """-> (problem, options, expected dict)"""
+    z = np.load(GOLDEN / f"{name}.npz")
+    meta = json.loads(str(z["meta"]))
+    p = getattr(P, meta["generator"])(**meta["kwargs"])
+    if p.digest() != meta["digest"]:
+        raise AssertionError(f"{name}: regenerated inputs differ from the fixture's")
+    opts = P.make_options(**meta["options"])
+    exp = {"phi": z["phi"], "si_counts": z["si_counts"], "converged": meta["converged"],
+           "mg_iterations": meta["mg_iterations"], "meta": meta}
+    return p, opts, exp
+
+
+def quadrature_sets():
+    z = np.load(GOLDEN / "quadrature.npz")
+    keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
+    out = []
+    for k in keys:
+        d, n_p, n_a = k.split("_")
+        out.append((int(d[1:]), int(n_p[2:]), int(n_a[2:]), z[k + "_mu"], z[k + "_eta"],
+                    z[k + "_xi"], z[k + "_w"], z[k + "_counts"]))
+    return out

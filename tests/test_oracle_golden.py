@@ -1,0 +1,49 @@
+"""Pin the CPU restatement (oracle/doma_oracle.c) to DOMA itself.
+
+The golden fixtures were produced by running DOMA's own solver on seeded
+synthetic problems (tests/golden/make_golden.py).  The restatement must
+reproduce them bit for bit: scalar flux, return value and every
+source-iteration count.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+from golden_cases import case_names, load_case, quadrature_sets
+
+
+@pytest.mark.parametrize("dims,np_,na,mu,eta,xi,w,counts", quadrature_sets())
+def test_quadrature_matches_reference(dims, np_, na, mu, eta, xi, w, counts):
+    m, e, x, ww, c = ol.oracle_quadrature(np_, na, dims)
+    assert np.array_equal(c, counts)
+    for a, b in ((m, mu), (e, eta), (x, xi), (ww, w)):
+        assert np.array_equal(a, b)
+    assert abs(w.sum() - (4 * np.pi if dims == 3 else 2 * np.pi)) < 1e-12
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_oracle_bitwise_equals_reference(name):
+    p, opts, exp = load_case(name)
+    phi, ok, si, mg, _ = ol.oracle_solve(p, opts, threads=1)
+    assert ok == exp["converged"]
+    assert list(si) == list(exp["si_counts"])
+    if exp["mg_iterations"] is not None:
+        assert mg == exp["mg_iterations"]
+    assert np.array_equal(phi, exp["phi"]), np.abs(phi - exp["phi"]).max()
+
+
+def test_oracle_threads_agree():
+    """The OpenMP split over ordinates changes only the summation order."""
+    p, opts, exp = load_case("small_cube_twdd")
+    phi, ok, si, _, _ = ol.oracle_solve(p, opts, threads=3)
+    assert ok and list(si) == list(exp["si_counts"])
+    rel = np.abs(phi - exp["phi"]).max() / np.abs(exp["phi"]).max()
+    assert rel < 1e-13
+
+
+def test_oracle_rejects_bad_input():
+    from doma_gb300 import problems as P
+    p = P.random_problem(0, 3, 3, 3, 3, groups=2)
+    p.cell_material[0] = 99
+    with pytest.raises(ValueError):
+        ol.oracle_solve(p, P.make_options())
