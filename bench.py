@@ -1,0 +1,360 @@
+"""Benchmark of the fixed-source sweep / source-iteration hot path on GB300.
+
+Workload (one step = one complete fixed-source solve, Gauss-Seidel over
+groups wrapping source iteration wrapping 8-octant sweeps, from a zero flux
+to the tolerance): a 64^3 mesh of 1 cm cells, 8 groups, Gauss-Chebyshev
+8 polar x 16 azimuthal = 128 directions, theta-weighted diamond difference
+with theta = 0.7, four materials in a seeded checkerboard of 8^3 blocks
+(sigma_t lognormal, median 1/cm; c ~ U[0.5, 0.95]; lower-triangular
+scattering plus upscatter between the last two groups), unit group-0 source
+in one seeded 8^3 block, vacuum boundaries.  Synthetic inputs from the seeded
+generator in doma_gb300.problems.
+
+metric: cell * direction * group updates per second (Gupdates/s) over whole
+solves; the sweep runs in FP32 with compensated angular sums, sources,
+fluxes and every norm in FP64.
+
+  value     device-resident: the solver is created once; each step re-zeroes
+            the flux and solves.  CUDA events on the solver's stream around
+            each step; L2 is flushed (a 512 MB write) between steps.
+  e2e       through the C ABI with host buffers: create (H2D of the problem),
+            solve, read the flux back (D2H), destroy -- wall clock per step.
+  roofline  the sweep kernels alone (bare sweeps of group 0), achieved
+            algorithmic bytes (6 s + 3 s / D_oct per update, s = 4) per second
+            against the measured HBM copy bandwidth.
+  cpu_baseline  the CPU restatement of DOMA's OpenMP sweep (oracle/) on the
+            host cores, a bounded sample of source iterations of group 0.
+
+--impl reference runs DOMA's CPU algorithm (the oracle port, the reference's
+own code cannot be compiled on this host) on the same workload and metric.
+Replicas only: with --gpus N each rank solves its own replica (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "sweep Gupdates/s over full fixed-source solves (time to tolerance per step)"
+UNIT = "Gupdates/s"
+
+
+def workload(seed: int = 0, n: int = 64):
+    from doma_gb300 import problems as P
+    p = P.checkerboard(seed, n=n, groups=8, np_=4, na=4, block=8)
+    return p
+
+
+def options(precision: str = "fp32", tol: float = 1e-8):
+    from doma_gb300 import problems as P
+    return P.make_options(scheme="tw_dd", theta=0.7, precision=precision, fs_tol=tol,
+                          fs_max_it=5000, mg_tol=tol, mg_max_it=500)
+
+
+def config_dict(p, args, extra=None):
+    d = {"workload": "checkerboard_64cube_8g_128dir_twdd_theta0.7",
+         "cells": p.num_cells, "groups": p.num_groups, "directions": p.num_directions,
+         "scheme": "tw_dd", "theta": 0.7, "tolerance": args.tol,
+         "l2": "flushed between steps (512 MB write)", "parallelism": "replicas"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"doma_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_sample(p, opts, threads: int, iters: int):
+    """Time `iters` source iterations of group 0 with the CPU restatement."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as ol
+    ol.oracle()  # build/load before timing
+    t0 = time.perf_counter()
+    ol.oracle_source_iterations(p, opts, 0, iters, threads=threads)
+    dt = time.perf_counter() - t0
+    upd = iters * p.updates_per_sweep()
+    return upd / dt / 1e9, dt, upd
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from doma_gb300 import problems as P  # noqa: F401
+    p = workload(args.seed)
+    opts = options("fp64", args.tol)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_sample(p, opts, threads, 1)
+    times, upds = [], []
+    for _ in range(args.steps):
+        rate, dt, upd = cpu_sample(p, opts, threads, args.ref_iters)
+        times.append(dt)
+        upds.append(upd)
+    value = sum(upds) / sum(times) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(p, args, {"sample": f"{args.ref_iters} source iterations of group 0 per step"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.ref_iters} source iterations (sweep + residual + update) "
+                                   f"of group 0 per step, {threads} OpenMP threads over the "
+                                   f"ordinates of each octant (DOMA's parallel-in-angle scheme)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from doma_gb300.solver import Solver
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    p = workload(args.seed + rank)
+    opts = options(args.precision, args.tol)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # -- device-resident leg ------------------------------------------------
+    solver = Solver(p, opts)
+    solver.set_stream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        rep = solver.solve_fixed_source()
+        assert rep.converged, "warm-up solve did not converge"
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms, updates, launches = [], 0, 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rep = solver.solve_fixed_source()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            updates += rep.updates
+            launches += rep.kernel_launches
+            assert rep.converged
+    torch.cuda.synchronize()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        u = torch.tensor([float(updates)], device=dev)
+        dist.all_reduce(u)
+        updates_all = float(u.item())
+    else:
+        updates_all = float(updates)
+    value = updates_all / (total_ms / 1e3) / 1e9
+    last_rep = rep
+    phi32 = solver.scalar_flux()
+
+    # -- roofline: the sweep kernels alone ------------------------------------
+    solver.source_iterations(0, 1)
+    nsw = args.roofline_sweeps
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.sweeps(0, nsw)
+    e1.record(stream)
+    e1.synchronize()
+    sweep_ms = e0.elapsed_time(e1) / nsw
+    desc = solver.describe()
+    s_bytes = 4 if args.precision == "fp32" else 8
+    d_oct = p.directions_per_octant
+    b_upd = 6 * s_bytes + 3 * s_bytes / d_oct
+    upd_sweep = p.updates_per_sweep()
+    achieved = b_upd * upd_sweep / (sweep_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    solver.close()
+
+    # -- FP64 drop-in reference solution and its rate ----------------------------
+    err = None
+    fp64_rate = None
+    if args.fp64_check:
+        with Solver(p, options("fp64", args.tol)) as s64:
+            s64.set_stream(stream.cuda_stream)
+            t0 = time.perf_counter()
+            r64 = s64.solve_fixed_source()
+            torch.cuda.synchronize()
+            dt64 = time.perf_counter() - t0
+            phi64 = s64.scalar_flux()
+        fp64_rate = r64.updates / dt64 / 1e9
+        err = float(np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64))
+
+    # -- e2e through the C ABI with host buffers ---------------------------------
+    h2d = (p.dx.nbytes + p.dy.nbytes + p.dz.nbytes + p.cell_material.nbytes + p.total.nbytes
+           + p.scatter.nbytes + (p.source.nbytes if p.source is not None else 0))
+    d2h = p.num_groups * p.num_cells * 8
+    e2e_times, e2e_upd = [], 0
+    for i in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with Solver(p, opts) as s:
+            r = s.solve_fixed_source()
+            _ = s.scalar_flux()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_upd += r.updates
+    e2e_value = e2e_upd / sum(e2e_times) / 1e9 * world
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, dt, upd = cpu_sample(p, options("fp64", args.tol), threads, args.ref_iters)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.ref_iters} source iterations of group 0 ({upd / 1e6:.1f} M updates, "
+                         f"{dt:.1f} s), {threads} OpenMP threads over ordinates"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+        "config": config_dict(p, args, {"precision": args.precision,
+                                        "tile": list(desc["tile"]),
+                                        "si_sweeps_per_solve": last_rep.si_iterations,
+                                        "mg_iterations": last_rep.mg_iterations}),
+        "time_to_tolerance_ms": total_ms / args.steps,
+        "error_vs_fp64_rel_l2": err,
+        "fp64_dropin_gupdates": fp64_rate,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind,
+                     "bytes_per_update": b_upd, "sweep_ms": sweep_ms,
+                     "sweep_launches": desc["launches_per_sweep"]},
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--roofline-sweeps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--ref-iters", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-check", type=int, default=1)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+// iteration.cu -- per-cell kernels around the sweep: the multigroup source,
+// the source-iteration epilogue (angular reduction, residual, increment
+// update) and the Gauss-Seidel residual.
+//
+// Replaces updateMultigroupSource (src/TransportSolver3D.cpp:339-402, fixed-
+// source terms), the thread reduction at the end of sweep (:610-621),
+// computeScatteringResidual (:547-563), updateScatteringSource (:531-545) and
+// computeMGFluxResidual (:318-337), with their 2D twins.  Sources and fluxes
+// are double in every mode and use DOMA's association with unfused,
+// correctly rounded operations.
+//
+// Norms are reduced deterministically without floating-point atomics: each
+// thread owns a fixed set of cells (fixed grid, grid-stride), blocks reduce
+// with a fixed shuffle tree, block partials go to a buffer, and the last block
+// to finish (one integer ticket) sums the partials in block order.
+#include "common.cuh"
+#include "iteration.cuh"
+
+namespace doma {
+namespace {
+
+__device__ __forceinline__ double dA(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dS(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dM(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dD(double a, double b) { return __ddiv_rn(a, b); }
+
+constexpr int kBlock = 256;
+
+// Fixed-order block sum of two values; the result is valid in thread 0.
+__device__ __forceinline__ void block_sum2(double & a, double & b)
+{
+  __shared__ double sh[2][kBlock / 32];
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, off);
+    b += __shfl_down_sync(0xffffffffu, b, off);
+  }
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (lane == 0) {
+    sh[0][warp] = a;
+    sh[1][warp] = b;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < kBlock / 32 ? sh[0][lane] : 0.0;
+    b = lane < kBlock / 32 ? sh[1][lane] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+  }
+  __syncthreads();
+}
+
+// Store this block's partial pair; the last block sums all pairs in block
+// order into out[0..1] and re-arms the ticket.
+__device__ __forceinline__ void finish_norms(double a, double b, double * partials,
+                                             unsigned * ticket, double * out)
+{
+  __shared__ bool last;
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = a;
+    partials[2 * blockIdx.x + 1] = b;
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double sa = 0.0, sb = 0.0;
+  for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+    sa += __ldcg(partials + 2 * k);
+    sb += __ldcg(partials + 2 * k + 1);
+  }
+  block_sum2(sa, sb);
+  if (threadIdx.x == 0) {
+    out[0] = sa;
+    out[1] = sb;
+    *ticket = 0u;
+  }
+}
+
+// updateMultigroupSource for group g (fixed source: external, in-scatter and
+// prompt fission); also saves the previous iterate, zeroes phi_g and stages
+// the sweep inputs (q and sigma_t of group g in the sweep's precision).
+template <typename T>
+__global__ void __launch_bounds__(kBlock) mg_source_kernel(const IterArgs A, int g, T * q_out,
+                                                          T * sigt_out)
+{
+  const size_t N = A.N;
+  const int G = A.G;
+  const double s = A.src_scale;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const unsigned m = A.mat[c];
+    double q = A.source ? dD(dM(s, A.source[(size_t)m * G + g]), kPi) : 0.0;
+    const bool fis = A.fis && A.fis[m];
+    for (int gp = 0; gp < G; ++gp) {
+      const double pg = A.phi[(size_t)gp * N + c];
+      if (gp != g) q = dA(q, dD(dM(dM(s, A.scatter[((size_t)m * G + g) * G + gp]), pg), kPi));
+      if (fis)
+        q = dA(q, dD(dM(dM(dM(s, A.chi[(size_t)m * G + g]), A.nsf[(size_t)m * G + gp]), pg), kPi));
+    }
+    q_out[c] = (T)q;
+    sigt_out[c] = (T)A.total[(size_t)m * G + g];
+    A.prev[(size_t)g * N + c] = A.phi[(size_t)g * N + c];
+    A.phi[(size_t)g * N + c] = 0.0;
+  }
+}
+
+// The source-iteration epilogue for group g:
+//   dphi = sum of the swept angular flux (exact: all ordinates in DOMA's
+//          single-thread order; fp32: the octant partials in octant order)
+//   diff += dphi^2 V, total += (phi + dphi)^2 V   (residual, before the update)
+//   phi += dphi;  q = s * S_gg * dphi / pi       (the next increment's source)
+template <typename T, bool EXACT>
+__global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, int g, T * q_out,
+                                                            double * norms)
+{
+  const size_t N = A.N;
+  const int G = A.G;
+  double diff = 0.0, tot = 0.0;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    double d = 0.0;
+    if (EXACT) {
+      const double * w = A.wpsi + c * (size_t)A.D;
+      for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
+    } else {
+      for (int o = 0; o < 8; ++o)
+        if (A.oct_mask & (1 << o)) d = dA(d, A.octphi[(size_t)o * N + c]);
+    }
+    const double V = A.vol[c];
+    double * ph = A.phi + (size_t)g * N + c;
+    const double t = dA(*ph, d);
+    diff = dA(diff, dM(dM(d, d), V));
+    tot = dA(tot, dM(dM(t, t), V));
+    *ph = t;
+    const unsigned m = A.mat[c];
+    q_out[c] = (T)dD(dM(dM(A.src_scale, A.scatter[((size_t)m * G + g) * G + g]), d), kPi);
+  }
+  finish_norms(diff, tot, A.partials, A.ticket, norms);
+}
+
+// computeMGFluxResidual: sums over cells and groups of (phi - prev)^2 V and phi^2 V.
+__global__ void __launch_bounds__(kBlock) mg_residual_kernel(const IterArgs A, double * norms)
+{
+  const size_t N = A.N;
+  double diff = 0.0, tot = 0.0;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const double V = A.vol[c];
+    for (int g = 0; g < A.G; ++g) {
+      const double a = A.phi[(size_t)g * N + c];
+      const double d = dS(a, A.prev[(size_t)g * N + c]);
+      diff = dA(diff, dM(dM(d, d), V));
+      tot = dA(tot, dM(dM(a, a), V));
+    }
+  }
+  finish_norms(diff, tot, A.partials, A.ticket, norms);
+}
+
+}  // namespace
+
+doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q, void * sigt,
+                             cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    mg_source_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, (double *)sigt);
+  else
+    mg_source_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, (float *)sigt);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * q,
+                               double * norms, cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    si_epilogue_kernel<double, true><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, norms);
+  else
+    si_epilogue_kernel<float, false><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, norms);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_mg_residual(const IterArgs & a, double * norms, cudaStream_t st)
+{
+  mg_residual_kernel<<<a.grid, kBlock, 0, st>>>(a, norms);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+int iteration_block() { return kBlock; }
+
+}  // namespace doma

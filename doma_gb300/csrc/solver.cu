@@ -1,0 +1,635 @@
+// solver.cu -- the C ABI: solver handle, device buffers, and the
+// Gauss-Seidel / source-iteration driver.
+//
+// The driver follows TransportSolver3D::solveFixedSource
+// (src/TransportSolver3D.cpp:262-316) and ::sourceIteration (:458-497) step by
+// step, including their exit rules: SI stops when it reaches fs_max_it or the
+// residual is <= fs_tol and succeeds iff it < fs_max_it; the Gauss-Seidel loop
+// runs once for one group and succeeds iff mg_it < mg_max_it; a norm whose
+// total is <= 1e-8 gives residual 0.  One deliberate difference: a NaN or
+// infinite norm stops the solve with DOMA_NUMERIC_ERROR (DOMA would report
+// convergence, because `tol < NaN` is false).
+//
+// Device layout (one solver = one problem, all resident in HBM):
+//   per cell   : material index, volume, q and sigma_t of the current group
+//                (sweep precision), the increment's octant partials (fp32:
+//                [8][N] double) or the weighted angular flux (exact: [N][D] double)
+//   per group  : phi and the previous Gauss-Seidel iterate, [G][N] double
+//   per octant : face planes x [nz][ny][Do], y [nz][nx][Do], z [ny][nx][Do]
+//   materials  : total [M][G], scatter [M][G][G], source, fission data
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "iteration.cuh"
+
+namespace doma {
+
+namespace {
+thread_local std::string g_error;
+}
+
+void set_error(const std::string & msg) { g_error = msg; }
+const char * get_error() { return g_error.c_str(); }
+
+}  // namespace doma
+
+using namespace doma;
+
+struct doma_solver {
+  int dims = 3, nx = 1, ny = 1, nz = 1, G = 1, M = 1;
+  size_t N = 0;
+  int D = 0, d_oct = 0;
+  unsigned oct_mask = 0;
+  doma_options opts{};
+  int offs[8] = {0};
+
+  // device buffers
+  double *d_dx = nullptr, *d_dy = nullptr, *d_dz = nullptr, *d_vol = nullptr;
+  uint32_t * d_mat = nullptr;
+  double *d_total = nullptr, *d_scatter = nullptr, *d_source = nullptr;
+  uint8_t * d_fis = nullptr;
+  double *d_chi = nullptr, *d_nsf = nullptr;
+  double *d_amu = nullptr, *d_aeta = nullptr, *d_axi = nullptr, *d_w = nullptr;
+  float *d_amu_f = nullptr, *d_aeta_f = nullptr, *d_axi_f = nullptr;
+  int * d_oct_offset = nullptr;
+  double *d_phi = nullptr, *d_prev = nullptr;
+  void *d_q = nullptr, *d_sigt = nullptr;
+  void *d_xf = nullptr, *d_yf = nullptr, *d_zf = nullptr;
+  double * d_wpsi = nullptr;
+  double * d_octphi = nullptr;
+  double * d_partials = nullptr;
+  unsigned * d_ticket = nullptr;
+  double * d_norms = nullptr;  // [4]: SI (diff, total), MG (diff, total)
+  Task * d_tasks = nullptr;
+  double * h_norms = nullptr;  // pinned [4]
+
+  Schedule sched;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  uint64_t launches = 0;
+  int device = 0;
+
+  SweepArgs<double> a64{};
+  SweepArgs<float> a32{};
+  IterArgs it{};
+  std::vector<void *> allocations;
+};
+
+namespace {
+
+template <typename T>
+doma_status dalloc(doma_solver * s, T ** p, size_t count)
+{
+  *p = nullptr;
+  if (count == 0) return DOMA_OK;
+  void * v = nullptr;
+  cudaError_t e = cudaMalloc(&v, count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) +
+              " bytes): " + cudaGetErrorString(e));
+    return DOMA_CUDA_ERROR;
+  }
+  s->allocations.push_back(v);
+  *p = static_cast<T *>(v);
+  return DOMA_OK;
+}
+
+template <typename T>
+doma_status upload(doma_solver * s, T ** p, const T * host, size_t count)
+{
+  doma_status st = dalloc(s, p, count);
+  if (st != DOMA_OK || count == 0) return st;
+  DOMA_CUDA_TRY(cudaMemcpy(*p, host, count * sizeof(T), cudaMemcpyHostToDevice));
+  return DOMA_OK;
+}
+
+#define DOMA_TRY(expr)                    \
+  do {                                    \
+    doma_status _s = (expr);              \
+    if (_s != DOMA_OK) return _s;         \
+  } while (0)
+
+doma_status bad(const std::string & msg)
+{
+  set_error(msg);
+  return DOMA_BAD_INPUT;
+}
+
+doma_status validate(const doma_problem * p, const doma_options * o)
+{
+  if (!p || !o) return bad("null problem or options");
+  if (p->num_dims != 2 && p->num_dims != 3) return bad("num_dims must be 2 or 3");
+  if (p->nx == 0 || p->ny == 0 || p->nz == 0) return bad("empty mesh");
+  if (p->num_dims == 2 && p->nz != 1) return bad("a 2D problem needs nz == 1");
+  if (!p->dx || !p->dy || (p->num_dims == 3 && !p->dz)) return bad("missing cell widths");
+  if (p->num_groups == 0) return bad("num_groups must be positive");
+  if (p->num_materials == 0) return bad("num_materials must be positive");
+  if (!p->cell_material || !p->total || !p->scatter) return bad("missing material data");
+  if (p->has_fission && (!p->chi_p || !p->nu_sigma_f))
+    return bad("has_fission given without chi_p / nu_sigma_f");
+  if (p->num_polar == 0 || p->num_azimuthal == 0) return bad("np and na must be positive");
+  if ((uint64_t)p->num_polar * p->num_azimuthal > (uint64_t)kMaxSweepThreads)
+    return bad("np*na (ordinates per octant) must be <= " + std::to_string(kMaxSweepThreads));
+  const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
+  if (N > (1ull << 31)) return bad("too many cells");
+  for (uint64_t c = 0; c < N; ++c)
+    if (p->cell_material[c] >= p->num_materials)
+      return bad("cell " + std::to_string(c) + " has material " +
+                 std::to_string(p->cell_material[c]) + " >= num_materials");
+  auto positive = [](const double * v, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+      if (!(v[i] > 0.0) || !std::isfinite(v[i])) return false;
+    return true;
+  };
+  if (!positive(p->dx, p->nx) || !positive(p->dy, p->ny) ||
+      (p->num_dims == 3 && !positive(p->dz, p->nz)))
+    return bad("cell widths must be positive and finite");
+  if (o->scheme != DOMA_SCHEME_DD && o->scheme != DOMA_SCHEME_TW_DD) return bad("unknown scheme");
+  if (o->precision != DOMA_PREC_FP64 && o->precision != DOMA_PREC_FP32)
+    return bad("unknown precision");
+  if (!(o->theta >= 0.0 && o->theta <= 1.0)) return bad("theta must lie in [0, 1]");
+  return DOMA_OK;
+}
+
+// Block shape: aim at ~256 threads (ordinates x pencils) per CTA.
+void pick_tile(doma_solver * s, const doma_options * o)
+{
+  int tx = o->tile_x, ty = o->tile_y, tz = o->tile_z;
+  const int pencils = s->d_oct >= 256 ? 1 : 256 / s->d_oct;
+  if (s->dims == 3) {
+    if (!ty || !tz) {
+      int a = 1, b = 1;
+      while (a * b * 2 <= pencils) {
+        if (a <= b) a *= 2; else b *= 2;
+      }
+      ty = ty ? ty : a;
+      tz = tz ? tz : b;
+    }
+    if (!tx) tx = 16;
+  } else {
+    tz = 1;
+    if (!ty) {
+      int a = 1;
+      while (a * 2 <= pencils) a *= 2;
+      ty = a;
+    }
+    if (!tx) tx = 32;
+  }
+  tx = std::max(1, std::min(tx, s->nx));
+  ty = std::max(1, std::min(ty, s->ny));
+  tz = std::max(1, std::min(tz, s->nz));
+  // keep the CTA within kMaxSweepThreads and the shared memory within 200 KB
+  while (s->d_oct * ty * tz > kMaxSweepThreads && (ty > 1 || tz > 1)) {
+    if (ty >= tz) ty = (ty + 1) / 2; else tz = (tz + 1) / 2;
+  }
+  while (tx > 1 && sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, tx, ty, tz,
+                                    s->d_oct) > 200 * 1024)
+    tx = (tx + 1) / 2;
+  s->sched.tx = tx;
+  s->sched.ty = ty;
+  s->sched.tz = tz;
+}
+
+void build_schedule(doma_solver * s)
+{
+  Schedule & sc = s->sched;
+  sc.nbx = (s->nx + sc.tx - 1) / sc.tx;
+  sc.nby = (s->ny + sc.ty - 1) / sc.ty;
+  sc.nbz = (s->nz + sc.tz - 1) / sc.tz;
+  sc.threads = s->d_oct * sc.ty * sc.tz;
+  sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx, sc.ty, sc.tz,
+                             s->d_oct);
+  const int levels = sc.nbx + sc.nby + sc.nbz - 2;
+  std::vector<std::vector<Task>> by_level(levels);
+  for (int o = 0; o < 8; ++o) {
+    if (!(s->oct_mask & (1u << o))) continue;
+    for (int bk = 0; bk < sc.nbz; ++bk)
+      for (int bj = 0; bj < sc.nby; ++bj)
+        for (int bi = 0; bi < sc.nbx; ++bi) by_level[bi + bj + bk].push_back(Task{o, bi, bj, bk});
+  }
+  sc.tasks.clear();
+  sc.level_begin.assign(1, 0);
+  for (auto & lv : by_level) {
+    sc.tasks.insert(sc.tasks.end(), lv.begin(), lv.end());
+    sc.level_begin.push_back((int)sc.tasks.size());
+  }
+}
+
+doma_status create_impl(const doma_problem * p, const doma_options * o, doma_solver * s)
+{
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    set_error("no CUDA device is visible");
+    return DOMA_NO_DEVICE;
+  }
+  DOMA_CUDA_TRY(cudaGetDevice(&s->device));
+  s->opts = *o;
+  s->dims = (int)p->num_dims;
+  s->nx = (int)p->nx;
+  s->ny = (int)p->ny;
+  s->nz = s->dims == 3 ? (int)p->nz : 1;
+  s->G = (int)p->num_groups;
+  s->M = (int)p->num_materials;
+  s->N = (size_t)s->nx * s->ny * s->nz;
+  s->d_oct = (int)(p->num_polar * p->num_azimuthal);
+  s->D = (s->dims == 3 ? 8 : 4) * s->d_oct;
+
+  std::vector<double> mu(s->D), eta(s->D), xi(s->D), w(s->D);
+  unsigned counts[8];
+  if (gc_quadrature(p->num_polar, p->num_azimuthal, p->num_dims, mu.data(), eta.data(),
+                    xi.data(), w.data(), counts) != s->D)
+    return bad("quadrature construction failed");
+  int off = 0;
+  for (int oc = 0; oc < 8; ++oc) {
+    s->offs[oc] = off;
+    off += (int)counts[oc];
+    if (counts[oc]) {
+      s->oct_mask |= 1u << oc;
+      if ((int)counts[oc] != s->d_oct) return bad("unexpected octant size");
+    }
+  }
+  std::vector<double> amu(s->D), aeta(s->D), axi(s->D);
+  std::vector<float> amu_f(s->D), aeta_f(s->D), axi_f(s->D);
+  for (int n = 0; n < s->D; ++n) {
+    amu[n] = std::abs(mu[n]);
+    aeta[n] = std::abs(eta[n]);
+    axi[n] = std::abs(xi[n]);
+    amu_f[n] = (float)amu[n];
+    aeta_f[n] = (float)aeta[n];
+    axi_f[n] = (float)axi[n];
+  }
+
+  // geometry and materials
+  const size_t N = s->N, G = s->G, M = s->M;
+  std::vector<double> dz(s->nz, 1.0);
+  if (s->dims == 3) dz.assign(p->dz, p->dz + s->nz);
+  std::vector<double> vol(N);
+  for (int k = 0; k < s->nz; ++k)
+    for (int j = 0; j < s->ny; ++j)
+      for (int i = 0; i < s->nx; ++i) {
+        const size_t c = ((size_t)k * s->ny + j) * s->nx + i;
+        vol[c] = s->dims == 3 ? p->dx[i] * p->dy[j] * dz[k] : p->dx[i] * p->dy[j];
+      }
+  DOMA_TRY(upload(s, &s->d_dx, p->dx, (size_t)s->nx));
+  DOMA_TRY(upload(s, &s->d_dy, p->dy, (size_t)s->ny));
+  DOMA_TRY(upload(s, &s->d_dz, dz.data(), (size_t)s->nz));
+  DOMA_TRY(upload(s, &s->d_vol, vol.data(), N));
+  DOMA_TRY(upload(s, &s->d_mat, p->cell_material, N));
+  DOMA_TRY(upload(s, &s->d_total, p->total, M * G));
+  DOMA_TRY(upload(s, &s->d_scatter, p->scatter, M * G * G));
+  if (p->source) DOMA_TRY(upload(s, &s->d_source, p->source, M * G));
+  if (p->has_fission) {
+    DOMA_TRY(upload(s, &s->d_fis, p->has_fission, M));
+    DOMA_TRY(upload(s, &s->d_chi, p->chi_p, M * G));
+    DOMA_TRY(upload(s, &s->d_nsf, p->nu_sigma_f, M * G));
+  }
+  DOMA_TRY(upload(s, &s->d_amu, amu.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_aeta, aeta.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_axi, axi.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_w, w.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_amu_f, amu_f.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_aeta_f, aeta_f.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_axi_f, axi_f.data(), (size_t)s->D));
+  DOMA_TRY(upload(s, &s->d_oct_offset, s->offs, 8));
+
+  // state
+  const bool exact = o->precision == DOMA_PREC_FP64;
+  const size_t ts = exact ? sizeof(double) : sizeof(float);
+  DOMA_TRY(dalloc(s, &s->d_phi, G * N));
+  DOMA_TRY(dalloc(s, &s->d_prev, G * N));
+  unsigned char * qb = nullptr;
+  DOMA_TRY(dalloc(s, &qb, 2 * N * ts));
+  s->d_q = qb;
+  s->d_sigt = qb + N * ts;
+  const size_t Do = s->d_oct;
+  unsigned char * fb = nullptr;
+  const size_t xf = 8 * (size_t)s->nz * s->ny * Do, yf = 8 * (size_t)s->nz * s->nx * Do,
+               zf = 8 * (size_t)s->ny * s->nx * Do;
+  DOMA_TRY(dalloc(s, &fb, (xf + yf + zf) * ts));
+  s->d_xf = fb;
+  s->d_yf = fb + xf * ts;
+  s->d_zf = fb + (xf + yf) * ts;
+  if (exact)
+    DOMA_TRY(dalloc(s, &s->d_wpsi, N * (size_t)s->D));
+  else
+    DOMA_TRY(dalloc(s, &s->d_octphi, 8 * N));
+
+  pick_tile(s, o);
+  build_schedule(s);
+  if (s->sched.smem > 227 * 1024) return bad("sweep block needs too much shared memory");
+  DOMA_TRY(sweep_prepare(s->sched.smem));
+  DOMA_TRY(upload(s, &s->d_tasks, s->sched.tasks.data(), s->sched.tasks.size()));
+
+  // per-cell kernels: fixed grid (determinism of the norms depends on it)
+  int sms = 0;
+  DOMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+  const size_t blocks_needed = (N + iteration_block() - 1) / iteration_block();
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>(blocks_needed, (size_t)sms * 8));
+  DOMA_TRY(dalloc(s, &s->d_partials, 2 * (size_t)grid));
+  DOMA_TRY(dalloc(s, &s->d_ticket, 1));
+  DOMA_CUDA_TRY(cudaMemset(s->d_ticket, 0, sizeof(unsigned)));
+  DOMA_TRY(dalloc(s, &s->d_norms, 4));
+  DOMA_CUDA_TRY(cudaMallocHost(&s->h_norms, 4 * sizeof(double)));
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+  s->stream = s->own_stream;
+
+  // kernel argument blocks
+  auto fill = [&](auto & a, auto * q, auto * st, auto * x, auto * y, auto * z) {
+    a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
+    a.d_oct = s->d_oct; a.d_total = s->D;
+    a.tx = s->sched.tx; a.ty = s->sched.ty; a.tz = s->sched.tz;
+    a.tasks = s->d_tasks; a.task_offset = 0; a.oct_offset = s->d_oct_offset;
+    a.amu = s->d_amu; a.aeta = s->d_aeta; a.axi = s->d_axi; a.wgt = s->d_w;
+    a.amu_f = s->d_amu_f; a.aeta_f = s->d_aeta_f; a.axi_f = s->d_axi_f;
+    a.dx = s->d_dx; a.dy = s->d_dy; a.dz = s->d_dz;
+    a.q = q; a.sigt = st; a.xf = x; a.yf = y; a.zf = z;
+    a.wpsi = s->d_wpsi; a.octphi = s->d_octphi; a.theta = o->theta;
+  };
+  if (exact)
+    fill(s->a64, (const double *)s->d_q, (const double *)s->d_sigt, (double *)s->d_xf,
+         (double *)s->d_yf, (double *)s->d_zf);
+  else
+    fill(s->a32, (const float *)s->d_q, (const float *)s->d_sigt, (float *)s->d_xf,
+         (float *)s->d_yf, (float *)s->d_zf);
+  IterArgs & it = s->it;
+  it.N = N; it.G = s->G; it.D = s->D; it.grid = grid; it.oct_mask = s->oct_mask;
+  it.src_scale = s->dims == 3 ? 0.25 : 0.5;
+  it.vol = s->d_vol; it.mat = s->d_mat; it.total = s->d_total; it.scatter = s->d_scatter;
+  it.source = s->d_source; it.fis = s->d_fis; it.chi = s->d_chi; it.nsf = s->d_nsf;
+  it.phi = s->d_phi; it.prev = s->d_prev; it.wpsi = s->d_wpsi; it.octphi = s->d_octphi;
+  it.partials = s->d_partials; it.ticket = s->d_ticket;
+
+  DOMA_CUDA_TRY(cudaMemset(s->d_phi, 0, G * N * sizeof(double)));
+  DOMA_CUDA_TRY(cudaMemset(s->d_prev, 0, G * N * sizeof(double)));
+  DOMA_CUDA_TRY(cudaMemset(s->d_q, 0, 2 * N * ts));
+  DOMA_CUDA_TRY(cudaDeviceSynchronize());
+  return DOMA_OK;
+}
+
+void release(doma_solver * s)
+{
+  if (!s) return;
+  for (void * p : s->allocations) cudaFree(p);
+  if (s->h_norms) cudaFreeHost(s->h_norms);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+}
+
+doma_status sweep_once(doma_solver * s)
+{
+  return launch_sweep(s->dims, s->opts.precision, s->opts.scheme, s->sched, &s->a64, &s->a32,
+                      s->stream, &s->launches);
+}
+
+// One source iteration: sweep, epilogue; norms land in d_norms[0..1].
+doma_status source_iteration(doma_solver * s, int g)
+{
+  DOMA_TRY(sweep_once(s));
+  DOMA_TRY(launch_si_epilogue(s->it, g, s->opts.precision, s->d_q, s->d_norms, s->stream));
+  ++s->launches;
+  return DOMA_OK;
+}
+
+doma_status read_norms(doma_solver * s, int first, double * diff, double * tot)
+{
+  DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_norms + first, s->d_norms + first, 2 * sizeof(double),
+                                cudaMemcpyDeviceToHost, s->stream));
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  *diff = s->h_norms[first];
+  *tot = s->h_norms[first + 1];
+  return DOMA_OK;
+}
+
+double ratio(double diff, double tot)
+{
+  return tot > 1e-8 ? std::sqrt(diff) / std::sqrt(tot) : 0.0;
+}
+
+doma_status solve_impl(doma_solver * s, doma_report * r)
+{
+  const doma_options & o = s->opts;
+  const int verbose = (int)o.verbose;
+  const size_t G = s->G, N = s->N;
+  const auto t0 = std::chrono::steady_clock::now();
+  const uint64_t launches0 = s->launches;
+  if (verbose) {
+    std::printf("Solving...\nInitializing the solver...\n");
+  }
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
+
+  uint64_t sweeps = 0;
+  size_t si_len = 0;
+  unsigned mg = 0;
+  double mg_res = 0.0, si_res = 0.0;
+  doma_status status = DOMA_OK;
+  do {
+    if (verbose) {
+      if (mg != 0u)
+        std::printf("Performing MGI %u, residual = %g\n", mg, mg_res);
+      else
+        std::printf("Performing MGI %u\n", mg);
+      std::printf("----------------------------------------------------------------------------------\n");
+    }
+    for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
+      DOMA_TRY(launch_mg_source(s->it, g, o.precision, s->d_q, s->d_sigt, s->stream));
+      ++s->launches;
+      unsigned it = 0;
+      si_res = 0.0;
+      do {
+        if (verbose >= 2) {
+          if (it != 0u)
+            std::printf("Performing SI %u for G%d, residual = %g\n", it, g, si_res);
+          else
+            std::printf("Performing SI %u for G%d\n", it, g);
+        }
+        DOMA_TRY(source_iteration(s, g));
+        ++sweeps;
+        double diff, tot;
+        DOMA_TRY(read_norms(s, 0, &diff, &tot));
+        if (!std::isfinite(diff) || !std::isfinite(tot)) {
+          set_error("source iteration norm is not finite (group " + std::to_string(g) + ")");
+          status = DOMA_NUMERIC_ERROR;
+          break;
+        }
+        si_res = ratio(diff, tot);
+        ++it;
+      } while (it < o.fs_max_it && o.fs_tol < si_res);
+      if (r && r->si_counts && si_len < r->si_counts_capacity) r->si_counts[si_len] = it;
+      ++si_len;
+      if (status != DOMA_OK) break;
+      if (it < o.fs_max_it) {
+        if (verbose)
+          std::printf("SI converged after %u iterations with a residual of %g for G%d\n", it,
+                      si_res, g);
+      } else {
+        if (verbose)
+          std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n",
+                      it, si_res, g);
+        status = DOMA_NOT_CONVERGED;
+      }
+    }
+    if (status != DOMA_OK) break;
+    DOMA_TRY(launch_mg_residual(s->it, s->d_norms + 2, s->stream));
+    ++s->launches;
+    double diff, tot;
+    DOMA_TRY(read_norms(s, 2, &diff, &tot));
+    if (!std::isfinite(diff) || !std::isfinite(tot)) {
+      set_error("Gauss-Seidel norm is not finite");
+      status = DOMA_NUMERIC_ERROR;
+      break;
+    }
+    mg_res = ratio(diff, tot);
+    ++mg;
+  } while (mg < o.mg_max_it && o.mg_tol < mg_res && s->G > 1);
+
+  if (status == DOMA_OK) {
+    if (mg < o.mg_max_it) {
+      if (verbose && s->G > 1)
+        std::printf("MGI converged after %u iterations with a residual of %g\n", mg, mg_res);
+    } else {
+      if (verbose)
+        std::printf("MGI failed to converge after %u iterations with a residual of %g\n", mg,
+                    mg_res);
+      status = DOMA_NOT_CONVERGED;
+      set_error("Gauss-Seidel iteration reached mg_max_it");
+    }
+  } else if (status == DOMA_NOT_CONVERGED) {
+    set_error("source iteration reached fs_max_it");
+  }
+  if (verbose) std::fflush(stdout);
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  const auto t1 = std::chrono::steady_clock::now();
+  if (r) {
+    r->status = status;
+    r->mg_iterations = mg;
+    r->si_iterations = sweeps;
+    r->updates = sweeps * (uint64_t)s->N * (uint64_t)s->D;
+    r->kernel_launches = s->launches - launches0;
+    r->mg_residual = mg_res;
+    r->si_residual = si_res;
+    r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    r->si_counts_len = si_len;
+  }
+  return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+void doma_default_options(doma_options * o)
+{
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->scheme = DOMA_SCHEME_DD;
+  o->theta = 0.9;
+  o->precision = DOMA_PREC_FP64;
+  o->fs_tol = 1e-8;
+  o->fs_max_it = 1000;
+  o->mg_tol = 1e-8;
+  o->mg_max_it = 100;
+}
+
+const char * doma_last_error(void) { return get_error(); }
+
+uint32_t doma_abi_version(void) { return DOMA_ABI_VERSION; }
+
+doma_status doma_quadrature(uint32_t np, uint32_t na, uint32_t dims, double * mu, double * eta,
+                            double * xi, double * w, uint32_t counts[8])
+{
+  if (!mu || !eta || !xi || !w || !counts) return bad("null output pointer");
+  unsigned c[8];
+  const int n = gc_quadrature(np, na, dims, mu, eta, xi, w, c);
+  if (n < 0) return bad("invalid quadrature order");
+  for (int o = 0; o < 8; ++o) counts[o] = c[o];
+  return DOMA_OK;
+}
+
+doma_status doma_solver_create(const doma_problem * problem, const doma_options * opts,
+                               doma_solver ** out)
+{
+  if (!out) return bad("null output handle");
+  *out = nullptr;
+  doma_status st = validate(problem, opts);
+  if (st != DOMA_OK) return st;
+  doma_solver * s = new (std::nothrow) doma_solver();
+  if (!s) return bad("out of host memory");
+  st = create_impl(problem, opts, s);
+  if (st != DOMA_OK) {
+    release(s);
+    return st;
+  }
+  *out = s;
+  return DOMA_OK;
+}
+
+doma_status doma_solver_set_stream(doma_solver * s, void * stream)
+{
+  if (!s) return bad("null solver");
+  s->stream = stream ? static_cast<cudaStream_t>(stream) : s->own_stream;
+  return DOMA_OK;
+}
+
+doma_status doma_solver_solve_fixed_source(doma_solver * s, doma_report * report)
+{
+  if (!s) return bad("null solver");
+  return solve_impl(s, report);
+}
+
+doma_status doma_solver_get_scalar_flux(doma_solver * s, double * out, size_t count)
+{
+  if (!s || !out) return bad("null solver or output");
+  if (count < (size_t)s->G * s->N) return bad("output buffer too small");
+  DOMA_CUDA_TRY(cudaMemcpyAsync(out, s->d_phi, (size_t)s->G * s->N * sizeof(double),
+                                cudaMemcpyDeviceToHost, s->stream));
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return DOMA_OK;
+}
+
+doma_status doma_solver_source_iterations(doma_solver * s, uint32_t group, uint32_t count)
+{
+  if (!s) return bad("null solver");
+  if ((int)group >= s->G) return bad("group out of range");
+  DOMA_TRY(launch_mg_source(s->it, (int)group, s->opts.precision, s->d_q, s->d_sigt, s->stream));
+  ++s->launches;
+  for (uint32_t i = 0; i < count; ++i) DOMA_TRY(source_iteration(s, (int)group));
+  return DOMA_OK;
+}
+
+doma_status doma_solver_sweeps(doma_solver * s, uint32_t group, uint32_t count)
+{
+  if (!s) return bad("null solver");
+  if ((int)group >= s->G) return bad("group out of range");
+  for (uint32_t i = 0; i < count; ++i) DOMA_TRY(sweep_once(s));
+  return DOMA_OK;
+}
+
+doma_status doma_solver_describe(const doma_solver * s, uint32_t tile[3],
+                                 uint32_t * launches_per_sweep, uint64_t * kernel_launches)
+{
+  if (!s) return bad("null solver");
+  if (tile) {
+    tile[0] = (uint32_t)s->sched.tx;
+    tile[1] = (uint32_t)s->sched.ty;
+    tile[2] = (uint32_t)s->sched.tz;
+  }
+  if (launches_per_sweep) {
+    uint32_t n = 0;
+    for (size_t L = 0; L + 1 < s->sched.level_begin.size(); ++L)
+      if (s->sched.level_begin[L + 1] > s->sched.level_begin[L]) ++n;
+    *launches_per_sweep = n;
+  }
+  if (kernel_launches) *kernel_launches = s->launches;
+  return DOMA_OK;
+}
+
+void doma_solver_destroy(doma_solver * s) { release(s); }
+
+}  // extern "C"

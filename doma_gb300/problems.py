@@ -11,9 +11,12 @@ prompt fission (``chi_p``, ``nu_sigma_f``).
 The generators are deterministic functions of a seed.  Random numbers come
 from a counter-based SplitMix64 stream (Steele, Lea and Flood, "Fast
 splittable pseudorandom number generators", OOPSLA 2014): value k of a stream
-is mix(key + (k + 1) * 0x9E3779B97F4A7C15); uniforms use the top 53 bits and
-normals use the Box-Muller transform.  Nothing depends on numpy's own
-generators, so inputs are identical on every machine.
+is mix(key + (k + 1) * 0x9E3779B97F4A7C15); uniforms use the top 53 bits.
+Every transform uses only correctly rounded basic arithmetic (no libm or
+SIMD transcendental functions, whose last bits differ between x86-64 and
+aarch64 builds): normals are Irwin-Hall sums of twelve uniforms and
+exponentials come from a scaled Taylor series, so inputs are bit-identical on
+every machine.
 """
 from __future__ import annotations
 
@@ -77,9 +80,12 @@ class Rng:
         return lo + (hi - lo) * u
 
     def normal(self, n: int) -> np.ndarray:
-        u1 = 1.0 - self.uniform(n)  # (0, 1]
-        u2 = self.uniform(n)
-        return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+        """Approximately standard normal: sum of 12 uniforms minus 6 (Irwin-Hall)."""
+        u = self.uniform(12 * n).reshape(n, 12)
+        acc = np.zeros(n)
+        for k in range(12):  # fixed summation order
+            acc = acc + u[:, k]
+        return acc - 6.0
 
     def integers(self, n: int, lo: int, hi: int) -> np.ndarray:
         """Integers in [lo, hi)."""
@@ -87,6 +93,19 @@ class Rng:
 
     def permutation(self, n: int) -> np.ndarray:
         return np.argsort(self.uniform(n), kind="stable")
+
+
+def portable_exp(x) -> np.ndarray:
+    """exp(x) from basic arithmetic only: exp(x) = (exp(x / 256))^256, the inner
+    factor by a 14-term Taylor series in Horner form, then 8 squarings.
+    Relative error about 1e-13 for |x| < 10; bit-identical on every platform."""
+    x = np.asarray(x, dtype=np.float64) / 256.0
+    acc = np.ones_like(x)
+    for k in range(14, 0, -1):
+        acc = 1.0 + (x / float(k)) * acc
+    for _ in range(8):
+        acc = acc * acc
+    return acc
 
 
 @dataclass
@@ -289,7 +308,7 @@ def checkerboard(seed: int = 0, n: int = 64, groups: int = 8, np_: int = 4, na: 
     r = Rng(seed, "checkerboard")
     G = groups
     perm = r.permutation(4)
-    sig = np.exp(0.5 * r.normal(4 * G)).reshape(4, G)
+    sig = portable_exp(0.5 * r.normal(4 * G)).reshape(4, G)
     c = r.uniform(4 * G, 0.5, 0.95).reshape(4, G)
     S = np.stack([_scatter_split(G, c[m], sig[m]) for m in range(4)])
     idx = np.arange(n) // block

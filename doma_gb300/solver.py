@@ -1,0 +1,132 @@
+"""Python host interface of the GB300 fixed-source solver (binds the C ABI).
+
+Mirrors DOMA's solver interface for this path: a solver is built from a
+problem and options (TransportSolver3D<T>(mesh, params, verbose, threads),
+src/TransportSolver3D.cpp:5-27) and ``solve_fixed_source()`` runs the
+Gauss-Seidel / source-iteration solve (TransportSolver3D::solveFixedSource,
+src/TransportSolver3D.cpp:262-316).  As in DOMA, non-convergence is a
+``False`` result, not an exception; invalid input and CUDA failures raise.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .problems import Problem, make_options
+
+
+@dataclass
+class Report:
+    converged: bool
+    status: int
+    mg_iterations: int
+    si_iterations: int
+    updates: int
+    kernel_launches: int
+    mg_residual: float
+    si_residual: float
+    solve_ms: float
+    si_counts: np.ndarray
+
+
+class Solver:
+    """One problem resident on the current CUDA device."""
+
+    def __init__(self, problem: Problem, options: abi.DomaOptions | None = None, **kw):
+        self.lib = abi.load_library()
+        self.problem = problem
+        self.options = options if options is not None else make_options(**kw)
+        self._cp = problem.to_c()
+        h = ctypes.c_void_p()
+        st = self.lib.doma_solver_create(ctypes.byref(self._cp), ctypes.byref(self.options),
+                                         ctypes.byref(h))
+        abi.check(st, "doma_solver_create", self.lib)
+        self._h = h
+
+    # -- lifecycle ----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.doma_solver_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- calls --------------------------------------------------------------
+    def set_stream(self, stream_ptr: int | None) -> None:
+        abi.check(self.lib.doma_solver_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)),
+                  "doma_solver_set_stream", self.lib)
+
+    def solve_fixed_source(self, si_capacity: int = 1 << 16) -> Report:
+        counts = np.zeros(si_capacity, dtype=np.uint32)
+        rep = abi.DomaReport()
+        rep.si_counts = counts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        rep.si_counts_capacity = si_capacity
+        st = self.lib.doma_solver_solve_fixed_source(self._h, ctypes.byref(rep))
+        abi.check(st, "doma_solver_solve_fixed_source", self.lib,
+                  allow=(abi.DOMA_OK, abi.DOMA_NOT_CONVERGED))
+        n = min(rep.si_counts_len, si_capacity)
+        return Report(converged=st == abi.DOMA_OK, status=st, mg_iterations=rep.mg_iterations,
+                      si_iterations=rep.si_iterations, updates=rep.updates,
+                      kernel_launches=rep.kernel_launches, mg_residual=rep.mg_residual,
+                      si_residual=rep.si_residual, solve_ms=rep.solve_ms,
+                      si_counts=counts[:n].copy())
+
+    def scalar_flux(self) -> np.ndarray:
+        p = self.problem
+        out = np.empty((p.num_groups, p.num_cells), dtype=np.float64)
+        abi.check(self.lib.doma_solver_get_scalar_flux(
+            self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size),
+            "doma_solver_get_scalar_flux", self.lib)
+        return out
+
+    def source_iterations(self, group: int, count: int) -> None:
+        abi.check(self.lib.doma_solver_source_iterations(self._h, group, count),
+                  "doma_solver_source_iterations", self.lib)
+
+    def sweeps(self, group: int, count: int) -> None:
+        abi.check(self.lib.doma_solver_sweeps(self._h, group, count), "doma_solver_sweeps",
+                  self.lib)
+
+    def describe(self) -> dict:
+        tile = (ctypes.c_uint32 * 3)()
+        lps = ctypes.c_uint32()
+        launches = ctypes.c_uint64()
+        abi.check(self.lib.doma_solver_describe(self._h, tile, ctypes.byref(lps),
+                                                ctypes.byref(launches)),
+                  "doma_solver_describe", self.lib)
+        return {"tile": tuple(tile), "launches_per_sweep": lps.value,
+                "kernel_launches": launches.value}
+
+
+def quadrature(num_polar: int, num_azimuthal: int, dims: int = 3):
+    """(mu, eta, xi, w, counts) from the library's host quadrature (no GPU needed)."""
+    lib = abi.load_library()
+    D = (8 if dims == 3 else 4) * num_polar * num_azimuthal
+    arrs = [np.zeros(D) for _ in range(4)]
+    counts = np.zeros(8, dtype=np.uint32)
+    dp = ctypes.POINTER(ctypes.c_double)
+    abi.check(lib.doma_quadrature(num_polar, num_azimuthal, dims,
+                                  *[a.ctypes.data_as(dp) for a in arrs],
+                                  counts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))),
+              "doma_quadrature", lib)
+    return (*arrs, counts)
+
+
+def solve(problem: Problem, **kw):
+    """Convenience: build, solve, read back.  -> (phi [G][N], Report)"""
+    with Solver(problem, **kw) as s:
+        rep = s.solve_fixed_source()
+        return s.scalar_flux(), rep

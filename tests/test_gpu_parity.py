@@ -1,0 +1,155 @@
+"""Parity of the GPU library (called through the C ABI) with DOMA.
+
+* FP64 drop-in mode against DOMA's own results (the golden fixtures, made by
+  running DOMA) and against the CPU oracle on fresh seeded problems: same
+  return value, same source-iteration count for every (MG iteration, group),
+  scalar flux within 1e-12 relative L-infinity (and, in practice, bit-equal).
+* FP32 sweep mode against the same references: relative L2 error <= 1e-5.
+* Determinism, block-shape independence and the failure paths.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+from doma_gb300 import problems as P
+from doma_gb300.solver import Solver, quadrature
+from golden_cases import case_names, load_case, quadrature_sets
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12   # relative L-infinity, FP64 drop-in mode
+FP32_RTOL = 1e-5    # relative L2, FP32 sweep vs FP64
+
+
+def rel_linf(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def run(p, opts):
+    with Solver(p, opts) as s:
+        rep = s.solve_fixed_source()
+        return s.scalar_flux(), rep
+
+
+@pytest.mark.parametrize("dims,np_,na,mu,eta,xi,w,counts", quadrature_sets())
+def test_quadrature_bitwise_on_this_host(dims, np_, na, mu, eta, xi, w, counts):
+    m, e, x, ww, c = quadrature(np_, na, dims)
+    assert np.array_equal(c, counts)
+    for a, b in ((m, mu), (e, eta), (x, xi), (ww, w)):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_fp64_matches_reference_golden(name):
+    p, opts, exp = load_case(name)
+    phi, rep = run(p, opts)
+    assert rep.converged == exp["converged"]
+    assert list(rep.si_counts) == list(exp["si_counts"])
+    if exp["mg_iterations"] is not None:
+        assert rep.mg_iterations == exp["mg_iterations"]
+    assert rel_linf(phi, exp["phi"]) <= FP64_RTOL
+
+
+def test_fp64_bit_equal_to_reference_golden():
+    """Stronger than the contract: with matching iteration counts, the
+    exact-order FP64 path reproduces DOMA's scalar flux bit for bit."""
+    unequal = []
+    for name in case_names():
+        p, opts, exp = load_case(name)
+        phi, rep = run(p, opts)
+        if not np.array_equal(phi, exp["phi"]):
+            unequal.append((name, rel_linf(phi, exp["phi"])))
+    assert not unequal, unequal
+
+
+@pytest.mark.parametrize("seed", [21, 22, 23])
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+@pytest.mark.parametrize("dims", [2, 3])
+def test_fp64_matches_oracle_random(seed, scheme, dims):
+    p = P.random_problem(seed, dims, 9, 7, 6, groups=3, np_=2, na=3, materials=4,
+                         fission=seed % 2 == 1)
+    opts = P.make_options(scheme=scheme, theta=0.8, fs_tol=1e-10, mg_tol=1e-10)
+    phi, rep = run(p, opts)
+    o_phi, ok, si, mg, _ = ol.oracle_solve(p, opts)
+    assert rep.converged == ok
+    assert list(rep.si_counts) == list(si)
+    assert rep.mg_iterations == mg
+    assert rel_linf(phi, o_phi) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("tile", [(1, 1, 1), (3, 2, 5), (8, 8, 2), (32, 1, 1), (5, 3, 1)])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_block_shape_does_not_change_results(tile, precision):
+    """Every block shape, including ragged edge blocks, gives the same bits."""
+    p = P.random_problem(31, 3, 11, 9, 7, groups=2, np_=2, na=2, materials=3)
+    base = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-9, mg_tol=1e-9)
+    ref_phi, _ = run(p, base)
+    opts = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-9, mg_tol=1e-9,
+                          tile=tile)
+    phi, _ = run(p, opts)
+    assert np.array_equal(phi, ref_phi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_deterministic(precision):
+    p = P.small_cube(3, n=14)
+    opts = P.make_options(scheme="tw_dd", precision=precision)
+    a, ra = run(p, opts)
+    b, rb = run(p, opts)
+    assert np.array_equal(a, b) and list(ra.si_counts) == list(rb.si_counts)
+
+
+@pytest.mark.parametrize("name", [n for n in case_names() if not n.startswith("capped")])
+def test_fp32_error_against_reference(name):
+    p, opts, exp = load_case(name)
+    opts.precision = 1
+    phi, rep = run(p, opts)
+    assert rep.converged
+    assert rel_l2(phi, exp["phi"]) <= FP32_RTOL, rel_l2(phi, exp["phi"])
+
+
+def test_2d_twdd_keeps_bare_xi_term():
+    """DOMA's 2D TW-DD b weight carries a bare |xi| term; removing it would
+    change the answer, so matching the oracle pins it."""
+    p = P.square_2d(4, n=12, groups=1)
+    opts = P.make_options(scheme="tw_dd", theta=0.9)
+    phi, _ = run(p, opts)
+    o_phi, *_ = ol.oracle_solve(p, opts)
+    assert rel_linf(phi, o_phi) <= FP64_RTOL
+
+
+def test_not_converged_keeps_last_iterate():
+    p, opts, exp = load_case("capped_si_twdd")
+    phi, rep = run(p, opts)
+    assert not rep.converged and rep.status == 1
+    assert np.array_equal(phi, exp["phi"])
+
+
+def test_source_iterations_match_oracle():
+    p = P.checkerboard(0, n=16, groups=4, np_=2, na=2, block=4)
+    opts = P.make_options(scheme="tw_dd", theta=0.7)
+    with Solver(p, opts) as s:
+        s.source_iterations(0, 5)
+        phi = s.scalar_flux()
+    o_phi, _ = ol.oracle_source_iterations(p, opts, 0, 5)
+    assert rel_linf(phi, o_phi) <= FP64_RTOL
+
+
+def test_empty_source_gives_zero_flux():
+    p = P.random_problem(2, 3, 4, 4, 4, groups=2)
+    p.source[:] = 0.0
+    phi, rep = run(p, P.make_options())
+    assert rep.converged and not phi.any()
+
+
+def test_single_cell_and_single_ordinate():
+    p = P.random_problem(9, 3, 1, 1, 1, groups=1, np_=1, na=1, materials=1)
+    opts = P.make_options(scheme="tw_dd")
+    phi, rep = run(p, opts)
+    o_phi, ok, si, _, _ = ol.oracle_solve(p, opts)
+    assert list(rep.si_counts) == list(si)
+    assert rel_linf(phi, o_phi) <= FP64_RTOL

@@ -1,0 +1,144 @@
+"""The C++ drop-in layer: deck reader, mesh, text output and (on a GPU) the
+TransportSolver3D/2D classes and the deck runner."""
+import json
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+from doma_gb300 import abi, build as nb
+from doma_gb300 import problems as P
+from doma_gb300.decks import read_deck_summary, write_deck
+
+ROOT = Path(__file__).resolve().parents[1]
+SRC = ROOT / "tests" / "cpp" / "host_check.cpp"
+EXE = ROOT / "tests" / "cpp" / "_build" / "host_check"
+REF_CASES = Path("/root/reference/cases")
+
+
+@pytest.fixture(scope="module")
+def host_check():
+    if not nb.HOST_LIB.exists() or not nb.LIB.exists():
+        nb.build()
+    if not EXE.exists() or EXE.stat().st_mtime < max(SRC.stat().st_mtime, nb.HOST_LIB.stat().st_mtime):
+        EXE.parent.mkdir(parents=True, exist_ok=True)
+        subprocess.run(["g++", "-O2", "-std=c++17", f"-I{nb.HOST / 'include'}", str(SRC), "-o", str(EXE),
+                        f"-L{nb.OUT}", "-ldoma_gb300_host", "-ldoma_gb300",
+                        f"-Wl,-rpath,{nb.OUT},-rpath,/usr/local/cuda/lib64"], check=True)
+    return EXE
+
+
+def run(exe, *args, check=True):
+    r = subprocess.run([str(exe), *map(str, args)], capture_output=True, text=True)
+    if check and r.returncode != 0:
+        raise AssertionError(f"{args}: rc={r.returncode}\n{r.stdout}\n{r.stderr}")
+    return r
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_generated_deck_round_trips(host_check, tmp_path, dims):
+    p = P.random_problem(4, dims, 5, 4, 3, groups=3, np_=2, na=3, materials=4, fission=True)
+    deck = write_deck(p, tmp_path / "d.xml", scheme="tw_dd", fs_tol=1e-9, theta=0.7,
+                      precision="fp32")
+    d = json.loads(run(host_check, "parse", deck).stdout)
+    assert (d["groups"], d["np"], d["na"], d["dims"]) == (3, 2, 3, dims)
+    assert d["scheme"] == 1 and d["fs_tol"] == 1e-9 and d["theta"] == 0.7 and d["precision"] == 1
+    assert np.array_equal(d["dx"], p.dx) and d["blocks"] == list(map(int, p.cell_material))
+    for m in range(p.num_materials):
+        mat = d["materials"][str(m)]
+        assert np.array_equal(mat["total"], p.total[m])
+        assert np.array_equal(mat["scatter"], p.scatter[m].ravel())
+        assert (len(mat["chi_p"]) > 0) == bool(p.has_fission[m])
+
+
+@pytest.mark.skipif(not REF_CASES.exists(), reason="DOMA's example decks are not present")
+def test_reference_decks_parse(host_check):
+    decks = sorted(REF_CASES.glob("[23]D_*.xml")) + sorted(REF_CASES.glob("*/[23]D_*.xml"))
+    assert decks
+    for deck in decks:
+        d = json.loads(run(host_check, "parse", deck).stdout)
+        s = read_deck_summary(deck)
+        assert (d["np"], d["na"], d["dims"], d["refinement"]) == (s["np"], s["na"], s["dims"],
+                                                                  s["refinement"]), deck
+        assert d["blocks"] == s["blocks"], deck
+        assert sorted(map(int, d["materials"])) == s["materials"], deck
+
+
+@pytest.mark.parametrize("text,msg", [
+    ("<doma_inp><angular_quad np='1' na='1'/></doma_inp>", "solver block"),
+    ("<doma_inp><solver solve_type='steady' scheme='xx' num_groups='1'/></doma_inp>", "Unknown scheme"),
+    ("<doma_inp><solver solve_type='steady'", "XML parse error"),
+    ("<doma_inp><solver solve_type='steady' scheme='dd' num_groups='1' fs_tol='-1'/></doma_inp>",
+     "valid param in fs_tol"),
+])
+def test_bad_decks_report_errors(host_check, tmp_path, text, msg):
+    deck = tmp_path / "bad.xml"
+    deck.write_text(text)
+    r = run(host_check, "parse", deck, check=False)
+    assert r.returncode == 1 and msg in r.stderr
+
+
+@pytest.mark.skipif(not ol.ref_available(), reason="DOMA reference not built here")
+@pytest.mark.parametrize("dims", [2, 3])
+def test_text_output_identical_to_reference(host_check, tmp_path, dims):
+    p = P.random_problem(6, dims, 6, 5, 4, groups=2, np_=1, na=2, materials=3)
+    opts = P.make_options(scheme="dd")
+    (tmp_path / "ref").mkdir()
+    (tmp_path / "ours").mkdir()
+    phi, ok, *_ = ol.ref_solve(p, opts, out_base=str(tmp_path / "ref" / "case"))
+    assert ok
+    deck = write_deck(p, tmp_path / "case.xml")
+    phi.astype(np.float64).tofile(tmp_path / "phi.bin")
+    run(host_check, "dump", deck, tmp_path / "phi.bin", tmp_path / "ours" / "case")
+    ref_files = sorted(x.name for x in (tmp_path / "ref").iterdir())
+    our_files = sorted(x.name for x in (tmp_path / "ours").iterdir())
+    assert ref_files == our_files
+    for f in ref_files:
+        assert (tmp_path / "ref" / f).read_bytes() == (tmp_path / "ours" / f).read_bytes(), f
+
+
+def test_flux_at_point(host_check, tmp_path):
+    p = P.random_problem(8, 3, 4, 3, 2, groups=2)
+    deck = write_deck(p, tmp_path / "d.xml")
+    phi = np.arange(p.num_groups * p.num_cells, dtype=np.float64)
+    phi.tofile(tmp_path / "phi.bin")
+    x = p.dx[0] + 0.4 * p.dx[1]       # cell i = 1 (a point inside, away from faces)
+    y = 0.5 * p.dy[0]                 # j = 0
+    z = p.dz[0] + 0.5 * p.dz[1]       # k = 1
+    d = json.loads(run(host_check, "point", deck, tmp_path / "phi.bin", x, y, z, 1).stdout)
+    c = (1 * p.ny + 0) * p.nx + 1
+    assert d["found"] and d["flux"] == phi[p.num_cells + c]
+    d = json.loads(run(host_check, "point", deck, tmp_path / "phi.bin", -1, 0, 0, 0).stdout)
+    assert not d["found"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,scheme", [(3, "dd"), (3, "tw_dd"), (2, "tw_dd")])
+def test_dropin_solver_matches_oracle(host_check, tmp_path, dims, scheme):
+    p = P.random_problem(12, dims, 7, 6, 5, groups=3, np_=2, na=2, materials=3, fission=True)
+    deck = write_deck(p, tmp_path / "d.xml", scheme=scheme, fs_tol=1e-10, mg_tol=1e-10)
+    d = json.loads(run(host_check, "solve", deck, tmp_path / "phi.bin").stdout.splitlines()[-1])
+    phi = np.fromfile(tmp_path / "phi.bin").reshape(p.num_groups, p.num_cells)
+    o_phi, ok, si, mg, _ = ol.oracle_solve(p, P.make_options(scheme=scheme, fs_tol=1e-10, mg_tol=1e-10))
+    assert d["converged"] == ok and d["si_counts"] == list(map(int, si)) and d["mg"] == mg
+    assert np.abs(phi - o_phi).max() <= 1e-12 * np.abs(o_phi).max()
+
+
+@pytest.mark.gpu
+def test_cli_writes_reference_layout(tmp_path):
+    if not nb.CLI.exists():
+        nb.build()
+    p = P.small_cube(1, n=8)
+    deck = write_deck(p, tmp_path / "cube.xml", scheme="dd")
+    r = subprocess.run([str(nb.CLI), "-i", str(deck), "-n", "4"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "Fixed source solver finished executing." in r.stdout
+    assert "SI converged after" in r.stdout and "Time elapsed:" in r.stdout
+    dims = (tmp_path / "cube_dims.txt").read_text().split()
+    assert dims == ["num_x:", "8", "num_y:", "8", "num_z:", "8", "num_g:", "2"]
+    o_phi, *_ = ol.oracle_solve(p, P.make_options(scheme="dd"))
+    for g in range(2):
+        vals = np.array([float(x) for x in (tmp_path / f"cube_g{g}_flux.txt").read_text().split()])
+        assert np.allclose(vals, o_phi[g], rtol=6e-6, atol=0)
