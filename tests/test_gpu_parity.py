@@ -105,8 +105,13 @@ def test_deterministic(precision):
 
 @pytest.mark.parametrize("name", [n for n in case_names() if not n.startswith("capped")])
 def test_fp32_error_against_reference(name):
+    """FP32 sweeps recompute each group's flux from zero at every Gauss-Seidel
+    iteration, so the Gauss-Seidel residual cannot fall much below the FP32
+    rounding of the flux (~1e-7): FP32 solves run at tolerances >= 1e-6."""
     p, opts, exp = load_case(name)
     opts.precision = 1
+    opts.fs_tol = max(opts.fs_tol, 1e-6)
+    opts.mg_tol = max(opts.mg_tol, 1e-6)
     phi, rep = run(p, opts)
     assert rep.converged
     assert rel_l2(phi, exp["phi"]) <= FP32_RTOL, rel_l2(phi, exp["phi"])
