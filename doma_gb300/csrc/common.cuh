@@ -13,8 +13,8 @@ namespace doma {
 
 constexpr double kPi = 3.14159265358979323846;  // M_PI
 
-// Largest sweep CTA (ordinates x pencils); bounds registers at 128 per thread.
-constexpr int kMaxSweepThreads = 512;
+// Largest sweep CTA: 16 ordinates x 16 pencils.
+constexpr int kMaxSweepThreads = 256;
 
 // Error reporting (per thread, read through doma_last_error()).
 void set_error(const std::string & msg);
@@ -29,10 +29,13 @@ const char * get_error();
     }                                                                                          \
   } while (0)
 
-// One sweep block task: octant and block coordinates in the octant's sweep
-// frame (i' = i for +mu, nx-1-i for -mu, likewise for y and z).
+// Ordinates of one octant handled by one sweep task (two per warp).
+constexpr int kGroup = 16;
+
+// One sweep task: octant, ordinate group and block coordinates in the
+// octant's sweep frame (i' = i for +mu, nx-1-i for -mu, likewise for y, z).
 struct Task {
-  int oct, bi, bj, bk;
+  int oct, og, bi, bj, bk;
 };
 
 // Everything a sweep launch needs.  Pointers are device pointers.
@@ -41,11 +44,13 @@ struct SweepArgs {
   int nx, ny, nz;
   int d_oct;           // ordinates per octant
   int d_total;         // ordinates over all octants (exact mode row length)
-  int tx, ty, tz;      // block shape in cells
-  const Task * tasks;  // all tasks, sorted by level
-  int task_offset;     // first task of this launch
+  int ngroups;         // ordinate groups per octant (ceil(d_oct / kGroup))
+  int nbx, nby, nbz;   // blocks per axis
+  int num_tasks;
+  const Task * tasks;  // all tasks, sorted by level (a topological order)
+  int task_offset;     // level-synchronous mode: first task of this launch
   const int * oct_offset;  // [8] first ordinate of each octant (octant-major tables)
-  // quadrature (octant-major, |cosines|)
+  // quadrature (octant-major, |cosines|, weights)
   const double * amu;
   const double * aeta;
   const double * axi;
@@ -53,29 +58,47 @@ struct SweepArgs {
   const float * amu_f;
   const float * aeta_f;
   const float * axi_f;
-  // geometry (physical index)
-  const double * dx;
-  const double * dy;
-  const double * dz;
+  // geometry in the sweep precision (physical index): widths and the
+  // coefficients 2|mu|/dx [D][nx], 2|eta|/dy [D][ny], 2|xi|/dz [D][nz]
+  const T * wx;
+  const T * wy;
+  const T * wz;
+  const T * cx;
+  const T * cy;
+  const T * cz;
   // per-cell sweep inputs of the group being swept
   const T * q;
   const T * sigt;
-  // face buffers (sweep frame, per octant): x [8][nz][ny][d_oct],
+  // face planes (sweep frame, per octant): x [8][nz][ny][d_oct],
   // y [8][nz][nx][d_oct], z [8][ny][nx][d_oct]
   T * xf;
   T * yf;
   T * zf;
   double * wpsi;     // exact mode: [N][d_total] weighted angular flux
-  double * octphi;   // fp32 mode: [8][N] per-octant scalar-flux partials
+  double * octphi;   // fp32 mode: [8 * ngroups][N] scalar-flux partials per (octant, group)
   double theta;
+  // persistent-mode scheduling state (device memory, kept between sweeps)
+  unsigned * ticket;      // next task to claim (reset by the last CTA to leave)
+  unsigned * exit_count;  // CTAs that have left
+  unsigned * epoch;       // sweeps completed
+  unsigned * done;        // [8][ngroups][nbz][nby][nbx] epoch in which the task finished
+  int * error;            // nonzero: a bounded wait gave up (DOMA_DEVICE_WAIT_TIMEOUT)
+  unsigned spin_limit;    // polls before a wait gives up
+  unsigned wait_bias;     // 0; nonzero only in the wait-timeout test, where every
+                          // wait targets an epoch that no block ever publishes
 };
 
 // Sweep schedule of one solver: block shape and the task list by level.
+// The block is tx cells along x by a fixed 16-pencil cross-section
+// (4 x 4 in (y, z) for 3D, 16 in y for 2D).
 struct Schedule {
   int tx = 0, ty = 0, tz = 0;
+  int ngroups = 1, gs = 1;
   int nbx = 0, nby = 0, nbz = 0;
   int threads = 0;
   size_t smem = 0;
+  bool persistent = true;  // dataflow kernel (true) or one launch per level
+  int grid = 0;            // persistent grid (CTAs)
   std::vector<Task> tasks;
   std::vector<int> level_begin;  // size levels+1
 };
@@ -84,8 +107,11 @@ struct Schedule {
 doma_status launch_sweep(int dims, int precision, int scheme, const Schedule & s,
                          const SweepArgs<double> * a64, const SweepArgs<float> * a32,
                          cudaStream_t stream, uint64_t * launches);
-size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx, int ty, int tz, int d_oct);
-doma_status sweep_prepare(size_t smem);
+int sweep_tile_x(int requested);  // supported block length along x: 8, 16 or 32
+size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx);
+doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem);
+// CTAs of the persistent sweep kernel that fit on the device at once.
+int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem);
 
 // Host quadrature (quadrature.cpp).
 int gc_quadrature(unsigned np, unsigned na, unsigned dims, double * mu, double * eta,

@@ -52,8 +52,9 @@ __device__ __forceinline__ void block_sum2(double & a, double & b)
 }
 
 // Store this block's partial pair; the last block sums all pairs in block
-// order into out[0..1] and re-arms the ticket.
-__device__ __forceinline__ void finish_norms(double a, double b, double * partials,
+// order into out[0..1] and re-arms the ticket.  Returns true in exactly one
+// thread (thread 0 of the last block), after out[] is written.
+__device__ __forceinline__ bool finish_norms(double a, double b, double * partials,
                                              unsigned * ticket, double * out)
 {
   __shared__ bool last;
@@ -65,7 +66,7 @@ __device__ __forceinline__ void finish_norms(double a, double b, double * partia
     last = atomicAdd(ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last) return;
+  if (!last) return false;
   __threadfence();
   double sa = 0.0, sb = 0.0;
   for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
@@ -77,7 +78,21 @@ __device__ __forceinline__ void finish_norms(double a, double b, double * partia
     out[0] = sa;
     out[1] = sb;
     *ticket = 0u;
+    return true;
   }
+  return false;
+}
+
+// DOMA's relative norm (src/TransportSolver3D.cpp:562): sqrt(diff)/sqrt(total),
+// or 0 when total <= 1e-8.  IEEE sqrt and division, the same bits as the host.
+__device__ __forceinline__ double norm_ratio(double diff, double tot)
+{
+  return tot > 1e-8 ? __ddiv_rn(__dsqrt_rn(diff), __dsqrt_rn(tot)) : 0.0;
+}
+
+__device__ __forceinline__ bool finite2(double a, double b)
+{
+  return isfinite(a) && isfinite(b);
 }
 
 // updateMultigroupSource for group g (fixed source: external, in-scatter and
@@ -85,8 +100,17 @@ __device__ __forceinline__ void finish_norms(double a, double b, double * partia
 // the sweep inputs (q and sigma_t of group g in the sweep's precision).
 template <typename T>
 __global__ void __launch_bounds__(kBlock) mg_source_kernel(const IterArgs A, int g, T * q_out,
-                                                          T * sigt_out)
+                                                          T * sigt_out, const LoopParams L)
 {
+  if (L.graph) {
+    // a failed group ends the solve: leave the flux of the last iterate alone
+    const bool stop = L.ctl->failed != 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (!stop) L.ctl->si_it = 0u;
+      cudaGraphSetConditional(L.si_handle, stop ? 0u : 1u);
+    }
+    if (stop) return;
+  }
   const size_t N = A.N;
   const int G = A.G;
   const double s = A.src_scale;
@@ -110,12 +134,12 @@ __global__ void __launch_bounds__(kBlock) mg_source_kernel(const IterArgs A, int
 
 // The source-iteration epilogue for group g:
 //   dphi = sum of the swept angular flux (exact: all ordinates in DOMA's
-//          single-thread order; fp32: the octant partials in octant order)
+//          single-thread order; fp32: the (octant, ordinate group) partials in order)
 //   diff += dphi^2 V, total += (phi + dphi)^2 V   (residual, before the update)
 //   phi += dphi;  q = s * S_gg * dphi / pi       (the next increment's source)
 template <typename T, bool EXACT>
 __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, int g, T * q_out,
-                                                            double * norms)
+                                                            double * norms, const LoopParams L)
 {
   const size_t N = A.N;
   const int G = A.G;
@@ -128,7 +152,9 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
       for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
     } else {
       for (int o = 0; o < 8; ++o)
-        if (A.oct_mask & (1 << o)) d = dA(d, A.octphi[(size_t)o * N + c]);
+        if (A.oct_mask & (1 << o))
+          for (int og = 0; og < A.ngroups; ++og)
+            d = dA(d, A.octphi[((size_t)o * A.ngroups + og) * N + c]);
     }
     const double V = A.vol[c];
     double * ph = A.phi + (size_t)g * N + c;
@@ -139,12 +165,39 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
     const unsigned m = A.mat[c];
     q_out[c] = (T)dD(dM(dM(A.src_scale, A.scatter[((size_t)m * G + g) * G + g]), d), kPi);
   }
-  finish_norms(diff, tot, A.partials, A.ticket, norms);
+  if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
+    // sourceIteration's loop test (src/TransportSolver3D.cpp:481), on the device
+    LoopCtl * C = L.ctl;
+    const double res = norm_ratio(norms[0], norms[1]);
+    const unsigned it = ++C->si_it;
+    ++C->sweeps;
+    if (L.si_hist && C->hist_len < L.hist_cap) L.si_hist[C->hist_len] = res;
+    ++C->hist_len;
+    C->si_res = res;
+    const bool ok = finite2(norms[0], norms[1]) && C->error == 0;
+    const bool more = ok && it < L.fs_max_it && L.fs_tol < res;
+    if (!more) {
+      if (C->pairs < L.pair_cap) {
+        L.pair_counts[C->pairs] = it;
+        L.pair_res[C->pairs] = res;
+      }
+      ++C->pairs;
+      if (C->error != 0) C->failed = DOMA_DEVICE_WAIT_TIMEOUT;
+      else if (!ok) C->failed = DOMA_NUMERIC_ERROR;
+      else if (!(it < L.fs_max_it)) C->failed = DOMA_NOT_CONVERGED;
+    }
+    cudaGraphSetConditional(L.si_handle, more ? 1u : 0u);
+  }
 }
 
 // computeMGFluxResidual: sums over cells and groups of (phi - prev)^2 V and phi^2 V.
-__global__ void __launch_bounds__(kBlock) mg_residual_kernel(const IterArgs A, double * norms)
+__global__ void __launch_bounds__(kBlock) mg_residual_kernel(const IterArgs A, double * norms,
+                                                            const LoopParams L)
 {
+  if (L.graph && L.ctl->failed != 0u) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(L.mg_handle, 0u);
+    return;
+  }
   const size_t N = A.N;
   double diff = 0.0, tot = 0.0;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
@@ -157,36 +210,48 @@ __global__ void __launch_bounds__(kBlock) mg_residual_kernel(const IterArgs A, d
       tot = dA(tot, dM(dM(a, a), V));
     }
   }
-  finish_norms(diff, tot, A.partials, A.ticket, norms);
+  if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
+    // solveFixedSource's loop test (src/TransportSolver3D.cpp:295), on the device
+    LoopCtl * C = L.ctl;
+    const double res = norm_ratio(norms[0], norms[1]);
+    if (C->mg_it < L.mg_cap) L.mg_hist[C->mg_it] = res;
+    const unsigned mg = ++C->mg_it;
+    C->mg_res = res;
+    const bool ok = finite2(norms[0], norms[1]);
+    if (!ok) C->failed = DOMA_NUMERIC_ERROR;
+    const bool more = ok && mg < L.mg_max_it && L.mg_tol < res && L.G > 1;
+    cudaGraphSetConditional(L.mg_handle, more ? 1u : 0u);
+  }
 }
 
 }  // namespace
 
 doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q, void * sigt,
-                             cudaStream_t st)
+                             const LoopParams & L, cudaStream_t st)
 {
   if (precision == DOMA_PREC_FP64)
-    mg_source_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, (double *)sigt);
+    mg_source_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, (double *)sigt, L);
   else
-    mg_source_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, (float *)sigt);
+    mg_source_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, (float *)sigt, L);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }
 
 doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * q,
-                               double * norms, cudaStream_t st)
+                               double * norms, const LoopParams & L, cudaStream_t st)
 {
   if (precision == DOMA_PREC_FP64)
-    si_epilogue_kernel<double, true><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, norms);
+    si_epilogue_kernel<double, true><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, norms, L);
   else
-    si_epilogue_kernel<float, false><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, norms);
+    si_epilogue_kernel<float, false><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, norms, L);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }
 
-doma_status launch_mg_residual(const IterArgs & a, double * norms, cudaStream_t st)
+doma_status launch_mg_residual(const IterArgs & a, double * norms, const LoopParams & L,
+                               cudaStream_t st)
 {
-  mg_residual_kernel<<<a.grid, kBlock, 0, st>>>(a, norms);
+  mg_residual_kernel<<<a.grid, kBlock, 0, st>>>(a, norms, L);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }

@@ -1,4 +1,5 @@
-// iteration.cuh -- per-cell iteration kernels (iteration.cu).
+// iteration.cuh -- per-cell iteration kernels (iteration.cu) and the device
+// state that lets them drive the solve's loops inside a CUDA graph.
 #pragma once
 
 #include "common.cuh"
@@ -11,6 +12,7 @@ struct IterArgs {
   int D = 0;                  // ordinates (exact-mode row length of wpsi)
   int grid = 0;               // fixed grid of every per-cell kernel
   unsigned oct_mask = 0;      // octants that carry ordinates
+  int ngroups = 1;            // fp32: ordinate groups per octant (partials per octant)
   double src_scale = 0.25;    // 1/(4 pi) prefactor numerator: 0.25 (3D), 0.5 (2D)
   const double * vol = nullptr;       // [N]
   const uint32_t * mat = nullptr;     // [N]
@@ -23,16 +25,55 @@ struct IterArgs {
   double * phi = nullptr;             // [G][N]
   double * prev = nullptr;            // [G][N]
   const double * wpsi = nullptr;      // exact: [N][D]
-  const double * octphi = nullptr;    // fp32: [8][N]
+  const double * octphi = nullptr;    // fp32: [8 * ngroups][N]
   double * partials = nullptr;        // [grid][2]
   unsigned * ticket = nullptr;        // last-block ticket (kept at 0 between launches)
 };
 
+// Device-side solve state (one per solver, in device memory; mirrored in
+// pinned host memory for read-back).
+struct LoopCtl {
+  double norms[4];          // SI (diff, total), MG (diff, total)
+  int error;                // a sweep wait timed out (DOMA_DEVICE_WAIT_TIMEOUT) or 0
+  unsigned ticket;          // persistent sweep: next task
+  unsigned exit_count;      // persistent sweep: CTAs that have left
+  unsigned epoch;           // persistent sweep: sweeps completed
+  // graph-driven loops
+  unsigned si_it;           // source iterations of the group being solved
+  unsigned mg_it;           // Gauss-Seidel iterations completed
+  unsigned failed;          // 0, or the doma_status that stopped the solve
+  unsigned pairs;           // (MG iteration, group) pairs completed
+  unsigned long long sweeps;    // source iterations over the whole solve
+  unsigned long long hist_len;  // SI residuals recorded
+  double si_res;            // last SI residual
+  double mg_res;            // last Gauss-Seidel residual
+};
+
+// Kernel argument for the graph-driven loops.  With graph == 0 the kernels
+// only compute (the host drives the loops and reads the norms).
+struct LoopParams {
+  LoopCtl * ctl = nullptr;
+  unsigned * pair_counts = nullptr;   // [pair_cap] SI count per (MG iteration, group)
+  double * pair_res = nullptr;        // [pair_cap] last SI residual per pair
+  unsigned pair_cap = 0;
+  double * si_hist = nullptr;         // [hist_cap] every SI residual (verbose runs)
+  unsigned long long hist_cap = 0;
+  double * mg_hist = nullptr;         // [mg_cap] every Gauss-Seidel residual
+  unsigned mg_cap = 0;
+  double fs_tol = 0.0, mg_tol = 0.0;
+  unsigned fs_max_it = 0, mg_max_it = 0;
+  int G = 0;
+  unsigned long long si_handle = 0;   // cudaGraphConditionalHandle of the SI loop
+  unsigned long long mg_handle = 0;   // cudaGraphConditionalHandle of the MG loop
+  int graph = 0;
+};
+
 doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q, void * sigt,
-                             cudaStream_t st);
+                             const LoopParams & L, cudaStream_t st);
 doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * q,
-                               double * norms, cudaStream_t st);
-doma_status launch_mg_residual(const IterArgs & a, double * norms, cudaStream_t st);
+                               double * norms, const LoopParams & L, cudaStream_t st);
+doma_status launch_mg_residual(const IterArgs & a, double * norms, const LoopParams & L,
+                               cudaStream_t st);
 int iteration_block();
 
 }  // namespace doma

@@ -19,6 +19,9 @@
 //   materials  : total [M][G], scatter [M][G][G], source, fission data
 #include <chrono>
 #include <cmath>
+#include <cstddef>
+#include <cstdlib>
+#include <type_traits>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -40,6 +43,8 @@ const char * get_error() { return g_error.c_str(); }
 }  // namespace doma
 
 using namespace doma;
+
+using DevCtl = LoopCtl;
 
 struct doma_solver {
   int dims = 3, nx = 1, ny = 1, nz = 1, G = 1, M = 1;
@@ -63,11 +68,25 @@ struct doma_solver {
   void *d_xf = nullptr, *d_yf = nullptr, *d_zf = nullptr;
   double * d_wpsi = nullptr;
   double * d_octphi = nullptr;
+  void *d_wx = nullptr, *d_wy = nullptr, *d_wz = nullptr;   // widths, sweep precision
+  void *d_cx = nullptr, *d_cy = nullptr, *d_cz = nullptr;   // 2|cosine|/width tables
   double * d_partials = nullptr;
   unsigned * d_ticket = nullptr;
-  double * d_norms = nullptr;  // [4]: SI (diff, total), MG (diff, total)
+  DevCtl * d_ctl = nullptr;
+  unsigned * d_done = nullptr;  // [tasks] persistent-sweep done epochs
   Task * d_tasks = nullptr;
-  double * h_norms = nullptr;  // pinned [4]
+  DevCtl * h_ctl = nullptr;     // pinned mirror
+
+  // graph-driven solve
+  unsigned * d_pair_counts = nullptr;
+  double * d_pair_res = nullptr;
+  double * d_mg_hist = nullptr;
+  double * d_si_hist = nullptr;
+  unsigned pair_cap = 0, mg_cap = 0;
+  unsigned long long hist_cap = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool use_graph = true;
 
   Schedule sched;
   cudaStream_t stream = nullptr;
@@ -134,8 +153,8 @@ doma_status validate(const doma_problem * p, const doma_options * o)
   if (p->has_fission && (!p->chi_p || !p->nu_sigma_f))
     return bad("has_fission given without chi_p / nu_sigma_f");
   if (p->num_polar == 0 || p->num_azimuthal == 0) return bad("np and na must be positive");
-  if ((uint64_t)p->num_polar * p->num_azimuthal > (uint64_t)kMaxSweepThreads)
-    return bad("np*na (ordinates per octant) must be <= " + std::to_string(kMaxSweepThreads));
+  if ((uint64_t)p->num_polar * p->num_azimuthal > 4096u)
+    return bad("np*na (ordinates per octant) must be <= 4096");
   const uint64_t N = (uint64_t)p->nx * p->ny * p->nz;
   if (N > (1ull << 31)) return bad("too many cells");
   for (uint64_t c = 0; c < N; ++c)
@@ -157,43 +176,16 @@ doma_status validate(const doma_problem * p, const doma_options * o)
   return DOMA_OK;
 }
 
-// Block shape: aim at ~256 threads (ordinates x pencils) per CTA.
+// Block shape: tx cells along x (8, 16 or 32) by the kernel's fixed 16-pencil
+// cross-section; ordinates split into groups of at most kGroup per task.
 void pick_tile(doma_solver * s, const doma_options * o)
 {
-  int tx = o->tile_x, ty = o->tile_y, tz = o->tile_z;
-  const int pencils = s->d_oct >= 256 ? 1 : 256 / s->d_oct;
-  if (s->dims == 3) {
-    if (!ty || !tz) {
-      int a = 1, b = 1;
-      while (a * b * 2 <= pencils) {
-        if (a <= b) a *= 2; else b *= 2;
-      }
-      ty = ty ? ty : a;
-      tz = tz ? tz : b;
-    }
-    if (!tx) tx = 16;
-  } else {
-    tz = 1;
-    if (!ty) {
-      int a = 1;
-      while (a * 2 <= pencils) a *= 2;
-      ty = a;
-    }
-    if (!tx) tx = 32;
-  }
-  tx = std::max(1, std::min(tx, s->nx));
-  ty = std::max(1, std::min(ty, s->ny));
-  tz = std::max(1, std::min(tz, s->nz));
-  // keep the CTA within kMaxSweepThreads and the shared memory within 200 KB
-  while (s->d_oct * ty * tz > kMaxSweepThreads && (ty > 1 || tz > 1)) {
-    if (ty >= tz) ty = (ty + 1) / 2; else tz = (tz + 1) / 2;
-  }
-  while (tx > 1 && sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, tx, ty, tz,
-                                    s->d_oct) > 200 * 1024)
-    tx = (tx + 1) / 2;
-  s->sched.tx = tx;
-  s->sched.ty = ty;
-  s->sched.tz = tz;
+  const int want = o->tile_x ? (int)o->tile_x : (s->dims == 3 ? 8 : 32);
+  s->sched.tx = sweep_tile_x(want);
+  s->sched.ty = s->dims == 3 ? 4 : 16;
+  s->sched.tz = s->dims == 3 ? 4 : 1;
+  s->sched.ngroups = (s->d_oct + kGroup - 1) / kGroup;
+  s->sched.gs = std::min(kGroup, s->d_oct);
 }
 
 void build_schedule(doma_solver * s)
@@ -202,16 +194,17 @@ void build_schedule(doma_solver * s)
   sc.nbx = (s->nx + sc.tx - 1) / sc.tx;
   sc.nby = (s->ny + sc.ty - 1) / sc.ty;
   sc.nbz = (s->nz + sc.tz - 1) / sc.tz;
-  sc.threads = s->d_oct * sc.ty * sc.tz;
-  sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx, sc.ty, sc.tz,
-                             s->d_oct);
+  sc.threads = ((16 * sc.gs + 31) / 32) * 32;
+  sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx);
   const int levels = sc.nbx + sc.nby + sc.nbz - 2;
   std::vector<std::vector<Task>> by_level(levels);
   for (int o = 0; o < 8; ++o) {
     if (!(s->oct_mask & (1u << o))) continue;
-    for (int bk = 0; bk < sc.nbz; ++bk)
-      for (int bj = 0; bj < sc.nby; ++bj)
-        for (int bi = 0; bi < sc.nbx; ++bi) by_level[bi + bj + bk].push_back(Task{o, bi, bj, bk});
+    for (int og = 0; og < sc.ngroups; ++og)
+      for (int bk = 0; bk < sc.nbz; ++bk)
+        for (int bj = 0; bj < sc.nby; ++bj)
+          for (int bi = 0; bi < sc.nbx; ++bi)
+            by_level[bi + bj + bk].push_back(Task{o, og, bi, bj, bk});
   }
   sc.tasks.clear();
   sc.level_begin.assign(1, 0);
@@ -301,6 +294,39 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   // state
   const bool exact = o->precision == DOMA_PREC_FP64;
   const size_t ts = exact ? sizeof(double) : sizeof(float);
+
+  // Sweep-precision geometry tables.  The coefficient 2|mu|/dx is formed on
+  // the host exactly as DOMA forms it per cell solve ((2.0 * |mu|) / l_x,
+  // include/DiamondDifference3D.h:36), so the exact mode sees the same bits.
+  {
+    const int D = s->D;
+    std::vector<double> cx((size_t)D * s->nx), cy((size_t)D * s->ny), cz((size_t)D * s->nz);
+    for (int n = 0; n < D; ++n) {
+      for (int i = 0; i < s->nx; ++i) cx[(size_t)n * s->nx + i] = (2.0 * amu[n]) / p->dx[i];
+      for (int j = 0; j < s->ny; ++j) cy[(size_t)n * s->ny + j] = (2.0 * aeta[n]) / p->dy[j];
+      for (int k = 0; k < s->nz; ++k) cz[(size_t)n * s->nz + k] = (2.0 * axi[n]) / dz[k];
+    }
+    std::vector<double> wx(p->dx, p->dx + s->nx), wy(p->dy, p->dy + s->ny), wz(dz);
+    auto put = [&](void ** dst, const std::vector<double> & v) -> doma_status {
+      if (exact) {
+        double * d = nullptr;
+        DOMA_TRY(upload(s, &d, v.data(), v.size()));
+        *dst = d;
+      } else {
+        std::vector<float> f(v.begin(), v.end());
+        float * d = nullptr;
+        DOMA_TRY(upload(s, &d, f.data(), f.size()));
+        *dst = d;
+      }
+      return DOMA_OK;
+    };
+    DOMA_TRY(put(&s->d_cx, cx));
+    DOMA_TRY(put(&s->d_cy, cy));
+    DOMA_TRY(put(&s->d_cz, cz));
+    DOMA_TRY(put(&s->d_wx, wx));
+    DOMA_TRY(put(&s->d_wy, wy));
+    DOMA_TRY(put(&s->d_wz, wz));
+  }
   DOMA_TRY(dalloc(s, &s->d_phi, G * N));
   DOMA_TRY(dalloc(s, &s->d_prev, G * N));
   unsigned char * qb = nullptr;
@@ -318,13 +344,26 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   if (exact)
     DOMA_TRY(dalloc(s, &s->d_wpsi, N * (size_t)s->D));
   else
-    DOMA_TRY(dalloc(s, &s->d_octphi, 8 * N));
+    DOMA_TRY(dalloc(s, &s->d_octphi, 8 * (size_t)((s->d_oct + kGroup - 1) / kGroup) * N));
 
   pick_tile(s, o);
   build_schedule(s);
   if (s->sched.smem > 227 * 1024) return bad("sweep block needs too much shared memory");
-  DOMA_TRY(sweep_prepare(s->sched.smem));
+  DOMA_TRY(sweep_prepare(s->dims, o->precision, o->scheme, s->sched.tx, s->sched.smem));
   DOMA_TRY(upload(s, &s->d_tasks, s->sched.tasks.data(), s->sched.tasks.size()));
+  {
+    const char * env = std::getenv("DOMA_SWEEP_SCHEDULE");
+    s->sched.persistent = !(env && std::string(env) == "levels");
+    const int fit = sweep_resident_ctas(s->dims, o->precision, o->scheme, s->sched.tx,
+                                        s->sched.threads, s->sched.smem);
+    if (fit <= 0) return bad("the sweep block does not fit on this device");
+    s->sched.grid = std::max(1, std::min<int>(fit, (int)s->sched.tasks.size()));
+    // one flag per (octant slot, block): indexed by octant 0..7 even when
+    // only four octants carry ordinates (2D)
+    const size_t flags = 8 * (size_t)s->sched.ngroups * s->sched.nbx * s->sched.nby * s->sched.nbz;
+    DOMA_TRY(dalloc(s, &s->d_done, flags));
+    DOMA_CUDA_TRY(cudaMemset(s->d_done, 0, flags * sizeof(unsigned)));
+  }
 
   // per-cell kernels: fixed grid (determinism of the norms depends on it)
   int sms = 0;
@@ -334,31 +373,63 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   DOMA_TRY(dalloc(s, &s->d_partials, 2 * (size_t)grid));
   DOMA_TRY(dalloc(s, &s->d_ticket, 1));
   DOMA_CUDA_TRY(cudaMemset(s->d_ticket, 0, sizeof(unsigned)));
-  DOMA_TRY(dalloc(s, &s->d_norms, 4));
-  DOMA_CUDA_TRY(cudaMallocHost(&s->h_norms, 4 * sizeof(double)));
+  DOMA_TRY(dalloc(s, &s->d_ctl, 1));
+  DOMA_CUDA_TRY(cudaMemset(s->d_ctl, 0, sizeof(DevCtl)));
+  DOMA_CUDA_TRY(cudaMallocHost(&s->h_ctl, sizeof(DevCtl)));
+  std::memset(s->h_ctl, 0, sizeof(DevCtl));
+  {
+    // histories of the graph-driven solve: one entry per (MG iteration, group)
+    // pair and per MG iteration; every SI residual only for verbose output
+    const char * env = std::getenv("DOMA_SOLVE_LOOP");
+    s->use_graph = !(env && std::string(env) == "host");
+    s->pair_cap = (unsigned)std::min<uint64_t>((uint64_t)o->mg_max_it * s->G + s->G, 1u << 22);
+    s->mg_cap = std::max(1u, o->mg_max_it);
+    DOMA_TRY(dalloc(s, &s->d_pair_counts, s->pair_cap));
+    DOMA_TRY(dalloc(s, &s->d_pair_res, s->pair_cap));
+    DOMA_TRY(dalloc(s, &s->d_mg_hist, s->mg_cap));
+    if (o->verbose >= 2) {
+      s->hist_cap = std::min<uint64_t>((uint64_t)o->fs_max_it * s->pair_cap, 1ull << 24);
+      DOMA_TRY(dalloc(s, &s->d_si_hist, (size_t)s->hist_cap));
+    }
+  }
   DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
   s->stream = s->own_stream;
 
   // kernel argument blocks
-  auto fill = [&](auto & a, auto * q, auto * st, auto * x, auto * y, auto * z) {
+  auto fill = [&](auto & a, auto * tp) {
+    using T = std::remove_pointer_t<decltype(tp)>;
     a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
-    a.d_oct = s->d_oct; a.d_total = s->D;
-    a.tx = s->sched.tx; a.ty = s->sched.ty; a.tz = s->sched.tz;
+    a.d_oct = s->d_oct; a.d_total = s->D; a.ngroups = s->sched.ngroups;
+    a.nbx = s->sched.nbx; a.nby = s->sched.nby; a.nbz = s->sched.nbz;
+    a.num_tasks = (int)s->sched.tasks.size();
     a.tasks = s->d_tasks; a.task_offset = 0; a.oct_offset = s->d_oct_offset;
     a.amu = s->d_amu; a.aeta = s->d_aeta; a.axi = s->d_axi; a.wgt = s->d_w;
     a.amu_f = s->d_amu_f; a.aeta_f = s->d_aeta_f; a.axi_f = s->d_axi_f;
-    a.dx = s->d_dx; a.dy = s->d_dy; a.dz = s->d_dz;
-    a.q = q; a.sigt = st; a.xf = x; a.yf = y; a.zf = z;
+    a.wx = (const T *)s->d_wx; a.wy = (const T *)s->d_wy; a.wz = (const T *)s->d_wz;
+    a.cx = (const T *)s->d_cx; a.cy = (const T *)s->d_cy; a.cz = (const T *)s->d_cz;
+    a.q = (const T *)s->d_q; a.sigt = (const T *)s->d_sigt;
+    a.xf = (T *)s->d_xf; a.yf = (T *)s->d_yf; a.zf = (T *)s->d_zf;
     a.wpsi = s->d_wpsi; a.octphi = s->d_octphi; a.theta = o->theta;
+    a.ticket = &s->d_ctl->ticket; a.exit_count = &s->d_ctl->exit_count;
+    a.epoch = &s->d_ctl->epoch; a.done = s->d_done; a.error = &s->d_ctl->error;
+    a.spin_limit = 1u << 22;
+    a.wait_bias = 0u;
+    // Failure-detection test: every upstream wait targets an epoch nobody
+    // publishes and gives up after 2000 polls, so the sweep reports
+    // DOMA_DEVICE_WAIT_TIMEOUT without hanging or faulting.
+    const char * wt = std::getenv("DOMA_SWEEP_WAIT_TEST");
+    if (wt && std::string(wt) == "1") {
+      a.spin_limit = 2000u;
+      a.wait_bias = 0x40000000u;
+    }
   };
   if (exact)
-    fill(s->a64, (const double *)s->d_q, (const double *)s->d_sigt, (double *)s->d_xf,
-         (double *)s->d_yf, (double *)s->d_zf);
+    fill(s->a64, (double *)nullptr);
   else
-    fill(s->a32, (const float *)s->d_q, (const float *)s->d_sigt, (float *)s->d_xf,
-         (float *)s->d_yf, (float *)s->d_zf);
+    fill(s->a32, (float *)nullptr);
   IterArgs & it = s->it;
   it.N = N; it.G = s->G; it.D = s->D; it.grid = grid; it.oct_mask = s->oct_mask;
+  it.ngroups = s->sched.ngroups;
   it.src_scale = s->dims == 3 ? 0.25 : 0.5;
   it.vol = s->d_vol; it.mat = s->d_mat; it.total = s->d_total; it.scatter = s->d_scatter;
   it.source = s->d_source; it.fis = s->d_fis; it.chi = s->d_chi; it.nsf = s->d_nsf;
@@ -375,8 +446,10 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
 void release(doma_solver * s)
 {
   if (!s) return;
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
   for (void * p : s->allocations) cudaFree(p);
-  if (s->h_norms) cudaFreeHost(s->h_norms);
+  if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
 }
@@ -387,22 +460,27 @@ doma_status sweep_once(doma_solver * s)
                       s->stream, &s->launches);
 }
 
-// One source iteration: sweep, epilogue; norms land in d_norms[0..1].
+// One source iteration: sweep, epilogue; norms land in d_ctl->norms[0..1].
 doma_status source_iteration(doma_solver * s, int g)
 {
   DOMA_TRY(sweep_once(s));
-  DOMA_TRY(launch_si_epilogue(s->it, g, s->opts.precision, s->d_q, s->d_norms, s->stream));
+  DOMA_TRY(launch_si_epilogue(s->it, g, s->opts.precision, s->d_q, s->d_ctl->norms, LoopParams{}, s->stream));
   ++s->launches;
   return DOMA_OK;
 }
 
+// Read a norm pair and the sweep error flag (synchronises the stream).
 doma_status read_norms(doma_solver * s, int first, double * diff, double * tot)
 {
-  DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_norms + first, s->d_norms + first, 2 * sizeof(double),
+  DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->d_ctl, offsetof(DevCtl, ticket),
                                 cudaMemcpyDeviceToHost, s->stream));
   DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
-  *diff = s->h_norms[first];
-  *tot = s->h_norms[first + 1];
+  if (s->h_ctl->error) {
+    set_error("a sweep wait for an upstream block timed out");
+    return DOMA_DEVICE_WAIT_TIMEOUT;
+  }
+  *diff = s->h_ctl->norms[first];
+  *tot = s->h_ctl->norms[first + 1];
   return DOMA_OK;
 }
 
@@ -411,8 +489,251 @@ double ratio(double diff, double tot)
   return tot > 1e-8 ? std::sqrt(diff) / std::sqrt(tot) : 0.0;
 }
 
+LoopParams loop_params(doma_solver * s, int G)
+{
+  LoopParams L;
+  L.ctl = s->d_ctl;
+  L.pair_counts = s->d_pair_counts;
+  L.pair_res = s->d_pair_res;
+  L.pair_cap = s->pair_cap;
+  L.si_hist = s->d_si_hist;
+  L.hist_cap = s->hist_cap;
+  L.mg_hist = s->d_mg_hist;
+  L.mg_cap = s->mg_cap;
+  L.fs_tol = s->opts.fs_tol;
+  L.mg_tol = s->opts.mg_tol;
+  L.fs_max_it = s->opts.fs_max_it;
+  L.mg_max_it = s->opts.mg_max_it;
+  L.G = G;
+  L.graph = 1;
+  return L;
+}
+
+// Insert a WHILE conditional node at the current position of a capture and
+// return its (empty) body graph.
+doma_status add_while(cudaStream_t cap, cudaGraphConditionalHandle h, cudaGraph_t * body)
+{
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t * deps = nullptr;
+  size_t ndeps = 0;
+  DOMA_CUDA_TRY(cudaStreamGetCaptureInfo(cap, &st, nullptr, &g, &deps, nullptr, &ndeps));
+  if (st != cudaStreamCaptureStatusActive) {
+    set_error("stream is not capturing");
+    return DOMA_CUDA_ERROR;
+  }
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  DOMA_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np));
+  DOMA_CUDA_TRY(cudaStreamUpdateCaptureDependencies(cap, &node, nullptr, 1,
+                                                    cudaStreamSetCaptureDependencies));
+  *body = np.conditional.phGraph_out[0];
+  return DOMA_OK;
+}
+
+// The whole fixed-source solve as one graph:
+//   WHILE(mg) { for g: mg_source(g) ; WHILE(si_g) { sweep ; si_epilogue(g) } ;
+//               mg_residual }
+// mg_source arms its group's SI loop, the epilogue decides whether the SI
+// loop goes on, the Gauss-Seidel residual kernel decides the outer loop.
+doma_status build_graph(doma_solver * s)
+{
+  cudaStream_t c0 = nullptr, c1 = nullptr, c2 = nullptr;
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c1, cudaStreamNonBlocking));
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c2, cudaStreamNonBlocking));
+  doma_status status = DOMA_OK;
+  auto fail = [&](doma_status st) {
+    status = st;
+    return st;
+  };
+  auto run = [&]() -> doma_status {
+    cudaGraph_t root = nullptr;
+    if (cudaGraphCreate(&root, 0) != cudaSuccess) return fail(DOMA_CUDA_ERROR);
+    s->graph = root;
+    cudaGraphConditionalHandle mg_h;
+    DOMA_CUDA_TRY(cudaGraphConditionalHandleCreate(&mg_h, root, 1u, cudaGraphCondAssignDefault));
+    std::vector<cudaGraphConditionalHandle> si_h(s->G);
+    for (int g = 0; g < s->G; ++g)
+      DOMA_CUDA_TRY(cudaGraphConditionalHandleCreate(&si_h[g], root, 0u, 0u));
+
+    DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c0, root, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t mg_body = nullptr;
+    doma_status st = add_while(c0, mg_h, &mg_body);
+    if (st == DOMA_OK) {
+      DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c1, mg_body, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+      for (int g = 0; g < s->G && st == DOMA_OK; ++g) {
+        LoopParams L = loop_params(s, s->G);
+        L.si_handle = si_h[g];
+        L.mg_handle = mg_h;
+        st = launch_mg_source(s->it, g, s->opts.precision, s->d_q, s->d_sigt, L, c1);
+        cudaGraph_t si_body = nullptr;
+        if (st == DOMA_OK) st = add_while(c1, si_h[g], &si_body);
+        if (st == DOMA_OK) {
+          DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c2, si_body, nullptr, nullptr, 0,
+                                                      cudaStreamCaptureModeThreadLocal));
+          st = launch_sweep(s->dims, s->opts.precision, s->opts.scheme, s->sched, &s->a64,
+                            &s->a32, c2, nullptr);
+          if (st == DOMA_OK)
+            st = launch_si_epilogue(s->it, g, s->opts.precision, s->d_q, s->d_ctl->norms, L, c2);
+          cudaGraph_t out = nullptr;
+          DOMA_CUDA_TRY(cudaStreamEndCapture(c2, &out));
+        }
+      }
+      if (st == DOMA_OK) {
+        LoopParams L = loop_params(s, s->G);
+        L.mg_handle = mg_h;
+        st = launch_mg_residual(s->it, s->d_ctl->norms + 2, L, c1);
+      }
+      cudaGraph_t out = nullptr;
+      DOMA_CUDA_TRY(cudaStreamEndCapture(c1, &out));
+    }
+    cudaGraph_t out = nullptr;
+    DOMA_CUDA_TRY(cudaStreamEndCapture(c0, &out));
+    if (st != DOMA_OK) return fail(st);
+    DOMA_CUDA_TRY(cudaGraphInstantiate(&s->graph_exec, root, 0));
+    return DOMA_OK;
+  };
+  doma_status st = run();
+  cudaStreamDestroy(c0);
+  cudaStreamDestroy(c1);
+  cudaStreamDestroy(c2);
+  if (st != DOMA_OK && status == DOMA_OK) status = st;
+  return status;
+}
+
+// Print DOMA's progress lines (src/TransportSolver3D.cpp:268-315,466-494)
+// from the histories the graph recorded.
+void print_history(doma_solver * s, const DevCtl & c, const std::vector<unsigned> & counts,
+                   const std::vector<double> & pres, const std::vector<double> & mgh,
+                   const std::vector<double> & sih)
+{
+  const int G = s->G;
+  const int verbose = (int)s->opts.verbose;
+  std::printf("Solving...\nInitializing the solver...\n");
+  size_t pair = 0, hist = 0;
+  for (unsigned m = 0;; ++m) {
+    if (pair >= c.pairs) break;
+    if (m != 0u)
+      std::printf("Performing MGI %u, residual = %g\n", m, mgh[m - 1]);
+    else
+      std::printf("Performing MGI %u\n", m);
+    std::printf("----------------------------------------------------------------------------------\n");
+    bool stop = false;
+    for (int g = 0; g < G && pair < c.pairs; ++g, ++pair) {
+      const unsigned n = pair < counts.size() ? counts[pair] : 0u;
+      const double r = pair < pres.size() ? pres[pair] : 0.0;
+      if (verbose >= 2)
+        for (unsigned k = 0; k < n; ++k, ++hist) {
+          if (k != 0u && hist - 1 < sih.size())
+            std::printf("Performing SI %u for G%d, residual = %g\n", k, g, sih[hist - 1]);
+          else
+            std::printf("Performing SI %u for G%d\n", k, g);
+        }
+      if (n < s->opts.fs_max_it && !(c.failed && pair + 1 == c.pairs)) {
+        std::printf("SI converged after %u iterations with a residual of %g for G%d\n", n, r, g);
+      } else {
+        std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n", n, r, g);
+        stop = true;
+      }
+    }
+    if (stop) break;
+  }
+  if (!c.failed) {
+    if (c.mg_it < s->opts.mg_max_it) {
+      if (G > 1)
+        std::printf("MGI converged after %u iterations with a residual of %g\n", c.mg_it, c.mg_res);
+    } else {
+      std::printf("MGI failed to converge after %u iterations with a residual of %g\n", c.mg_it,
+                  c.mg_res);
+    }
+  }
+  std::fflush(stdout);
+}
+
+doma_status solve_graph(doma_solver * s, doma_report * r)
+{
+  const size_t G = s->G, N = s->N;
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!s->graph_exec) DOMA_TRY(build_graph(s));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
+  // clear error and loop state; keep the persistent-sweep counters
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->si_it, 0, sizeof(DevCtl) - offsetof(DevCtl, si_it),
+                                s->stream));
+  DOMA_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+  DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s->stream));
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  const DevCtl c = *s->h_ctl;
+  const size_t npairs = std::min<size_t>(c.pairs, s->pair_cap);
+  std::vector<unsigned> counts(npairs);
+  std::vector<double> pres(npairs), mgh(std::min<size_t>(c.mg_it, s->mg_cap)), sih;
+  if (npairs) {
+    DOMA_CUDA_TRY(cudaMemcpy(counts.data(), s->d_pair_counts, npairs * sizeof(unsigned),
+                             cudaMemcpyDeviceToHost));
+    DOMA_CUDA_TRY(cudaMemcpy(pres.data(), s->d_pair_res, npairs * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+  }
+  if (!mgh.empty())
+    DOMA_CUDA_TRY(cudaMemcpy(mgh.data(), s->d_mg_hist, mgh.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+  if (s->d_si_hist && c.hist_len) {
+    sih.resize(std::min<unsigned long long>(c.hist_len, s->hist_cap));
+    DOMA_CUDA_TRY(cudaMemcpy(sih.data(), s->d_si_hist, sih.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+  }
+  if (s->opts.verbose) print_history(s, c, counts, pres, mgh, sih);
+
+  doma_status status = DOMA_OK;
+  if (c.failed == DOMA_DEVICE_WAIT_TIMEOUT) {
+    set_error("a sweep wait for an upstream block timed out");
+    status = DOMA_DEVICE_WAIT_TIMEOUT;
+  } else if (c.failed == DOMA_NUMERIC_ERROR) {
+    set_error("a residual norm is not finite");
+    status = DOMA_NUMERIC_ERROR;
+  } else if (c.failed == DOMA_NOT_CONVERGED) {
+    set_error("source iteration reached fs_max_it");
+    status = DOMA_NOT_CONVERGED;
+  } else if (!(c.mg_it < s->opts.mg_max_it)) {
+    set_error("Gauss-Seidel iteration reached mg_max_it");
+    status = DOMA_NOT_CONVERGED;
+  }
+  // kernel launches: the graph launches G mg_source + one MG residual per MG
+  // iteration and (sweep launches + 1) per source iteration
+  uint64_t per_sweep = s->sched.persistent ? 1 : 0;
+  if (!s->sched.persistent)
+    for (size_t L = 0; L + 1 < s->sched.level_begin.size(); ++L)
+      per_sweep += s->sched.level_begin[L + 1] > s->sched.level_begin[L];
+  const uint64_t launches = c.sweeps * (per_sweep + 1) +
+                            (uint64_t)(c.mg_it + (c.failed ? 1 : 0)) * (uint64_t)(s->G + 1);
+  s->launches += launches;
+  const auto t1 = std::chrono::steady_clock::now();
+  if (r) {
+    r->status = status;
+    r->mg_iterations = c.mg_it;
+    r->si_iterations = c.sweeps;
+    r->updates = c.sweeps * (uint64_t)s->N * (uint64_t)s->D;
+    r->kernel_launches = launches;
+    r->mg_residual = c.mg_res;
+    r->si_residual = c.si_res;
+    r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    r->si_counts_len = c.pairs;
+    if (r->si_counts)
+      for (size_t k = 0; k < npairs && k < r->si_counts_capacity; ++k) r->si_counts[k] = counts[k];
+  }
+  return status;
+}
+
 doma_status solve_impl(doma_solver * s, doma_report * r)
 {
+  if (s->use_graph) return solve_graph(s, r);
   const doma_options & o = s->opts;
   const int verbose = (int)o.verbose;
   const size_t G = s->G, N = s->N;
@@ -423,6 +744,7 @@ doma_status solve_impl(doma_solver * s, doma_report * r)
   }
   DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
   DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
 
   uint64_t sweeps = 0;
   size_t si_len = 0;
@@ -438,7 +760,7 @@ doma_status solve_impl(doma_solver * s, doma_report * r)
       std::printf("----------------------------------------------------------------------------------\n");
     }
     for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
-      DOMA_TRY(launch_mg_source(s->it, g, o.precision, s->d_q, s->d_sigt, s->stream));
+      DOMA_TRY(launch_mg_source(s->it, g, o.precision, s->d_q, s->d_sigt, LoopParams{}, s->stream));
       ++s->launches;
       unsigned it = 0;
       si_res = 0.0;
@@ -476,7 +798,7 @@ doma_status solve_impl(doma_solver * s, doma_report * r)
       }
     }
     if (status != DOMA_OK) break;
-    DOMA_TRY(launch_mg_residual(s->it, s->d_norms + 2, s->stream));
+    DOMA_TRY(launch_mg_residual(s->it, s->d_ctl->norms + 2, LoopParams{}, s->stream));
     ++s->launches;
     double diff, tot;
     DOMA_TRY(read_norms(s, 2, &diff, &tot));
@@ -597,7 +919,8 @@ doma_status doma_solver_source_iterations(doma_solver * s, uint32_t group, uint3
 {
   if (!s) return bad("null solver");
   if ((int)group >= s->G) return bad("group out of range");
-  DOMA_TRY(launch_mg_source(s->it, (int)group, s->opts.precision, s->d_q, s->d_sigt, s->stream));
+  DOMA_TRY(launch_mg_source(s->it, (int)group, s->opts.precision, s->d_q, s->d_sigt, LoopParams{},
+                            s->stream));
   ++s->launches;
   for (uint32_t i = 0; i < count; ++i) DOMA_TRY(source_iteration(s, (int)group));
   return DOMA_OK;

@@ -18,9 +18,16 @@
 // in shared memory (one slot per (kl, il) and (jl, il), written by one thread
 // and read by its downwind neighbour on the next step).  Faces crossing a
 // block boundary go through per-octant global face planes, one slot per face
-// position: the next block along that axis reads it only after this block's
-// launch has finished.  Tasks are launched level by level (level =
-// bi + bj + bk); a level holds every independent task of all octants.
+// position, read only after the upstream block has published them.
+//
+// Scheduling.  A persistent grid (the CTAs that fit on the device) claims
+// tasks from a ticket counter in level order (level = bi + bj + bk, all
+// octants interleaved), stages the task's cell data, waits -- bounded, with
+// an acquire load -- for the done flags of its upstream blocks, and publishes
+// its own done flag (the sweep's epoch number) with a release store.  The
+// last CTA to leave re-arms the counters, so consecutive sweeps need no
+// host work.  A level-synchronous variant (one launch per level, ordering by
+// kernel boundaries) runs the same task body and is kept for cross-checks.
 //
 // Arithmetic.
 //   * double ("exact"): each cell solve evaluates DOMA's expression with
@@ -151,24 +158,33 @@ __device__ __forceinline__ double twdd2_exact(double q, double st, double amu, d
 }
 
 // ---- single-precision cell solves ------------------------------------------
+// Every operation is an explicit intrinsic (separately rounded add/mul, fused
+// multiply-add where written), so the compiler has no contraction choices and
+// the bits do not depend on which kernel the solve is inlined into.
+
+__device__ __forceinline__ float fA(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fS(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fM(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fF(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 // DD with cx = 2|mu|/lx etc.: psi = (q + cx x + cy y + cz z) / (cx + cy + cz + st).
 __device__ __forceinline__ float dd_f32(float q, float st, float cx, float cy, float cz,
                                         float & x, float & y, float & z)
 {
-  const float num = fmaf(cz, z, fmaf(cy, y, fmaf(cx, x, q)));
-  const float c = __fdividef(num, cx + cy + cz + st);
-  x = fmaf(2.0f, c, -x);
-  y = fmaf(2.0f, c, -y);
-  z = fmaf(2.0f, c, -z);
+  const float num = fF(cz, z, fF(cy, y, fF(cx, x, q)));
+  const float c = __fdividef(num, fA(fA(fA(cx, cy), cz), st));
+  x = fF(2.0f, c, -x);
+  y = fF(2.0f, c, -y);
+  z = fF(2.0f, c, -z);
   return c;
 }
 
+// TW-DD weight: 1 - num / (den * flux), clamped to [0.5, 1]; 0.5 when the
+// upwind flux is <= 1e-8 (include/TWDiamondDifference3D.h:43-75).
 __device__ __forceinline__ float tw_weight(float num, float den_in, float flux)
 {
-  // 1 - num / (den_in * flux), clamped to [0.5, 1]; 0.5 when the upwind flux is <= 1e-8.
   float a = 0.5f;
-  if (flux > 1e-8f) a = 1.0f - __fdividef(num, den_in * flux);
+  if (flux > 1e-8f) a = fS(1.0f, __fdividef(num, fM(den_in, flux)));
   return fminf(fmaxf(a, 0.5f), 1.0f);
 }
 
@@ -176,143 +192,182 @@ __device__ __forceinline__ float twdd3_f32(float q, float st, float amu, float a
                                            float lx, float ly, float lz, float th, float & x,
                                            float & y, float & z)
 {
-  const float A = ly * lz, B = lx * lz, C = lx * ly, V = lx * ly * lz;
-  const float muA = amu * A, etB = aeta * B, xiC = axi * C;
-  const float qVt = q * V * th, sV = st * V;
-  const float mx = muA * x, ey = etB * y, xz = xiC * z;
-  const float a = tw_weight(qVt + (ey + xz) * th + mx, sV + 2.0f * (etB + xiC), x);
-  const float b = tw_weight(qVt + (mx + xz) * th + ey, sV + 2.0f * (muA + xiC), y);
-  const float c3 = tw_weight(qVt + (mx + ey) * th + xz, sV + 2.0f * (muA + etB), z);
+  const float A = fM(ly, lz), B = fM(lx, lz), C = fM(lx, ly), V = fM(fM(lx, ly), lz);
+  const float muA = fM(amu, A), etB = fM(aeta, B), xiC = fM(axi, C);
+  const float qV = fM(q, V), qVt = fM(qV, th), sV = fM(st, V);
+  const float mx = fM(muA, x), ey = fM(etB, y), xz = fM(xiC, z);
+  const float a = tw_weight(fF(fA(ey, xz), th, fA(qVt, mx)), fF(2.0f, fA(etB, xiC), sV), x);
+  const float b = tw_weight(fF(fA(mx, xz), th, fA(qVt, ey)), fF(2.0f, fA(muA, xiC), sV), y);
+  const float c3 = tw_weight(fF(fA(mx, ey), th, fA(qVt, xz)), fF(2.0f, fA(muA, etB), sV), z);
   const float ra = __frcp_rn(a), rb = __frcp_rn(b), rc = __frcp_rn(c3);
-  const float ta = muA * ra, tb = etB * rb, tc = xiC * rc;
-  const float c = __fdividef(fmaf(tc, z, fmaf(tb, y, fmaf(ta, x, q * V))), sV + ta + tb + tc);
-  x = (c - (1.0f - a) * x) * ra;
-  y = (c - (1.0f - b) * y) * rb;
-  z = (c - (1.0f - c3) * z) * rc;
+  const float ta = fM(muA, ra), tb = fM(etB, rb), tc = fM(xiC, rc);
+  const float c = __fdividef(fF(tc, z, fF(tb, y, fF(ta, x, qV))), fA(fA(fA(sV, ta), tb), tc));
+  x = fM(fF(fS(a, 1.0f), x, c), ra);   // (c - (1 - a) x) / a
+  y = fM(fF(fS(b, 1.0f), y, c), rb);
+  z = fM(fF(fS(c3, 1.0f), z, c), rc);
   return c;
 }
 
 __device__ __forceinline__ float dd2_f32(float q, float st, float cx, float cy, float & x,
                                          float & y)
 {
-  const float c = __fdividef(fmaf(cy, y, fmaf(cx, x, q)), cx + cy + st);
-  x = fmaf(2.0f, c, -x);
-  y = fmaf(2.0f, c, -y);
+  const float c = __fdividef(fF(cy, y, fF(cx, x, q)), fA(fA(cx, cy), st));
+  x = fF(2.0f, c, -x);
+  y = fF(2.0f, c, -y);
   return c;
 }
 
 __device__ __forceinline__ float twdd2_f32(float q, float st, float amu, float aeta, float axi,
                                            float lx, float ly, float th, float & x, float & y)
 {
-  const float A = ly, B = lx, V = lx * ly;
-  const float muA = amu * A, etB = aeta * B;
-  const float qVt = q * V * th, sV = st * V;
-  const float mx = muA * x, ey = etB * y;
-  const float a = tw_weight(qVt + ey * th + mx, sV + 2.0f * etB, x);
-  const float b = tw_weight(qVt + (mx + axi) * th + ey, sV + 2.0f * muA, y);
+  const float A = ly, B = lx, V = fM(lx, ly);
+  const float muA = fM(amu, A), etB = fM(aeta, B);
+  const float qV = fM(q, V), qVt = fM(qV, th), sV = fM(st, V);
+  const float mx = fM(muA, x), ey = fM(etB, y);
+  const float a = tw_weight(fF(ey, th, fA(qVt, mx)), fF(2.0f, etB, sV), x);
+  const float b = tw_weight(fF(fA(mx, axi), th, fA(qVt, ey)), fF(2.0f, muA, sV), y);
   const float ra = __frcp_rn(a), rb = __frcp_rn(b);
-  const float ta = muA * ra, tb = etB * rb;
-  const float c = __fdividef(fmaf(tb, y, fmaf(ta, x, q * V)), sV + ta + tb);
-  x = (c - (1.0f - a) * x) * ra;
-  y = (c - (1.0f - b) * y) * rb;
+  const float ta = fM(muA, ra), tb = fM(etB, rb);
+  const float c = __fdividef(fF(tb, y, fF(ta, x, qV)), fA(fA(sV, ta), tb));
+  x = fM(fF(fS(a, 1.0f), x, c), ra);
+  y = fM(fF(fS(b, 1.0f), y, c), rb);
   return c;
 }
 
-// ---- the sweep kernel ------------------------------------------------------
+// ---- scheduling primitives -------------------------------------------------
 
-template <typename T, int DIMS, int SCHEME>
-__global__ void __launch_bounds__(kMaxSweepThreads) sweep_kernel(const SweepArgs<T> A)
+__device__ __forceinline__ void st_release(unsigned * p, unsigned v)
 {
-  constexpr bool EXACT = std::is_same<T, double>::value;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
-  const Task task = A.tasks[A.task_offset + blockIdx.x];
-  const int o = task.oct;
+__device__ __forceinline__ unsigned ld_acquire(const unsigned * p)
+{
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_relaxed(const int * p)
+{
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Wait until *flag == epoch.  Bounded: after `limit` polls (with exponential
+// back-off up to ~1 us) it records DOMA_DEVICE_WAIT_TIMEOUT in *error and
+// returns false; it also gives up at once when another CTA has already failed.
+__device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, int * error)
+{
+  unsigned ns = 32;
+  for (unsigned it = 0; it < limit; ++it) {
+    if (ld_acquire(flag) == epoch) return true;
+    if (ld_relaxed(error) != 0) return false;
+    __nanosleep(ns);
+    if (ns < 1024) ns *= 2;
+  }
+  atomicCAS(error, 0, (int)DOMA_DEVICE_WAIT_TIMEOUT);
+  return false;
+}
+
+// ---- one task: (octant, ordinate group, block) --------------------------------
+//
+// Lanes are pencil-major: a warp holds two ordinates, each over a 16-pencil
+// cross-section of the block (4 x 4 in (y, z) for 3D, 16 in y for 2D), and
+// every thread walks its x-pencil on the skewed schedule il = s - jl - kl.
+// A cell's y-upwind neighbour is then lane - 1 and its z-upwind neighbour
+// lane - PY, both computed on the previous step, so faces move between
+// lanes with __shfl_up_sync and the warps advance with no block barrier.
+// Shared memory carries only the block-boundary faces (staged in and out
+// coalesced) and, in fp32 mode, the w*psi values for the angular reduction.
+
+template <int DIMS> struct Pencils;
+template <> struct Pencils<3> { static constexpr int PY = 4, PZ = 4; };
+template <> struct Pencils<2> { static constexpr int PY = 16, PZ = 1; };
+
+template <typename T, int DIMS, int TX>
+struct TaskSmem {
+  static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
+  static constexpr int CELLS = TX * PY * PZ;
+  static constexpr int YF = PZ * TX * kGroup;                  // y faces [PZ][TX][kGroup]
+  static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
+  static constexpr int NT = 2 * YF + 2 * ZF + 2 * CELLS + TX + PY + PZ + kGroup * (TX + PY + PZ);
+  static constexpr bool EXACT = std::is_same<T, double>::value;
+  static constexpr size_t bytes = NT * sizeof(T) + (EXACT ? 0 : (size_t)kGroup * CELLS * sizeof(float));
+};
+
+template <typename T, int DIMS, int SCHEME, int TX>
+__device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task,
+                                         unsigned char * smem_raw, bool dataflow, unsigned epoch)
+{
+  using SM = TaskSmem<T, DIMS, TX>;
+  constexpr bool EXACT = SM::EXACT;
+  constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int o = task.oct, og = task.og;
   const bool rx = (o & 4) != 0, ry = (o & 2) != 0, rz = (o & 1) != 0;
-  const int TX = A.tx, TY = A.ty, TZ = DIMS == 3 ? A.tz : 1;
-  const int Do = A.d_oct;
   const int nx = A.nx, ny = A.ny, nz = DIMS == 3 ? A.nz : 1;
-  const int i0 = task.bi * TX, j0 = task.bj * TY, k0 = task.bk * TZ;
-  const int vx = min(TX, nx - i0), vy = min(TY, ny - j0), vz = min(TZ, nz - k0);
-  const int cells = TX * TY * TZ;
+  const int Do = A.d_oct;
+  const int n0 = og * kGroup;
+  const int gs = min(kGroup, Do - n0);
+  const int i0 = task.bi * TX, j0 = task.bj * PY, k0 = task.bk * PZ;
+  const int vx = min(TX, nx - i0), vy = min(PY, ny - j0), vz = min(PZ, nz - k0);
 
   const int t = threadIdx.x;
-  const int n = t % Do;
-  const int pen = t / Do;
-  const int jl = pen % TY;
-  const int kl = pen / TY;
-  const bool active = jl < vy && kl < vz;
-  const int ord = A.oct_offset[o] + n;
+  const int lane = t & 31;
+  const int p = lane & 15;
+  const int nl = (t >> 5) * 2 + (lane >> 4);
+  const int jl = DIMS == 3 ? (p & 3) : p;
+  const int kl = DIMS == 3 ? (p >> 2) : 0;
+  const bool active = nl < gs && jl < vy && kl < vz;
+  const int ob = A.oct_offset[o] + n0;        // first global ordinate of the group
+  const int ord = ob + min(nl, gs - 1);
 
-  // shared memory carve-up (all T-sized arrays first, then the float buffer)
-  T * yface = reinterpret_cast<T *>(smem_raw);     // [TZ][TX][Do]
-  T * zface = yface + TZ * TX * Do;                // [TY][TX][Do] (3D)
-  T * qs = zface + (DIMS == 3 ? TY * TX * Do : 0); // [TZ][TY][TX]
-  T * ss = qs + cells;                             // [TZ][TY][TX]
-  T * lxs = ss + cells;                            // [TX]
-  T * lys = lxs + TX;                              // [TY]
-  T * lzs = lys + TY;                              // [TZ]
-  T * cxs = lzs + TZ;                              // [Do][TX]  2|mu|/lx
-  T * cys = cxs + Do * TX;                         // [Do][TY]  2|eta|/ly
-  T * czs = cys + Do * TY;                         // [Do][TZ]  2|xi|/lz
-  float * P = reinterpret_cast<float *>(czs + Do * TZ);  // fp32: [cells][Do]
+  T * yin = reinterpret_cast<T *>(smem_raw);
+  T * yout = yin + SM::YF;
+  T * zin = yout + SM::YF;
+  T * zout = zin + SM::ZF;
+  T * qs = zout + SM::ZF;
+  T * ss = qs + CELLS;
+  T * lxs = ss + CELLS;
+  T * lys = lxs + TX;
+  T * lzs = lys + PY;
+  T * cxs = lzs + PZ;                 // [kGroup][TX]
+  T * cys = cxs + kGroup * TX;        // [kGroup][PY]
+  T * czs = cys + kGroup * PY;        // [kGroup][PZ]
+  float * P = reinterpret_cast<float *>(czs + kGroup * PZ);  // fp32: [kGroup][CELLS]
 
   auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
   auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
   auto phys_k = [&](int kk) { return rz ? nz - 1 - (k0 + kk) : k0 + kk; };
 
-  // -- prologue: stage cell data, widths, coefficients and incoming faces --
-  for (int e = t; e < cells; e += blockDim.x) {
-    const int il = e % TX, r = e / TX, jj = r % TY, kk = r / TY;
+  // -- stage what does not depend on upstream blocks ----------------------------
+  for (int e = t; e < CELLS; e += blockDim.x) {
+    const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
     if (il < vx && jj < vy && kk < vz) {
       const size_t c = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
       qs[e] = A.q[c];
       ss[e] = A.sigt[c];
     }
   }
-  for (int e = t; e < TX; e += blockDim.x) lxs[e] = e < vx ? (T)A.dx[phys_i(e)] : (T)1;
-  for (int e = t; e < TY; e += blockDim.x) lys[e] = e < vy ? (T)A.dy[phys_j(e)] : (T)1;
+  for (int e = t; e < TX; e += blockDim.x) lxs[e] = e < vx ? A.wx[phys_i(e)] : (T)1;
+  for (int e = t; e < PY; e += blockDim.x) lys[e] = e < vy ? A.wy[phys_j(e)] : (T)1;
   if (DIMS == 3)
-    for (int e = t; e < TZ; e += blockDim.x) lzs[e] = e < vz ? (T)A.dz[phys_k(e)] : (T)1;
-  const int ob = A.oct_offset[o];
-  for (int e = t; e < Do * TX; e += blockDim.x) {
+    for (int e = t; e < PZ; e += blockDim.x) lzs[e] = e < vz ? A.wz[phys_k(e)] : (T)1;
+  for (int e = t; e < kGroup * TX; e += blockDim.x) {
     const int nn = e / TX, il = e % TX;
-    const double lx = il < vx ? A.dx[phys_i(il)] : 1.0;
-    cxs[e] = EXACT ? (T)dD(dM(2.0, A.amu[ob + nn]), lx) : (T)(2.0 * A.amu[ob + nn] / lx);
+    cxs[e] = (nn < gs && il < vx) ? A.cx[(size_t)(ob + nn) * nx + phys_i(il)] : (T)0;
   }
-  for (int e = t; e < Do * TY; e += blockDim.x) {
-    const int nn = e / TY, jj = e % TY;
-    const double ly = jj < vy ? A.dy[phys_j(jj)] : 1.0;
-    cys[e] = EXACT ? (T)dD(dM(2.0, A.aeta[ob + nn]), ly) : (T)(2.0 * A.aeta[ob + nn] / ly);
+  for (int e = t; e < kGroup * PY; e += blockDim.x) {
+    const int nn = e / PY, jj = e % PY;
+    cys[e] = (nn < gs && jj < vy) ? A.cy[(size_t)(ob + nn) * ny + phys_j(jj)] : (T)0;
   }
   if (DIMS == 3)
-    for (int e = t; e < Do * TZ; e += blockDim.x) {
-      const int nn = e / TZ, kk = e % TZ;
-      const double lz = kk < vz ? A.dz[phys_k(kk)] : 1.0;
-      czs[e] = EXACT ? (T)dD(dM(2.0, A.axi[ob + nn]), lz) : (T)(2.0 * A.axi[ob + nn] / lz);
+    for (int e = t; e < kGroup * PZ; e += blockDim.x) {
+      const int nn = e / PZ, kk = e % PZ;
+      czs[e] = (nn < gs && kk < vz) ? A.cz[(size_t)(ob + nn) * nz + phys_k(kk)] : (T)0;
     }
-  // y faces: smem [kk][il][nn] <- global yf[o][k'][i'][nn]
-  for (int e = t; e < TZ * TX * Do; e += blockDim.x) {
-    const int nn = e % Do, r = e / Do, il = r % TX, kk = r / TX;
-    T v = (T)0;
-    if (task.bj > 0 && il < vx && kk < vz)
-      v = A.yf[(((size_t)o * nz + (k0 + kk)) * nx + (i0 + il)) * Do + nn];
-    yface[e] = v;
-  }
-  if (DIMS == 3) {
-    // z faces: smem [jj][il][nn] <- global zf[o][j'][i'][nn]
-    for (int e = t; e < TY * TX * Do; e += blockDim.x) {
-      const int nn = e % Do, r = e / Do, il = r % TX, jj = r / TX;
-      T v = (T)0;
-      if (task.bk > 0 && il < vx && jj < vy)
-        v = A.zf[(((size_t)o * ny + (j0 + jj)) * nx + (i0 + il)) * Do + nn];
-      zface[e] = v;
-    }
-  }
-  T xin = (T)0;
-  const size_t xslot = (((size_t)o * nz + (k0 + kl)) * ny + (j0 + jl)) * Do + n;
-  if (active && task.bi > 0) xin = A.xf[xslot];
-
   T amu, aeta, axi;
   if (EXACT) {
     amu = (T)A.amu[ord]; aeta = (T)A.aeta[ord]; axi = (T)A.axi[ord];
@@ -323,31 +378,74 @@ __global__ void __launch_bounds__(kMaxSweepThreads) sweep_kernel(const SweepArgs
   const float wgt_f = (float)wgt;
   const T th = (T)A.theta;
   const size_t N = (size_t)nx * ny * nz;
+  const size_t slot = (size_t)o * A.ngroups + og;   // (octant, group) slot
+
+  // -- wait for the upstream blocks (dataflow mode) --------------------------------
+  if (dataflow) {
+    if (t == 0) {
+      const int nbx = A.nbx, nby = A.nby, nbz = A.nbz;
+      const size_t base = slot * nbz;
+      const unsigned want = epoch + A.wait_bias;
+      if (task.bi > 0)
+        wait_for(A.done + ((base + task.bk) * nby + task.bj) * nbx + task.bi - 1, want,
+                 A.spin_limit, A.error);
+      if (task.bj > 0)
+        wait_for(A.done + ((base + task.bk) * nby + task.bj - 1) * nbx + task.bi, want,
+                 A.spin_limit, A.error);
+      if (DIMS == 3 && task.bk > 0)
+        wait_for(A.done + ((base + task.bk - 1) * nby + task.bj) * nbx + task.bi, want,
+                 A.spin_limit, A.error);
+    }
+    __syncthreads();
+  }
+
+  // -- incoming faces (written by other CTAs: read through L2) -----------------------
+  for (int e = t; e < SM::YF; e += blockDim.x) {
+    const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
+    T v = (T)0;
+    if (task.bj > 0 && nn < gs && il < vx && kk < vz)
+      v = __ldcg(A.yf + (((size_t)o * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn);
+    yin[e] = v;
+  }
+  if (DIMS == 3)
+    for (int e = t; e < SM::ZF; e += blockDim.x) {
+      const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
+      T v = (T)0;
+      if (task.bk > 0 && nn < gs && il < vx && jj < vy)
+        v = __ldcg(A.zf + (((size_t)o * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn);
+      zin[e] = v;
+    }
+  T xin = (T)0;
+  const size_t xslot = (((size_t)o * nz + (k0 + kl)) * ny + (j0 + jl)) * Do + n0 + nl;
+  if (active && task.bi > 0) xin = __ldcg(A.xf + xslot);
   __syncthreads();
 
-  // -- wavefront: step s solves the cells with il + jl + kl == s ------------
-  const int steps = TX + TY + TZ - 2;
-  for (int s = 0; s < steps; ++s) {
+  // -- wavefront: step s solves the cells with il + jl + kl == s, warp-synchronously --
+  T ysh = (T)0, zsh = (T)0;   // faces handed over by the upwind lanes
+  T yo = (T)0, zo = (T)0;
+  constexpr int STEPS = TX + PY + PZ - 2;
+#pragma unroll 4
+  for (int s = 0; s < STEPS; ++s) {
     const int il = s - jl - kl;
-    if (active && il >= 0 && il < vx) {
-      const int e = (kl * TY + jl) * TX + il;
-      T & yref = yface[(kl * TX + il) * Do + n];
-      T y = yref;
+    const bool valid = active && il >= 0 && il < vx;
+    if (valid) {
+      T y = jl == 0 ? yin[(kl * TX + il) * kGroup + nl] : ysh;
       T z = (T)0;
-      if (DIMS == 3) z = zface[(jl * TX + il) * Do + n];
+      if (DIMS == 3) z = kl == 0 ? zin[(jl * TX + il) * kGroup + nl] : zsh;
+      const int e = (kl * PY + jl) * TX + il;
       const T q = qs[e], st = ss[e];
       T psi;
       if constexpr (EXACT) {
         if constexpr (DIMS == 3) {
           if constexpr (SCHEME == DOMA_SCHEME_DD) {
-            const double geo = dA(dA(cxs[n * TX + il], cys[n * TY + jl]), czs[n * TZ + kl]);
+            const double geo = dA(dA(cxs[nl * TX + il], cys[nl * PY + jl]), czs[nl * PZ + kl]);
             psi = dd3_exact(q, st, amu, aeta, axi, lxs[il], lys[jl], lzs[kl], geo, xin, y, z);
           } else {
             psi = twdd3_exact(q, st, amu, aeta, axi, lxs[il], lys[jl], lzs[kl], th, xin, y, z);
           }
         } else {
           if constexpr (SCHEME == DOMA_SCHEME_DD) {
-            const double geo = dA(cxs[n * TX + il], cys[n * TY + jl]);
+            const double geo = dA(cxs[nl * TX + il], cys[nl * PY + jl]);
             psi = dd2_exact(q, st, amu, aeta, lxs[il], lys[jl], geo, xin, y);
           } else {
             psi = twdd2_exact(q, st, amu, aeta, axi, lxs[il], lys[jl], th, xin, y);
@@ -358,128 +456,213 @@ __global__ void __launch_bounds__(kMaxSweepThreads) sweep_kernel(const SweepArgs
       } else {
         if constexpr (DIMS == 3) {
           if constexpr (SCHEME == DOMA_SCHEME_DD)
-            psi = dd_f32(q, st, cxs[n * TX + il], cys[n * TY + jl], czs[n * TZ + kl], xin, y, z);
+            psi = dd_f32(q, st, cxs[nl * TX + il], cys[nl * PY + jl], czs[nl * PZ + kl], xin, y, z);
           else
             psi = twdd3_f32(q, st, amu, aeta, axi, lxs[il], lys[jl], lzs[kl], th, xin, y, z);
         } else {
           if constexpr (SCHEME == DOMA_SCHEME_DD)
-            psi = dd2_f32(q, st, cxs[n * TX + il], cys[n * TY + jl], xin, y);
+            psi = dd2_f32(q, st, cxs[nl * TX + il], cys[nl * PY + jl], xin, y);
           else
             psi = twdd2_f32(q, st, amu, aeta, axi, lxs[il], lys[jl], th, xin, y);
         }
-        P[e * Do + n] = wgt_f * psi;
+        P[nl * CELLS + e] = fM(wgt_f, psi);
       }
-      yref = y;
-      if (DIMS == 3) zface[(jl * TX + il) * Do + n] = z;
+      yo = y;
+      zo = z;
+      if (jl == vy - 1) yout[(kl * TX + il) * kGroup + nl] = y;
+      if (DIMS == 3 && kl == vz - 1) zout[(jl * TX + il) * kGroup + nl] = z;
     }
-    __syncthreads();
+    ysh = __shfl_up_sync(FULL, yo, 1);
+    if (DIMS == 3) zsh = __shfl_up_sync(FULL, zo, PY);
   }
+  __syncthreads();
 
-  // -- epilogue: outgoing faces and (fp32) the per-octant scalar flux ---------
+  // -- outgoing faces and (fp32) the group's scalar-flux partial ------------------------
   if (active) A.xf[xslot] = xin;
-  for (int e = t; e < TZ * TX * Do; e += blockDim.x) {
-    const int nn = e % Do, r = e / Do, il = r % TX, kk = r / TX;
-    if (il < vx && kk < vz) A.yf[(((size_t)o * nz + (k0 + kk)) * nx + (i0 + il)) * Do + nn] = yface[e];
+  for (int e = t; e < SM::YF; e += blockDim.x) {
+    const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
+    if (nn < gs && il < vx && kk < vz)
+      A.yf[(((size_t)o * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn] = yout[e];
   }
-  if (DIMS == 3) {
-    for (int e = t; e < TY * TX * Do; e += blockDim.x) {
-      const int nn = e % Do, r = e / Do, il = r % TX, jj = r / TX;
-      if (il < vx && jj < vy)
-        A.zf[(((size_t)o * ny + (j0 + jj)) * nx + (i0 + il)) * Do + nn] = zface[e];
+  if (DIMS == 3)
+    for (int e = t; e < SM::ZF; e += blockDim.x) {
+      const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
+      if (nn < gs && il < vx && jj < vy)
+        A.zf[(((size_t)o * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn] = zout[e];
     }
-  }
   if constexpr (!EXACT) {
-    for (int e = t; e < cells; e += blockDim.x) {
-      const int il = e % TX, r = e / TX, jj = r % TY, kk = r / TY;
+    for (int e = t; e < CELLS; e += blockDim.x) {
+      const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
       if (il < vx && jj < vy && kk < vz) {
-        float s = 0.0f, comp = 0.0f;
-        const float * pv = P + (size_t)e * Do;
-        for (int nn = 0; nn < Do; ++nn) {  // Kahan, fixed ordinate order
-          const float yv = pv[nn] - comp;
-          const float tv = s + yv;
-          comp = (tv - s) - yv;
-          s = tv;
+        float sum = 0.0f, comp = 0.0f;
+        for (int nn = 0; nn < gs; ++nn) {  // Kahan, fixed ordinate order
+          const float yv = fS(P[nn * CELLS + e], comp);
+          const float tv = fA(sum, yv);
+          comp = fS(fS(tv, sum), yv);
+          sum = tv;
         }
         const size_t cg = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
-        A.octphi[(size_t)o * N + cg] = (double)s - (double)comp;
+        A.octphi[slot * N + cg] = (double)sum - (double)comp;
       }
+    }
+  }
+
+  // -- publish completion (dataflow mode) ---------------------------------------------
+  if (dataflow) {
+    __threadfence();
+    __syncthreads();
+    if (t == 0)
+      st_release(A.done + ((slot * A.nbz + task.bk) * A.nby + task.bj) * A.nbx + task.bi, epoch);
+  }
+}
+
+// Persistent dataflow sweep: CTAs claim tasks in topological order from a
+// ticket counter; a claimed task waits only on tasks with smaller tickets,
+// which running CTAs already hold, so progress never depends on residency.
+template <typename T, int DIMS, int SCHEME, int TX>
+__global__ void __launch_bounds__(kMaxSweepThreads) sweep_persistent_kernel(const SweepArgs<T> A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned s_task;
+  const unsigned epoch = *A.epoch + 1u;
+  for (;;) {
+    __syncthreads();  // previous task's shared memory is free
+    if (threadIdx.x == 0) s_task = atomicAdd(A.ticket, 1u);
+    __syncthreads();
+    const unsigned tk = s_task;
+    if (tk >= (unsigned)A.num_tasks) break;
+    run_task<T, DIMS, SCHEME, TX>(A, A.tasks[tk], smem_raw, true, epoch);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(A.exit_count, 1u) == gridDim.x - 1) {
+      // last CTA out: re-arm the counters for the next sweep
+      *A.ticket = 0u;
+      *A.exit_count = 0u;
+      __threadfence();
+      *A.epoch = epoch;
     }
   }
 }
 
-template <typename T, int DIMS, int SCHEME>
-doma_status launch_levels(const Schedule & s, const SweepArgs<T> & args, cudaStream_t stream,
-                          uint64_t * launches)
+// One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
+template <typename T, int DIMS, int SCHEME, int TX>
+__global__ void __launch_bounds__(kMaxSweepThreads) sweep_level_kernel(const SweepArgs<T> A)
 {
-  SweepArgs<T> a = args;
-  const int levels = (int)s.level_begin.size() - 1;
-  for (int L = 0; L < levels; ++L) {
-    const int count = s.level_begin[L + 1] - s.level_begin[L];
-    if (count == 0) continue;
-    a.task_offset = s.level_begin[L];
-    sweep_kernel<T, DIMS, SCHEME><<<count, s.threads, s.smem, stream>>>(a);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  run_task<T, DIMS, SCHEME, TX>(A, A.tasks[A.task_offset + blockIdx.x], smem_raw, false, 0u);
+}
+
+template <typename T, int DIMS, int SCHEME, int TX>
+doma_status launch_impl(const Schedule & s, const SweepArgs<T> & args, cudaStream_t stream,
+                        uint64_t * launches)
+{
+  if (s.persistent) {
+    sweep_persistent_kernel<T, DIMS, SCHEME, TX><<<s.grid, s.threads, s.smem, stream>>>(args);
     if (launches) ++*launches;
+  } else {
+    SweepArgs<T> a = args;
+    const int levels = (int)s.level_begin.size() - 1;
+    for (int L = 0; L < levels; ++L) {
+      const int count = s.level_begin[L + 1] - s.level_begin[L];
+      if (count == 0) continue;
+      a.task_offset = s.level_begin[L];
+      sweep_level_kernel<T, DIMS, SCHEME, TX><<<count, s.threads, s.smem, stream>>>(a);
+      if (launches) ++*launches;
+    }
   }
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }
 
-template <typename T, int DIMS, int SCHEME>
-cudaError_t set_smem_attr(size_t smem)
+template <typename T>
+struct TypeTag {
+  using type = T;
+};
+
+// Dispatch over the compile-time choices: precision, dimension, scheme, TX.
+template <typename F>
+auto dispatch(int dims, int precision, int scheme, int tx, F && f)
 {
-  return cudaFuncSetAttribute(sweep_kernel<T, DIMS, SCHEME>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto by_tx = [&](auto tag_t, auto dims_c, auto scheme_c) {
+    using T = typename decltype(tag_t)::type;
+    constexpr int D = decltype(dims_c)::value, S = decltype(scheme_c)::value;
+    if (tx <= 8) return f(tag_t, dims_c, scheme_c, std::integral_constant<int, 8>{});
+    if (tx <= 16) return f(tag_t, dims_c, scheme_c, std::integral_constant<int, 16>{});
+    (void)sizeof(T); (void)D; (void)S;
+    return f(tag_t, dims_c, scheme_c, std::integral_constant<int, 32>{});
+  };
+  auto by_scheme = [&](auto tag_t, auto dims_c) {
+    if (scheme == DOMA_SCHEME_TW_DD)
+      return by_tx(tag_t, dims_c, std::integral_constant<int, DOMA_SCHEME_TW_DD>{});
+    return by_tx(tag_t, dims_c, std::integral_constant<int, DOMA_SCHEME_DD>{});
+  };
+  auto by_dims = [&](auto tag_t) {
+    if (dims == 2) return by_scheme(tag_t, std::integral_constant<int, 2>{});
+    return by_scheme(tag_t, std::integral_constant<int, 3>{});
+  };
+  if (precision == DOMA_PREC_FP64) return by_dims(TypeTag<double>{});
+  return by_dims(TypeTag<float>{});
 }
 
 }  // namespace
 
-size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx, int ty, int tz, int d_oct)
+int sweep_tile_x(int requested)
 {
-  (void)scheme;
-  const size_t ts = precision == DOMA_PREC_FP64 ? 8 : 4;
-  const size_t tzz = dims == 3 ? tz : 1;
-  const size_t cells = (size_t)tx * ty * tzz;
-  size_t n = tzz * tx * d_oct;                       // y faces
-  if (dims == 3) n += (size_t)ty * tx * d_oct;       // z faces
-  n += 2 * cells + tx + ty + tzz;                    // q, sigma_t, widths
-  n += (size_t)d_oct * (tx + ty + tzz);              // coefficients
-  size_t bytes = n * ts;
-  if (precision == DOMA_PREC_FP32) bytes += cells * d_oct * 4;  // P
-  return bytes;
+  return requested <= 8 ? 8 : requested <= 16 ? 16 : 32;
 }
 
-doma_status sweep_prepare(size_t smem)
+size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx)
 {
-  if (smem <= 48 * 1024) return DOMA_OK;
-  cudaError_t e = cudaSuccess;
-  cudaError_t r;
-#define DOMA_SET(T, D, S) if ((r = set_smem_attr<T, D, S>(smem)) != cudaSuccess) e = r;
-  DOMA_SET(double, 3, DOMA_SCHEME_DD) DOMA_SET(double, 3, DOMA_SCHEME_TW_DD)
-  DOMA_SET(double, 2, DOMA_SCHEME_DD) DOMA_SET(double, 2, DOMA_SCHEME_TW_DD)
-  DOMA_SET(float, 3, DOMA_SCHEME_DD) DOMA_SET(float, 3, DOMA_SCHEME_TW_DD)
-  DOMA_SET(float, 2, DOMA_SCHEME_DD) DOMA_SET(float, 2, DOMA_SCHEME_TW_DD)
-#undef DOMA_SET
+  return dispatch(dims, precision, scheme, tx, [](auto tag_t, auto dims_c, auto, auto tx_c) {
+    using T = typename decltype(tag_t)::type;
+    return TaskSmem<T, decltype(dims_c)::value, decltype(tx_c)::value>::bytes;
+  });
+}
+
+doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem)
+{
+  cudaError_t e = dispatch(dims, precision, scheme, tx, [&](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
+    using T = typename decltype(tag_t)::type;
+    constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
+    cudaError_t r = cudaFuncSetAttribute(sweep_persistent_kernel<T, D, S, X>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (r != cudaSuccess) return r;
+    return cudaFuncSetAttribute(sweep_level_kernel<T, D, S, X>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
   DOMA_CUDA_TRY(e);
   return DOMA_OK;
+}
+
+int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem)
+{
+  return dispatch(dims, precision, scheme, tx, [&](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
+    using T = typename decltype(tag_t)::type;
+    constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T, D, S, X>,
+                                                      threads, smem) != cudaSuccess)
+      return 0;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return per_sm * sms;
+  });
 }
 
 doma_status launch_sweep(int dims, int precision, int scheme, const Schedule & s,
                          const SweepArgs<double> * a64, const SweepArgs<float> * a32,
                          cudaStream_t stream, uint64_t * launches)
 {
-  const bool tw = scheme == DOMA_SCHEME_TW_DD;
-  if (precision == DOMA_PREC_FP64) {
-    if (dims == 3)
-      return tw ? launch_levels<double, 3, DOMA_SCHEME_TW_DD>(s, *a64, stream, launches)
-                : launch_levels<double, 3, DOMA_SCHEME_DD>(s, *a64, stream, launches);
-    return tw ? launch_levels<double, 2, DOMA_SCHEME_TW_DD>(s, *a64, stream, launches)
-              : launch_levels<double, 2, DOMA_SCHEME_DD>(s, *a64, stream, launches);
-  }
-  if (dims == 3)
-    return tw ? launch_levels<float, 3, DOMA_SCHEME_TW_DD>(s, *a32, stream, launches)
-              : launch_levels<float, 3, DOMA_SCHEME_DD>(s, *a32, stream, launches);
-  return tw ? launch_levels<float, 2, DOMA_SCHEME_TW_DD>(s, *a32, stream, launches)
-            : launch_levels<float, 2, DOMA_SCHEME_DD>(s, *a32, stream, launches);
+  return dispatch(dims, precision, scheme, s.tx, [&](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
+    using T = typename decltype(tag_t)::type;
+    constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
+    if constexpr (std::is_same<T, double>::value)
+      return launch_impl<T, D, S, X>(s, *a64, stream, launches);
+    else
+      return launch_impl<T, D, S, X>(s, *a32, stream, launches);
+  });
 }
 
 }  // namespace doma

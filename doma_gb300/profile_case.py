@@ -1,0 +1,66 @@
+"""A small, self-contained sweep workload for profilers (ncu) and timing.
+
+    python -m doma_gb300.profile_case [--n 64] [--groups 8] [--np 4] [--na 4]
+        [--precision fp32|fp64] [--scheme dd|tw_dd] [--tile 8] [--sweeps 3]
+        [--solve] [--schedule persistent|levels]
+
+Builds the seeded checkerboard problem (doma_gb300.problems.checkerboard) on
+cuda:0, sets up group 0's source with one source iteration, then runs
+`--sweeps` bare sweeps (or, with --solve, one full fixed-source solve) and
+prints the solver's block shape and launch counts.  Device memory stays
+well under 1 GB at the default size.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--groups", type=int, default=8)
+    ap.add_argument("--np", dest="np_", type=int, default=4)
+    ap.add_argument("--na", type=int, default=4)
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--scheme", choices=["dd", "tw_dd"], default="tw_dd")
+    ap.add_argument("--theta", type=float, default=0.7)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--sweeps", type=int, default=3)
+    ap.add_argument("--solve", action="store_true")
+    ap.add_argument("--schedule", choices=["persistent", "levels"], default="persistent")
+    a = ap.parse_args()
+    if a.schedule == "levels":
+        os.environ["DOMA_SWEEP_SCHEDULE"] = "levels"
+
+    import torch
+
+    from . import problems as P
+    from .solver import Solver
+
+    torch.cuda.set_device(0)
+    p = P.checkerboard(0, n=a.n, groups=a.groups, np_=a.np_, na=a.na, block=8)
+    o = P.make_options(scheme=a.scheme, theta=a.theta, precision=a.precision,
+                       fs_tol=1e-6 if a.precision == "fp32" else 1e-8,
+                       mg_tol=1e-6 if a.precision == "fp32" else 1e-8,
+                       fs_max_it=5000, mg_max_it=500, tile=(a.tile, 0, 0))
+    with Solver(p, o) as s:
+        t0 = time.perf_counter()
+        if a.solve:
+            r = s.solve_fixed_source()
+            extra = {"converged": r.converged, "si_iterations": r.si_iterations,
+                     "mg_iterations": r.mg_iterations}
+        else:
+            s.source_iterations(0, 1)
+            s.sweeps(0, a.sweeps)
+            extra = {"sweeps": a.sweeps}
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        print(json.dumps({"workload": p.name, "precision": a.precision, "scheme": a.scheme,
+                          "seconds": round(dt, 4), **extra, **s.describe()}))
+
+
+if __name__ == "__main__":
+    main()

@@ -71,6 +71,9 @@ CASES = {
                      {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-12, "mg_max_it": 2}),
 }
 
+# cases whose --verbose output (every SI residual) is also recorded
+VERBOSE_LOGS = {"capped_mg_dd", "capped_si_twdd", "random2d_dd"}
+
 QUAD_SETS = [(dims, np_, na) for dims in (2, 3)
              for (np_, na) in [(1, 1), (2, 2), (3, 3), (4, 4), (6, 6), (2, 5), (5, 2)]]
 
@@ -95,10 +98,14 @@ def main() -> None:
         p = make_problem(gen, kw)
         opts = P.make_options(**okw)
         t0 = time.time()
-        phi, ok, si, mg, _log = ol.ref_solve(p, opts, threads=1)
+        phi, ok, si, mg, log = ol.ref_solve(p, opts, threads=1)
         dt = time.time() - t0
         meta = {"generator": gen, "kwargs": kw, "options": okw, "digest": p.digest(),
-                "converged": ok, "mg_iterations": mg, "reference_seconds": round(dt, 3)}
+                "converged": ok, "mg_iterations": mg, "reference_seconds": round(dt, 3),
+                "log": log}
+        if name in VERBOSE_LOGS:
+            vopts = P.make_options(**okw, verbose=2)
+            meta["log_verbose"] = ol.ref_solve(p, vopts, threads=1)[4]
         np.savez_compressed(HERE / f"{name}.npz", phi=phi, si_counts=si,
                             meta=np.array(json.dumps(meta)))
         print(f"{name:28s} converged={ok} mg={mg} si={list(map(int, si))[:8]}... "

@@ -24,7 +24,8 @@ def load_case(name: str):
         raise AssertionError(f"{name}: regenerated inputs differ from the fixture's")
     opts = P.make_options(**meta["options"])
     exp = {"phi": z["phi"], "si_counts": z["si_counts"], "converged": meta["converged"],
-           "mg_iterations": meta["mg_iterations"], "meta": meta}
+           "mg_iterations": meta["mg_iterations"], "meta": meta, "log": meta.get("log"),
+           "log_verbose": meta.get("log_verbose")}
     return p, opts, exp
 
 

@@ -71,7 +71,7 @@ def _create(lib, p, o):
     (lambda p: p.cell_material.__setitem__(0, 7), "material"),
     (lambda p: p.dx.__setitem__(0, -1.0), "widths"),
     (lambda p: setattr(p, "num_polar", 0), "np"),
-    (lambda p: setattr(p, "num_polar", 600), "ordinates per octant"),
+    (lambda p: setattr(p, "num_polar", 5000), "ordinates per octant"),
 ])
 def test_bad_input_is_rejected(lib, mutate, msg):
     p = P.random_problem(0, 3, 3, 3, 3, groups=2)

@@ -81,11 +81,13 @@ def test_fp64_matches_oracle_random(seed, scheme, dims):
     assert rel_linf(phi, o_phi) <= FP64_RTOL
 
 
-@pytest.mark.parametrize("tile", [(1, 1, 1), (3, 2, 5), (8, 8, 2), (32, 1, 1), (5, 3, 1)])
+@pytest.mark.parametrize("tile", [(8, 0, 0), (16, 0, 0), (32, 0, 0)])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_block_shape_does_not_change_results(tile, precision):
-    """Every block shape, including ragged edge blocks, gives the same bits."""
-    p = P.random_problem(31, 3, 11, 9, 7, groups=2, np_=2, na=2, materials=3)
+@pytest.mark.parametrize("dims", [2, 3])
+def test_block_shape_does_not_change_results(tile, precision, dims):
+    """Every block length, with ragged edge blocks in every axis and a
+    partial ordinate group (9 ordinates per octant), gives the same bits."""
+    p = P.random_problem(31, dims, 37, 19, 7, groups=2, np_=3, na=3, materials=3)
     base = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-9, mg_tol=1e-9)
     ref_phi, _ = run(p, base)
     opts = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-9, mg_tol=1e-9,
@@ -158,3 +160,69 @@ def test_single_cell_and_single_ordinate():
     o_phi, ok, si, _, _ = ol.oracle_solve(p, opts)
     assert list(rep.si_counts) == list(si)
     assert rel_linf(phi, o_phi) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("dims", [2, 3])
+def test_persistent_and_level_schedules_agree(monkeypatch, precision, dims):
+    """The dataflow sweep and the one-launch-per-level sweep run the same task
+    body; their results must be bit-identical."""
+    p = P.random_problem(41, dims, 13, 11, 9, groups=2, np_=2, na=3, materials=3)
+    opts = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-8, mg_tol=1e-8,
+                          tile=(4, 3, 2))
+    a, ra = run(p, opts)
+    monkeypatch.setenv("DOMA_SWEEP_SCHEDULE", "levels")
+    b, rb = run(p, opts)
+    assert np.array_equal(a, b) and list(ra.si_counts) == list(rb.si_counts)
+
+
+def test_wait_timeout_is_reported_and_context_survives(monkeypatch):
+    """A dependency wait that can never be satisfied gives up after a bounded
+    number of polls; the host sees DOMA_DEVICE_WAIT_TIMEOUT and the CUDA
+    context stays usable."""
+    from doma_gb300 import abi
+    p = P.random_problem(42, 3, 10, 9, 8, groups=1, np_=1, na=2, materials=2)
+    opts = P.make_options(tile=(4, 4, 4))
+    monkeypatch.setenv("DOMA_SWEEP_WAIT_TEST", "1")
+    with pytest.raises(abi.DomaError) as ei:
+        run(p, opts)
+    assert ei.value.status == abi.DOMA_DEVICE_WAIT_TIMEOUT
+    monkeypatch.delenv("DOMA_SWEEP_WAIT_TEST")
+    phi, rep = run(p, opts)
+    o_phi, ok, si, _, _ = ol.oracle_solve(p, opts)
+    assert rep.converged and rel_linf(phi, o_phi) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("name", ["random3d_fission_twdd", "capped_si_twdd", "capped_mg_dd",
+                                  "square2d_dd"])
+def test_graph_loop_equals_host_loop(monkeypatch, name):
+    """The solve captured as one CUDA graph (device-side loop tests through
+    conditional WHILE nodes) and the host-driven loop give the same bits,
+    iteration counts and status."""
+    p, opts, exp = load_case(name)
+    a, ra = run(p, opts)
+    monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    b, rb = run(p, opts)
+    assert np.array_equal(a, b)
+    assert list(ra.si_counts) == list(rb.si_counts)
+    assert (ra.status, ra.mg_iterations, ra.si_iterations) == (rb.status, rb.mg_iterations,
+                                                               rb.si_iterations)
+    assert np.array_equal(a, exp["phi"])
+
+
+@pytest.mark.parametrize("loop", ["graph", "host"])
+@pytest.mark.parametrize("name", case_names())
+def test_progress_lines_match_reference(monkeypatch, capfd, loop, name):
+    """DOMA's stdout (MGI / SI lines) is reproduced line for line."""
+    p, opts, exp = load_case(name)
+    if loop == "host":
+        monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    opts.verbose = 1
+    capfd.readouterr()
+    run(p, opts)
+    out = capfd.readouterr().out
+    assert out == exp["log"]
+    if exp["log_verbose"] is not None:
+        opts.verbose = 2
+        run(p, opts)
+        assert capfd.readouterr().out == exp["log_verbose"]
