@@ -121,6 +121,11 @@ SIGNATURES = {
         [ctypes.c_void_p, _u32p, _u32p, ctypes.POINTER(ctypes.c_uint64)],
     ),
     "doma_solver_destroy": (None, [ctypes.c_void_p]),
+    "doma_sweep_noalloc": (
+        ctypes.c_int,
+        [ctypes.POINTER(DomaProblem), ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    ),
 }
 
 _LIB = None

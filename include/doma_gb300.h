@@ -175,6 +175,27 @@ doma_status doma_solver_describe(const doma_solver *solver, uint32_t tile[3],
 
 void doma_solver_destroy(doma_solver *solver);
 
+/* One FP32 sweep that allocates no memory -- no counterpart in DOMA.
+ * For callers that cannot call cudaMalloc (code inside another framework's
+ * memory pool or allocator budget, or that must keep its device footprint
+ * fixed after start-up): one transport sweep of one group over all octants
+ * and ordinates, the solver's FP32 kernel, with every piece of device scratch
+ * in a fixed static device array of DOMA_NOALLOC_SCRATCH_BYTES (64 MiB, held
+ * by every GPU that loads the library) and host staging in static buffers.
+ * Inputs: the mesh and quadrature of `problem` (dims, nx/ny/nz, dx/dy/dz,
+ * num_polar, num_azimuthal <= 8; materials are not read), the scheme and
+ * theta, and device arrays q[N] (isotropic source per steradian) and
+ * sigma_t[N] of the group, N = nx*ny*nz, x fastest.  Output: the swept scalar
+ * flux phi_out[N] (device, double) -- what one source iteration from a zero
+ * flux gives.  Problems that need more scratch are rejected with
+ * DOMA_BAD_INPUT.  All calls share the array: calls that overlap on the GPU
+ * race.  The first call on a device sets up the array's address and should
+ * come before any stream capture.  Synchronises `stream` before returning. */
+#define DOMA_NOALLOC_SCRATCH_BYTES (64u << 20)
+doma_status doma_sweep_noalloc(const doma_problem *problem, uint32_t scheme, double theta,
+                               const float *q, const float *sigma_t, double *phi_out,
+                               void *stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
