@@ -269,7 +269,8 @@ def run_ours(args):
     err = None
     fp64_rate = None
     if args.fp64_check:
-        with Solver(p, options("fp64", args.tol)) as s64:
+        # the FP64 oracle converged tightly (1e-8), independent of --tol
+        with Solver(p, options("fp64", 1e-8)) as s64:
             s64.set_stream(stream.cuda_stream)
             t0 = time.perf_counter()
             r64 = s64.solve_fixed_source()

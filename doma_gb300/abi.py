@@ -37,6 +37,9 @@ DOMA_SCHEME_DD = 0
 DOMA_SCHEME_TW_DD = 1
 DOMA_PREC_FP64 = 0
 DOMA_PREC_FP32 = 1
+DOMA_ITER_GAUSS_SEIDEL = 0
+DOMA_ITER_MULTIGROUP = 1
+ABI_VERSION = 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _u32p = ctypes.POINTER(ctypes.c_uint32)
@@ -79,6 +82,7 @@ class DomaOptions(ctypes.Structure):
         ("tile_x", ctypes.c_uint32),
         ("tile_y", ctypes.c_uint32),
         ("tile_z", ctypes.c_uint32),
+        ("iteration", ctypes.c_uint32),
     ]
 
 
@@ -153,7 +157,7 @@ def load_library(path: os.PathLike | str | None = None) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.doma_abi_version() != 1:
+    if lib.doma_abi_version() != ABI_VERSION:
         raise RuntimeError("doma_gb300 ABI version mismatch")
     if path is None:
         _LIB = lib

@@ -32,10 +32,11 @@ const char * get_error();
 // Ordinates of one octant handled by one sweep task (two per warp).
 constexpr int kGroup = 16;
 
-// One sweep task: octant, ordinate group and block coordinates in the
-// octant's sweep frame (i' = i for +mu, nx-1-i for -mu, likewise for y, z).
+// One sweep task: energy group (multigroup mode; 0 otherwise), octant,
+// ordinate group and block coordinates in the octant's sweep frame
+// (i' = i for +mu, nx-1-i for -mu, likewise for y and z).
 struct Task {
-  int oct, og, bi, bj, bk;
+  int oct, og, bi, bj, bk, grp;
 };
 
 // Everything a sweep launch needs.  Pointers are device pointers.
@@ -66,22 +67,22 @@ struct SweepArgs {
   const T * cx;
   const T * cy;
   const T * cz;
-  // per-cell sweep inputs of the group being swept
+  // per-cell sweep inputs: [groups in flight][N] (one group in Gauss-Seidel mode)
   const T * q;
   const T * sigt;
-  // face planes (sweep frame, per octant): x [8][nz][ny][d_oct],
-  // y [8][nz][nx][d_oct], z [8][ny][nx][d_oct]
+  // face planes (sweep frame, per (group in flight, octant)):
+  // x [G*8][nz][ny][d_oct], y [G*8][nz][nx][d_oct], z [G*8][ny][nx][d_oct]
   T * xf;
   T * yf;
   T * zf;
-  double * wpsi;     // exact mode: [N][d_total] weighted angular flux
-  double * octphi;   // fp32 mode: [8 * ngroups][N] scalar-flux partials per (octant, group)
+  double * wpsi;     // exact mode: [groups in flight][N][d_total] weighted angular flux
+  double * octphi;   // fp32 mode: [G*8*ngroups][N] scalar-flux partials per (group, octant, ordinate group)
   double theta;
   // persistent-mode scheduling state (device memory, kept between sweeps)
   unsigned * ticket;      // next task to claim (reset by the last CTA to leave)
   unsigned * exit_count;  // CTAs that have left
   unsigned * epoch;       // sweeps completed
-  unsigned * done;        // [8][ngroups][nbz][nby][nbx] epoch in which the task finished
+  unsigned * done;        // [G*8][ngroups][nbz][nby][nbx] epoch in which the task finished
   int * error;            // nonzero: a bounded wait gave up (DOMA_DEVICE_WAIT_TIMEOUT)
   unsigned spin_limit;    // polls before a wait gives up
   unsigned wait_bias;     // 0; nonzero only in the wait-timeout test, where every

@@ -224,7 +224,124 @@ __global__ void __launch_bounds__(kBlock) mg_residual_kernel(const IterArgs A, d
   }
 }
 
+// Multigroup mode, start of the solve: phi = 0, the first increment's source
+// is the external source of every group, and sigma_t of every group is staged.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) mgi_init_kernel(const IterArgs A, T * q, T * sigt)
+{
+  const size_t N = A.N;
+  const int G = A.G;
+  const double s = A.src_scale;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const unsigned m = A.mat[c];
+    for (int g = 0; g < G; ++g) {
+      q[(size_t)g * N + c] = (T)(A.source ? dD(dM(s, A.source[(size_t)m * G + g]), kPi) : 0.0);
+      sigt[(size_t)g * N + c] = (T)A.total[(size_t)m * G + g];
+      A.phi[(size_t)g * N + c] = 0.0;
+    }
+  }
+}
+
+// Multigroup mode, after an all-group sweep:
+//   d_g  = sum of group g's (octant, ordinate group) partials, in slot order
+//   diff += d_g^2 V, total += (phi_g + d_g)^2 V over all groups
+//   phi_g += d_g
+//   q_h  = s / pi * sum_g (S[h][g] + chi[h] nu_sigma_f[g]) d_g   (next increment)
+// The G x G contraction per cell is small (G <= 16 in every workload here)
+// and memory-bound, so it stays on the CUDA cores.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) mgi_epilogue_kernel(const IterArgs A, T * q,
+                                                             double * dscratch, double * norms,
+                                                             const LoopParams L)
+{
+  const size_t N = A.N;
+  const int G = A.G;
+  const int per_group = 8 * A.ngroups;
+  double diff = 0.0, tot = 0.0;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const double V = A.vol[c];
+    for (int g = 0; g < G; ++g) {
+      double d = 0.0;
+      if (A.exact) {
+        // every ordinate in DOMA's single-thread order (octant, then ordinate)
+        const double * w = A.wpsi + ((size_t)g * N + c) * (size_t)A.D;
+        for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
+      } else {
+        for (int o = 0; o < 8; ++o)
+          if (A.oct_mask & (1 << o))
+            for (int og = 0; og < A.ngroups; ++og)
+              d = dA(d, A.octphi[((size_t)g * per_group + (size_t)o * A.ngroups + og) * N + c]);
+      }
+      double * ph = A.phi + (size_t)g * N + c;
+      const double t = dA(*ph, d);
+      diff = dA(diff, dM(dM(d, d), V));
+      tot = dA(tot, dM(dM(t, t), V));
+      *ph = t;
+      dscratch[(size_t)g * N + c] = d;
+    }
+    const unsigned m = A.mat[c];
+    const bool fis = A.fis && A.fis[m];
+    for (int h = 0; h < G; ++h) {
+      double acc = 0.0;
+      const double * Sh = A.scatter + ((size_t)m * G + h) * G;
+      const double chi = fis ? A.chi[(size_t)m * G + h] : 0.0;
+      for (int g = 0; g < G; ++g) {
+        double k = Sh[g];
+        if (fis) k = dA(k, dM(chi, A.nsf[(size_t)m * G + g]));
+        acc = dA(acc, dM(k, dscratch[(size_t)g * N + c]));
+      }
+      q[(size_t)h * N + c] = (T)dD(dM(A.src_scale, acc), kPi);
+    }
+  }
+  if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
+    LoopCtl * C = L.ctl;
+    const double res = norm_ratio(norms[0], norms[1]);
+    const unsigned it = ++C->si_it;
+    ++C->sweeps;
+    if (L.si_hist && C->hist_len < L.hist_cap) L.si_hist[C->hist_len] = res;
+    ++C->hist_len;
+    C->si_res = res;
+    const bool ok = finite2(norms[0], norms[1]) && C->error == 0;
+    const bool more = ok && it < L.fs_max_it && L.fs_tol < res;
+    if (!more) {
+      if (C->pairs < L.pair_cap) {
+        L.pair_counts[C->pairs] = it;
+        L.pair_res[C->pairs] = res;
+      }
+      ++C->pairs;
+      if (C->error != 0) C->failed = DOMA_DEVICE_WAIT_TIMEOUT;
+      else if (!ok) C->failed = DOMA_NUMERIC_ERROR;
+      else if (!(it < L.fs_max_it)) C->failed = DOMA_NOT_CONVERGED;
+    }
+    cudaGraphSetConditional(L.si_handle, more ? 1u : 0u);
+  }
+}
+
 }  // namespace
+
+doma_status launch_mgi_init(const IterArgs & a, int precision, void * q, void * sigt,
+                            cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    mgi_init_kernel<double><<<a.grid, kBlock, 0, st>>>(a, (double *)q, (double *)sigt);
+  else
+    mgi_init_kernel<float><<<a.grid, kBlock, 0, st>>>(a, (float *)q, (float *)sigt);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_mgi_epilogue(const IterArgs & a, int precision, void * q, double * dscratch,
+                                double * norms, const LoopParams & L, cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    mgi_epilogue_kernel<double><<<a.grid, kBlock, 0, st>>>(a, (double *)q, dscratch, norms, L);
+  else
+    mgi_epilogue_kernel<float><<<a.grid, kBlock, 0, st>>>(a, (float *)q, dscratch, norms, L);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
 
 doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q, void * sigt,
                              const LoopParams & L, cudaStream_t st)

@@ -13,6 +13,7 @@ struct IterArgs {
   int grid = 0;               // fixed grid of every per-cell kernel
   unsigned oct_mask = 0;      // octants that carry ordinates
   int ngroups = 1;            // fp32: ordinate groups per octant (partials per octant)
+  bool exact = false;         // FP64 exact mode: the sweep wrote wpsi, not octphi
   double src_scale = 0.25;    // 1/(4 pi) prefactor numerator: 0.25 (3D), 0.5 (2D)
   const double * vol = nullptr;       // [N]
   const uint32_t * mat = nullptr;     // [N]
@@ -24,7 +25,7 @@ struct IterArgs {
   const double * nsf = nullptr;       // [M][G]
   double * phi = nullptr;             // [G][N]
   double * prev = nullptr;            // [G][N]
-  const double * wpsi = nullptr;      // exact: [N][D]
+  const double * wpsi = nullptr;      // exact: [groups in flight][N][D]
   const double * octphi = nullptr;    // fp32: [8 * ngroups][N]
   double * partials = nullptr;        // [grid][2]
   unsigned * ticket = nullptr;        // last-block ticket (kept at 0 between launches)
@@ -74,6 +75,11 @@ doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * 
                                double * norms, const LoopParams & L, cudaStream_t st);
 doma_status launch_mg_residual(const IterArgs & a, double * norms, const LoopParams & L,
                                cudaStream_t st);
+// Multigroup mode (every group in flight).
+doma_status launch_mgi_init(const IterArgs & a, int precision, void * q, void * sigt,
+                            cudaStream_t st);
+doma_status launch_mgi_epilogue(const IterArgs & a, int precision, void * q, double * dscratch,
+                                double * norms, const LoopParams & L, cudaStream_t st);
 int iteration_block();
 
 }  // namespace doma

@@ -51,6 +51,11 @@ struct doma_solver {
   size_t N = 0;
   int D = 0, d_oct = 0;
   unsigned oct_mask = 0;
+  bool mgi = false;     // multigroup iteration: every group in flight
+  int gif = 1;          // groups in flight per sweep (G in multigroup mode, else 1)
+  double * d_dscratch = nullptr;   // multigroup mode: [G][N] increments
+  cudaGraph_t mgi_graph = nullptr;
+  cudaGraphExec_t mgi_exec = nullptr;
   doma_options opts{};
   int offs[8] = {0};
 
@@ -173,6 +178,8 @@ doma_status validate(const doma_problem * p, const doma_options * o)
   if (o->precision != DOMA_PREC_FP64 && o->precision != DOMA_PREC_FP32)
     return bad("unknown precision");
   if (!(o->theta >= 0.0 && o->theta <= 1.0)) return bad("theta must lie in [0, 1]");
+  if (o->iteration != DOMA_ITER_GAUSS_SEIDEL && o->iteration != DOMA_ITER_MULTIGROUP)
+    return bad("unknown iteration");
   return DOMA_OK;
 }
 
@@ -180,7 +187,10 @@ doma_status validate(const doma_problem * p, const doma_options * o)
 // cross-section; ordinates split into groups of at most kGroup per task.
 void pick_tile(doma_solver * s, const doma_options * o)
 {
-  const int want = o->tile_x ? (int)o->tile_x : (s->dims == 3 ? 8 : 32);
+  // measured on GB300 (64^3, 16 ordinates per octant): DD is fastest with
+  // 8-cell blocks, TW-DD (more arithmetic per cell) with 16
+  const int want = o->tile_x ? (int)o->tile_x
+                             : (s->dims == 3 ? (o->scheme == DOMA_SCHEME_TW_DD ? 16 : 8) : 32);
   s->sched.tx = sweep_tile_x(want);
   s->sched.ty = s->dims == 3 ? 4 : 16;
   s->sched.tz = s->dims == 3 ? 4 : 1;
@@ -198,14 +208,15 @@ void build_schedule(doma_solver * s)
   sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx);
   const int levels = sc.nbx + sc.nby + sc.nbz - 2;
   std::vector<std::vector<Task>> by_level(levels);
-  for (int o = 0; o < 8; ++o) {
-    if (!(s->oct_mask & (1u << o))) continue;
-    for (int og = 0; og < sc.ngroups; ++og)
-      for (int bk = 0; bk < sc.nbz; ++bk)
-        for (int bj = 0; bj < sc.nby; ++bj)
-          for (int bi = 0; bi < sc.nbx; ++bi)
-            by_level[bi + bj + bk].push_back(Task{o, og, bi, bj, bk});
-  }
+  for (int g = 0; g < s->gif; ++g)
+    for (int o = 0; o < 8; ++o) {
+      if (!(s->oct_mask & (1u << o))) continue;
+      for (int og = 0; og < sc.ngroups; ++og)
+        for (int bk = 0; bk < sc.nbz; ++bk)
+          for (int bj = 0; bj < sc.nby; ++bj)
+            for (int bi = 0; bi < sc.nbx; ++bi)
+              by_level[bi + bj + bk].push_back(Task{o, og, bi, bj, bk, g});
+    }
   sc.tasks.clear();
   sc.level_begin.assign(1, 0);
   for (auto & lv : by_level) {
@@ -232,6 +243,8 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   s->N = (size_t)s->nx * s->ny * s->nz;
   s->d_oct = (int)(p->num_polar * p->num_azimuthal);
   s->D = (s->dims == 3 ? 8 : 4) * s->d_oct;
+  s->mgi = o->iteration == DOMA_ITER_MULTIGROUP;
+  s->gif = s->mgi ? s->G : 1;
 
   std::vector<double> mu(s->D), eta(s->D), xi(s->D), w(s->D);
   unsigned counts[8];
@@ -329,22 +342,24 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   }
   DOMA_TRY(dalloc(s, &s->d_phi, G * N));
   DOMA_TRY(dalloc(s, &s->d_prev, G * N));
+  const size_t gif = (size_t)s->gif;
   unsigned char * qb = nullptr;
-  DOMA_TRY(dalloc(s, &qb, 2 * N * ts));
+  DOMA_TRY(dalloc(s, &qb, 2 * gif * N * ts));
   s->d_q = qb;
-  s->d_sigt = qb + N * ts;
+  s->d_sigt = qb + gif * N * ts;
   const size_t Do = s->d_oct;
   unsigned char * fb = nullptr;
-  const size_t xf = 8 * (size_t)s->nz * s->ny * Do, yf = 8 * (size_t)s->nz * s->nx * Do,
-               zf = 8 * (size_t)s->ny * s->nx * Do;
+  const size_t xf = gif * 8 * (size_t)s->nz * s->ny * Do, yf = gif * 8 * (size_t)s->nz * s->nx * Do,
+               zf = gif * 8 * (size_t)s->ny * s->nx * Do;
   DOMA_TRY(dalloc(s, &fb, (xf + yf + zf) * ts));
   s->d_xf = fb;
   s->d_yf = fb + xf * ts;
   s->d_zf = fb + (xf + yf) * ts;
   if (exact)
-    DOMA_TRY(dalloc(s, &s->d_wpsi, N * (size_t)s->D));
+    DOMA_TRY(dalloc(s, &s->d_wpsi, gif * N * (size_t)s->D));
   else
-    DOMA_TRY(dalloc(s, &s->d_octphi, 8 * (size_t)((s->d_oct + kGroup - 1) / kGroup) * N));
+    DOMA_TRY(dalloc(s, &s->d_octphi, gif * 8 * (size_t)((s->d_oct + kGroup - 1) / kGroup) * N));
+  if (s->mgi) DOMA_TRY(dalloc(s, &s->d_dscratch, (size_t)s->G * N));
 
   pick_tile(s, o);
   build_schedule(s);
@@ -360,7 +375,7 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
     s->sched.grid = std::max(1, std::min<int>(fit, (int)s->sched.tasks.size()));
     // one flag per (octant slot, block): indexed by octant 0..7 even when
     // only four octants carry ordinates (2D)
-    const size_t flags = 8 * (size_t)s->sched.ngroups * s->sched.nbx * s->sched.nby * s->sched.nbz;
+    const size_t flags = (size_t)s->gif * 8 * s->sched.ngroups * s->sched.nbx * s->sched.nby * s->sched.nbz;
     DOMA_TRY(dalloc(s, &s->d_done, flags));
     DOMA_CUDA_TRY(cudaMemset(s->d_done, 0, flags * sizeof(unsigned)));
   }
@@ -430,6 +445,7 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   IterArgs & it = s->it;
   it.N = N; it.G = s->G; it.D = s->D; it.grid = grid; it.oct_mask = s->oct_mask;
   it.ngroups = s->sched.ngroups;
+  it.exact = exact;
   it.src_scale = s->dims == 3 ? 0.25 : 0.5;
   it.vol = s->d_vol; it.mat = s->d_mat; it.total = s->d_total; it.scatter = s->d_scatter;
   it.source = s->d_source; it.fis = s->d_fis; it.chi = s->d_chi; it.nsf = s->d_nsf;
@@ -438,7 +454,7 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
 
   DOMA_CUDA_TRY(cudaMemset(s->d_phi, 0, G * N * sizeof(double)));
   DOMA_CUDA_TRY(cudaMemset(s->d_prev, 0, G * N * sizeof(double)));
-  DOMA_CUDA_TRY(cudaMemset(s->d_q, 0, 2 * N * ts));
+  DOMA_CUDA_TRY(cudaMemset(s->d_q, 0, 2 * gif * N * ts));
   DOMA_CUDA_TRY(cudaDeviceSynchronize());
   return DOMA_OK;
 }
@@ -446,6 +462,8 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
 void release(doma_solver * s)
 {
   if (!s) return;
+  if (s->mgi_exec) cudaGraphExecDestroy(s->mgi_exec);
+  if (s->mgi_graph) cudaGraphDestroy(s->mgi_graph);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->graph) cudaGraphDestroy(s->graph);
   for (void * p : s->allocations) cudaFree(p);
@@ -731,8 +749,136 @@ doma_status solve_graph(doma_solver * s, doma_report * r)
   return status;
 }
 
+// ---- multigroup mode (every group in flight) ------------------------------
+
+// One multigroup iteration: all-group sweep, then the epilogue that forms the
+// next increment's source for every group.
+doma_status mgi_iteration(doma_solver * s, const LoopParams & L, cudaStream_t st)
+{
+  DOMA_TRY(launch_sweep(s->dims, s->opts.precision, s->opts.scheme, s->sched, &s->a64, &s->a32,
+                        st, &s->launches));
+  DOMA_TRY(launch_mgi_epilogue(s->it, s->opts.precision, s->d_q, s->d_dscratch, s->d_ctl->norms, L,
+                               st));
+  ++s->launches;
+  return DOMA_OK;
+}
+
+// WHILE(si) { sweep(all groups); mgi_epilogue } -- the epilogue decides.
+doma_status build_mgi_graph(doma_solver * s)
+{
+  cudaStream_t c0 = nullptr, c1 = nullptr;
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c1, cudaStreamNonBlocking));
+  auto run = [&]() -> doma_status {
+    DOMA_CUDA_TRY(cudaGraphCreate(&s->mgi_graph, 0));
+    cudaGraphConditionalHandle h;
+    DOMA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, s->mgi_graph, 1u, cudaGraphCondAssignDefault));
+    DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c0, s->mgi_graph, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t body = nullptr;
+    doma_status st = add_while(c0, h, &body);
+    if (st == DOMA_OK) {
+      DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c1, body, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+      LoopParams L = loop_params(s, s->G);
+      L.si_handle = h;
+      const uint64_t before = s->launches;
+      st = mgi_iteration(s, L, c1);
+      s->launches = before;
+      cudaGraph_t out = nullptr;
+      DOMA_CUDA_TRY(cudaStreamEndCapture(c1, &out));
+    }
+    cudaGraph_t out = nullptr;
+    DOMA_CUDA_TRY(cudaStreamEndCapture(c0, &out));
+    if (st != DOMA_OK) return st;
+    DOMA_CUDA_TRY(cudaGraphInstantiate(&s->mgi_exec, s->mgi_graph, 0));
+    return DOMA_OK;
+  };
+  const doma_status st = run();
+  cudaStreamDestroy(c0);
+  cudaStreamDestroy(c1);
+  return st;
+}
+
+doma_status solve_multigroup(doma_solver * s, doma_report * r)
+{
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t G = s->G, N = s->N;
+  const doma_options & o = s->opts;
+  if (o.verbose) std::printf("Solving (multigroup source iteration, all %d groups in flight)...\n", s->G);
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->si_it, 0, sizeof(DevCtl) - offsetof(DevCtl, si_it),
+                                s->stream));
+  DOMA_TRY(launch_mgi_init(s->it, o.precision, s->d_q, s->d_sigt, s->stream));
+  uint64_t launches = 1;
+  unsigned iters = 0;
+  double res = 0.0;
+  doma_status status = DOMA_OK;
+  std::vector<double> hist;
+  if (s->use_graph) {
+    if (!s->mgi_exec) DOMA_TRY(build_mgi_graph(s));
+    DOMA_CUDA_TRY(cudaGraphLaunch(s->mgi_exec, s->stream));
+    DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s->stream));
+    DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    const DevCtl c = *s->h_ctl;
+    iters = c.si_it;
+    res = c.si_res;
+    launches += 2ull * iters;
+    if (c.failed) status = (doma_status)c.failed;
+    if (s->d_si_hist && c.hist_len) {
+      hist.resize(std::min<unsigned long long>(c.hist_len, s->hist_cap));
+      DOMA_CUDA_TRY(cudaMemcpy(hist.data(), s->d_si_hist, hist.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost));
+    }
+  } else {
+    const LoopParams L{};
+    do {
+      DOMA_TRY(mgi_iteration(s, L, s->stream));
+      launches += 2;
+      double diff, tot;
+      DOMA_TRY(read_norms(s, 0, &diff, &tot));
+      ++iters;
+      if (!std::isfinite(diff) || !std::isfinite(tot)) {
+        status = DOMA_NUMERIC_ERROR;
+        break;
+      }
+      res = ratio(diff, tot);
+      hist.push_back(res);
+    } while (iters < o.fs_max_it && o.fs_tol < res);
+    if (status == DOMA_OK && !(iters < o.fs_max_it)) status = DOMA_NOT_CONVERGED;
+  }
+  if (o.verbose >= 2)
+    for (size_t k = 0; k < hist.size(); ++k)
+      std::printf("Performing MGSI %zu, residual = %g\n", k, hist[k]);
+  if (o.verbose) {
+    std::printf("Multigroup source iteration %s after %u iterations with a residual of %g\n",
+                status == DOMA_OK ? "converged" : "failed to converge", iters, res);
+    std::fflush(stdout);
+  }
+  if (status == DOMA_NOT_CONVERGED) set_error("multigroup source iteration reached fs_max_it");
+  else if (status == DOMA_NUMERIC_ERROR) set_error("a residual norm is not finite");
+  else if (status == DOMA_DEVICE_WAIT_TIMEOUT) set_error("a sweep wait for an upstream block timed out");
+  if (s->use_graph) s->launches += launches;  // (the host loop counted its own launches)
+  const auto t1 = std::chrono::steady_clock::now();
+  if (r) {
+    r->status = status;
+    r->mg_iterations = iters;
+    r->si_iterations = (uint64_t)iters * G;
+    r->updates = (uint64_t)iters * G * N * (uint64_t)s->D;
+    r->kernel_launches = launches;
+    r->mg_residual = res;
+    r->si_residual = res;
+    r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    r->si_counts_len = 1;
+    if (r->si_counts && r->si_counts_capacity) r->si_counts[0] = iters;
+  }
+  return status;
+}
+
 doma_status solve_impl(doma_solver * s, doma_report * r)
 {
+  if (s->mgi) return solve_multigroup(s, r);
   if (s->use_graph) return solve_graph(s, r);
   const doma_options & o = s->opts;
   const int verbose = (int)o.verbose;
@@ -919,6 +1065,13 @@ doma_status doma_solver_source_iterations(doma_solver * s, uint32_t group, uint3
 {
   if (!s) return bad("null solver");
   if ((int)group >= s->G) return bad("group out of range");
+  if (s->mgi) {
+    // multigroup mode: `count` iterations of all groups from the external source
+    DOMA_TRY(launch_mgi_init(s->it, s->opts.precision, s->d_q, s->d_sigt, s->stream));
+    ++s->launches;
+    for (uint32_t i = 0; i < count; ++i) DOMA_TRY(mgi_iteration(s, LoopParams{}, s->stream));
+    return DOMA_OK;
+  }
   DOMA_TRY(launch_mg_source(s->it, (int)group, s->opts.precision, s->d_q, s->d_sigt, LoopParams{},
                             s->stream));
   ++s->launches;
@@ -945,8 +1098,12 @@ doma_status doma_solver_describe(const doma_solver * s, uint32_t tile[3],
   }
   if (launches_per_sweep) {
     uint32_t n = 0;
-    for (size_t L = 0; L + 1 < s->sched.level_begin.size(); ++L)
-      if (s->sched.level_begin[L + 1] > s->sched.level_begin[L]) ++n;
+    if (s->sched.persistent) {
+      n = 1;
+    } else {
+      for (size_t L = 0; L + 1 < s->sched.level_begin.size(); ++L)
+        if (s->sched.level_begin[L + 1] > s->sched.level_begin[L]) ++n;
+    }
     *launches_per_sweep = n;
   }
   if (kernel_launches) *kernel_launches = s->launches;

@@ -166,6 +166,8 @@ __device__ __forceinline__ float fA(float a, float b) { return __fadd_rn(a, b); 
 __device__ __forceinline__ float fS(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fM(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fF(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// Approximate reciprocal (one MUFU op); the TW-DD weights it inverts lie in [0.5, 1].
+__device__ __forceinline__ float fR(float a) { return __fdividef(1.0f, a); }
 
 // DD with cx = 2|mu|/lx etc.: psi = (q + cx x + cy y + cz z) / (cx + cy + cz + st).
 __device__ __forceinline__ float dd_f32(float q, float st, float cx, float cy, float cz,
@@ -199,7 +201,7 @@ __device__ __forceinline__ float twdd3_f32(float q, float st, float amu, float a
   const float a = tw_weight(fF(fA(ey, xz), th, fA(qVt, mx)), fF(2.0f, fA(etB, xiC), sV), x);
   const float b = tw_weight(fF(fA(mx, xz), th, fA(qVt, ey)), fF(2.0f, fA(muA, xiC), sV), y);
   const float c3 = tw_weight(fF(fA(mx, ey), th, fA(qVt, xz)), fF(2.0f, fA(muA, etB), sV), z);
-  const float ra = __frcp_rn(a), rb = __frcp_rn(b), rc = __frcp_rn(c3);
+  const float ra = fR(a), rb = fR(b), rc = fR(c3);
   const float ta = fM(muA, ra), tb = fM(etB, rb), tc = fM(xiC, rc);
   const float c = __fdividef(fF(tc, z, fF(tb, y, fF(ta, x, qV))), fA(fA(fA(sV, ta), tb), tc));
   x = fM(fF(fS(a, 1.0f), x, c), ra);   // (c - (1 - a) x) / a
@@ -226,7 +228,7 @@ __device__ __forceinline__ float twdd2_f32(float q, float st, float amu, float a
   const float mx = fM(muA, x), ey = fM(etB, y);
   const float a = tw_weight(fF(ey, th, fA(qVt, mx)), fF(2.0f, etB, sV), x);
   const float b = tw_weight(fF(fA(mx, axi), th, fA(qVt, ey)), fF(2.0f, muA, sV), y);
-  const float ra = __frcp_rn(a), rb = __frcp_rn(b);
+  const float ra = fR(a), rb = fR(b);
   const float ta = fM(muA, ra), tb = fM(etB, rb);
   const float c = __fdividef(fF(tb, y, fF(ta, x, qV)), fA(fA(sV, ta), tb));
   x = fM(fF(fS(a, 1.0f), x, c), ra);
@@ -255,17 +257,20 @@ __device__ __forceinline__ int ld_relaxed(const int * p)
   return v;
 }
 
-// Wait until *flag == epoch.  Bounded: after `limit` polls (with exponential
-// back-off up to ~1 us) it records DOMA_DEVICE_WAIT_TIMEOUT in *error and
-// returns false; it also gives up at once when another CTA has already failed.
+// Wait until *flag == epoch.  Bounded: the first polls are back to back,
+// then exponential back-off up to ~0.5 us; after `limit` polls it records
+// DOMA_DEVICE_WAIT_TIMEOUT in *error and returns false.  It also gives up at
+// once when another CTA has already failed.
 __device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, int * error)
 {
   unsigned ns = 32;
   for (unsigned it = 0; it < limit; ++it) {
     if (ld_acquire(flag) == epoch) return true;
     if (ld_relaxed(error) != 0) return false;
-    __nanosleep(ns);
-    if (ns < 1024) ns *= 2;
+    if (it >= 8) {
+      __nanosleep(ns);
+      if (ns < 512) ns *= 2;
+    }
   }
   atomicCAS(error, 0, (int)DOMA_DEVICE_WAIT_TIMEOUT);
   return false;
@@ -294,7 +299,7 @@ struct TaskSmem {
   static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
   static constexpr int NT = 2 * YF + 2 * ZF + 2 * CELLS + TX + PY + PZ + kGroup * (TX + PY + PZ);
   static constexpr bool EXACT = std::is_same<T, double>::value;
-  static constexpr size_t bytes = NT * sizeof(T) + (EXACT ? 0 : (size_t)kGroup * CELLS * sizeof(float));
+  static constexpr size_t bytes = NT * sizeof(T) + (EXACT ? 0 : (size_t)(kGroup / 2) * CELLS * sizeof(float));
 };
 
 template <typename T, int DIMS, int SCHEME, int TX>
@@ -305,9 +310,14 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   constexpr bool EXACT = SM::EXACT;
   constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
   constexpr unsigned FULL = 0xffffffffu;
-  const int o = task.oct, og = task.og;
+  const int og = task.og;
+  const int o = task.oct;                 // octant: sweep directions
+  const int of = task.grp * 8 + o;        // (group in flight, octant) plane index
   const bool rx = (o & 4) != 0, ry = (o & 2) != 0, rz = (o & 1) != 0;
   const int nx = A.nx, ny = A.ny, nz = DIMS == 3 ? A.nz : 1;
+  const size_t N = (size_t)nx * ny * nz;
+  const T * gq = A.q + (size_t)task.grp * N;
+  const T * gsig = A.sigt + (size_t)task.grp * N;
   const int Do = A.d_oct;
   const int n0 = og * kGroup;
   const int gs = min(kGroup, Do - n0);
@@ -336,7 +346,7 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   T * cxs = lzs + PZ;                 // [kGroup][TX]
   T * cys = cxs + kGroup * TX;        // [kGroup][PY]
   T * czs = cys + kGroup * PY;        // [kGroup][PZ]
-  float * P = reinterpret_cast<float *>(czs + kGroup * PZ);  // fp32: [kGroup][CELLS]
+  float * P = reinterpret_cast<float *>(czs + kGroup * PZ);  // fp32: [kGroup / 2][CELLS] pair sums
 
   auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
   auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
@@ -347,8 +357,8 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
     const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
     if (il < vx && jj < vy && kk < vz) {
       const size_t c = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
-      qs[e] = A.q[c];
-      ss[e] = A.sigt[c];
+      qs[e] = gq[c];
+      ss[e] = gsig[c];
     }
   }
   for (int e = t; e < TX; e += blockDim.x) lxs[e] = e < vx ? A.wx[phys_i(e)] : (T)1;
@@ -377,8 +387,7 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   const double wgt = A.wgt[ord];
   const float wgt_f = (float)wgt;
   const T th = (T)A.theta;
-  const size_t N = (size_t)nx * ny * nz;
-  const size_t slot = (size_t)o * A.ngroups + og;   // (octant, group) slot
+  const size_t slot = (size_t)of * A.ngroups + og;   // (group, octant, ordinate group) slot
 
   // -- wait for the upstream blocks (dataflow mode) --------------------------------
   if (dataflow) {
@@ -404,7 +413,7 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
     const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
     T v = (T)0;
     if (task.bj > 0 && nn < gs && il < vx && kk < vz)
-      v = __ldcg(A.yf + (((size_t)o * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn);
+      v = __ldcg(A.yf + (((size_t)of * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn);
     yin[e] = v;
   }
   if (DIMS == 3)
@@ -412,65 +421,82 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
       const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
       T v = (T)0;
       if (task.bk > 0 && nn < gs && il < vx && jj < vy)
-        v = __ldcg(A.zf + (((size_t)o * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn);
+        v = __ldcg(A.zf + (((size_t)of * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn);
       zin[e] = v;
     }
   T xin = (T)0;
-  const size_t xslot = (((size_t)o * nz + (k0 + kl)) * ny + (j0 + jl)) * Do + n0 + nl;
+  const size_t xslot = (((size_t)of * nz + (k0 + kl)) * ny + (j0 + jl)) * Do + n0 + nl;
   if (active && task.bi > 0) xin = __ldcg(A.xf + xslot);
   __syncthreads();
 
   // -- wavefront: step s solves the cells with il + jl + kl == s, warp-synchronously --
+  // per-thread constants of the pencil (valid for every active thread)
+  const int ebase = (kl * PY + jl) * TX;          // cell index of il = 0
+  const int ybase = kl * TX * kGroup + nl;        // y-face slot of il = 0
+  const int zbase = jl * TX * kGroup + nl;        // z-face slot of il = 0
+  const int cxbase = nl * TX;
+  const T cy_t = cys[nl * PY + jl];
+  const T cz_t = DIMS == 3 ? czs[nl * PZ + kl] : (T)0;
+  const T ly_t = lys[jl];
+  const T lz_t = DIMS == 3 ? lzs[kl] : (T)1;
   T ysh = (T)0, zsh = (T)0;   // faces handed over by the upwind lanes
   T yo = (T)0, zo = (T)0;
   constexpr int STEPS = TX + PY + PZ - 2;
-#pragma unroll 4
+#pragma unroll 2
   for (int s = 0; s < STEPS; ++s) {
     const int il = s - jl - kl;
-    const bool valid = active && il >= 0 && il < vx;
+    const bool valid = active && (unsigned)il < (unsigned)vx;
+    float wp = 0.0f;
+    int e = 0;
     if (valid) {
-      T y = jl == 0 ? yin[(kl * TX + il) * kGroup + nl] : ysh;
+      T y = jl == 0 ? yin[ybase + il * kGroup] : ysh;
       T z = (T)0;
-      if (DIMS == 3) z = kl == 0 ? zin[(jl * TX + il) * kGroup + nl] : zsh;
-      const int e = (kl * PY + jl) * TX + il;
+      if (DIMS == 3) z = kl == 0 ? zin[zbase + il * kGroup] : zsh;
+      e = ebase + il;
       const T q = qs[e], st = ss[e];
       T psi;
       if constexpr (EXACT) {
         if constexpr (DIMS == 3) {
           if constexpr (SCHEME == DOMA_SCHEME_DD) {
-            const double geo = dA(dA(cxs[nl * TX + il], cys[nl * PY + jl]), czs[nl * PZ + kl]);
-            psi = dd3_exact(q, st, amu, aeta, axi, lxs[il], lys[jl], lzs[kl], geo, xin, y, z);
+            const double geo = dA(dA(cxs[cxbase + il], cy_t), cz_t);
+            psi = dd3_exact(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, geo, xin, y, z);
           } else {
-            psi = twdd3_exact(q, st, amu, aeta, axi, lxs[il], lys[jl], lzs[kl], th, xin, y, z);
+            psi = twdd3_exact(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, th, xin, y, z);
           }
         } else {
           if constexpr (SCHEME == DOMA_SCHEME_DD) {
-            const double geo = dA(cxs[nl * TX + il], cys[nl * PY + jl]);
-            psi = dd2_exact(q, st, amu, aeta, lxs[il], lys[jl], geo, xin, y);
+            const double geo = dA(cxs[cxbase + il], cy_t);
+            psi = dd2_exact(q, st, amu, aeta, lxs[il], ly_t, geo, xin, y);
           } else {
-            psi = twdd2_exact(q, st, amu, aeta, axi, lxs[il], lys[jl], th, xin, y);
+            psi = twdd2_exact(q, st, amu, aeta, axi, lxs[il], ly_t, th, xin, y);
           }
         }
         const size_t cg = ((size_t)phys_k(kl) * ny + phys_j(jl)) * nx + phys_i(il);
-        A.wpsi[cg * A.d_total + ord] = dM(wgt, psi);
+        A.wpsi[((size_t)task.grp * N + cg) * A.d_total + ord] = dM(wgt, psi);
       } else {
         if constexpr (DIMS == 3) {
           if constexpr (SCHEME == DOMA_SCHEME_DD)
-            psi = dd_f32(q, st, cxs[nl * TX + il], cys[nl * PY + jl], czs[nl * PZ + kl], xin, y, z);
+            psi = dd_f32(q, st, cxs[cxbase + il], cy_t, cz_t, xin, y, z);
           else
-            psi = twdd3_f32(q, st, amu, aeta, axi, lxs[il], lys[jl], lzs[kl], th, xin, y, z);
+            psi = twdd3_f32(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, th, xin, y, z);
         } else {
           if constexpr (SCHEME == DOMA_SCHEME_DD)
-            psi = dd2_f32(q, st, cxs[nl * TX + il], cys[nl * PY + jl], xin, y);
+            psi = dd2_f32(q, st, cxs[cxbase + il], cy_t, xin, y);
           else
-            psi = twdd2_f32(q, st, amu, aeta, axi, lxs[il], lys[jl], th, xin, y);
+            psi = twdd2_f32(q, st, amu, aeta, axi, lxs[il], ly_t, th, xin, y);
         }
-        P[nl * CELLS + e] = fM(wgt_f, psi);
+        wp = fM(wgt_f, psi);
       }
       yo = y;
       zo = z;
-      if (jl == vy - 1) yout[(kl * TX + il) * kGroup + nl] = y;
-      if (DIMS == 3 && kl == vz - 1) zout[(jl * TX + il) * kGroup + nl] = z;
+      if (jl == vy - 1) yout[ybase + il * kGroup] = y;
+      if (DIMS == 3 && kl == vz - 1) zout[zbase + il * kGroup] = z;
+    }
+    if constexpr (!EXACT) {
+      // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1:
+      // sum the pair in-warp, store one value per pair
+      const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
+      if (valid && lane < 16) P[(nl >> 1) * CELLS + e] = pair;
     }
     ysh = __shfl_up_sync(FULL, yo, 1);
     if (DIMS == 3) zsh = __shfl_up_sync(FULL, zo, PY);
@@ -482,20 +508,21 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   for (int e = t; e < SM::YF; e += blockDim.x) {
     const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
     if (nn < gs && il < vx && kk < vz)
-      A.yf[(((size_t)o * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn] = yout[e];
+      A.yf[(((size_t)of * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn] = yout[e];
   }
   if (DIMS == 3)
     for (int e = t; e < SM::ZF; e += blockDim.x) {
       const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
       if (nn < gs && il < vx && jj < vy)
-        A.zf[(((size_t)o * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn] = zout[e];
+        A.zf[(((size_t)of * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn] = zout[e];
     }
   if constexpr (!EXACT) {
     for (int e = t; e < CELLS; e += blockDim.x) {
       const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
       if (il < vx && jj < vy && kk < vz) {
         float sum = 0.0f, comp = 0.0f;
-        for (int nn = 0; nn < gs; ++nn) {  // Kahan, fixed ordinate order
+        const int npairs = (gs + 1) >> 1;
+        for (int nn = 0; nn < npairs; ++nn) {  // Kahan over ordinate pairs, fixed order
           const float yv = fS(P[nn * CELLS + e], comp);
           const float tv = fA(sum, yv);
           comp = fS(fS(tv, sum), yv);
@@ -523,14 +550,18 @@ template <typename T, int DIMS, int SCHEME, int TX>
 __global__ void __launch_bounds__(kMaxSweepThreads) sweep_persistent_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ unsigned s_task;
+  __shared__ unsigned s_next;
   const unsigned epoch = *A.epoch + 1u;
+  const unsigned claimer = blockDim.x - 1;   // not thread 0, which does the waits
+  if (threadIdx.x == claimer) s_next = atomicAdd(A.ticket, 1u);
+  __syncthreads();
   for (;;) {
-    __syncthreads();  // previous task's shared memory is free
-    if (threadIdx.x == 0) s_task = atomicAdd(A.ticket, 1u);
-    __syncthreads();
-    const unsigned tk = s_task;
+    const unsigned tk = s_next;
+    __syncthreads();  // everyone has read the ticket; the previous task's smem is free
     if (tk >= (unsigned)A.num_tasks) break;
+    // claim the following ticket now: its round trip overlaps this task (the
+    // task's internal barriers order the write before the next read)
+    if (threadIdx.x == claimer) s_next = atomicAdd(A.ticket, 1u);
     run_task<T, DIMS, SCHEME, TX>(A, A.tasks[tk], smem_raw, true, epoch);
   }
   if (threadIdx.x == 0) {

@@ -221,13 +221,16 @@ class Problem:
 
 def make_options(scheme: str = "dd", theta: float = 0.9, precision: str = "fp64",
                  fs_tol: float = 1e-8, fs_max_it: int = 1000, mg_tol: float = 1e-8,
-                 mg_max_it: int = 200, verbose: int = 0, tile=(0, 0, 0)) -> abi.DomaOptions:
+                 mg_max_it: int = 200, verbose: int = 0, tile=(0, 0, 0),
+                 iteration: str = "gauss_seidel") -> abi.DomaOptions:
     schemes = {"dd": abi.DOMA_SCHEME_DD, "tw_dd": abi.DOMA_SCHEME_TW_DD}
     precs = {"fp64": abi.DOMA_PREC_FP64, "fp32": abi.DOMA_PREC_FP32}
+    iters = {"gauss_seidel": abi.DOMA_ITER_GAUSS_SEIDEL, "multigroup": abi.DOMA_ITER_MULTIGROUP}
     return abi.DomaOptions(
         scheme=schemes[scheme], theta=theta, precision=precs[precision],
         fs_tol=fs_tol, fs_max_it=fs_max_it, mg_tol=mg_tol, mg_max_it=mg_max_it,
         verbose=verbose, tile_x=tile[0], tile_y=tile[1], tile_z=tile[2],
+        iteration=iters[iteration],
     )
 
 

@@ -2,7 +2,7 @@
 
     python -m doma_gb300.profile_case [--n 64] [--groups 8] [--np 4] [--na 4]
         [--precision fp32|fp64] [--scheme dd|tw_dd] [--tile 8] [--sweeps 3]
-        [--solve] [--schedule persistent|levels]
+        [--solve] [--schedule persistent|levels] [--loop graph|host]
 
 Builds the seeded checkerboard problem (doma_gb300.problems.checkerboard) on
 cuda:0, sets up group 0's source with one source iteration, then runs
@@ -31,9 +31,13 @@ def main() -> None:
     ap.add_argument("--sweeps", type=int, default=3)
     ap.add_argument("--solve", action="store_true")
     ap.add_argument("--schedule", choices=["persistent", "levels"], default="persistent")
+    ap.add_argument("--loop", choices=["graph", "host"], default="graph",
+                    help="host: host-driven solve loop (kernels profilable one by one)")
     a = ap.parse_args()
     if a.schedule == "levels":
         os.environ["DOMA_SWEEP_SCHEDULE"] = "levels"
+    if a.loop == "host":
+        os.environ["DOMA_SOLVE_LOOP"] = "host"
 
     import torch
 

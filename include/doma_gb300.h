@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define DOMA_ABI_VERSION 1u
+#define DOMA_ABI_VERSION 2u
 
 /* Status codes returned by every entry point. */
 typedef enum doma_status {
@@ -67,6 +67,17 @@ enum { DOMA_SCHEME_DD = 0, DOMA_SCHEME_TW_DD = 1 };
  *   DOMA_PREC_FP32: single-precision sweep with compensated angular sums;
  *     sources, scalar flux, residual and convergence norms stay double. */
 enum { DOMA_PREC_FP64 = 0, DOMA_PREC_FP32 = 1 };
+
+/* Iteration structure.
+ *   DOMA_ITER_GAUSS_SEIDEL: DOMA's own (solveFixedSource): groups in order,
+ *     each with a within-group source iteration; fs_* and mg_* apply.
+ *   DOMA_ITER_MULTIGROUP: every group in flight.  Source iteration on the
+ *     whole multigroup scattering + fission operator in increment form: each
+ *     iteration sweeps all groups in one launch, then forms the next
+ *     increment's source for every group from all groups' increments.
+ *     Converges to the same solution; fs_tol (relative L2 of the increment
+ *     over all groups) and fs_max_it apply, mg_* are unused. */
+enum { DOMA_ITER_GAUSS_SEIDEL = 0, DOMA_ITER_MULTIGROUP = 1 };
 
 /* A fixed-source problem on a tensor-product Cartesian mesh.
  * Cells are numbered x fastest, then y, then z (src/BrickMesh3D.cpp:83-102).
@@ -103,6 +114,7 @@ typedef struct doma_options {
   uint32_t verbose;     /* 0: silent, 1: the reference's progress lines on stdout,
                            2: also every SI residual (the reference's --verbose) */
   uint32_t tile_x, tile_y, tile_z;   /* sweep block shape in cells; 0 = pick */
+  uint32_t iteration;   /* DOMA_ITER_GAUSS_SEIDEL (default) or DOMA_ITER_MULTIGROUP */
 } doma_options;
 
 /* Filled by doma_solver_solve_fixed_source. */

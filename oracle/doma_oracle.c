@@ -550,3 +550,66 @@ int oracle_source_iterations(const doma_problem *p, const doma_options *o,
   state_free(&s);
   return 0;
 }
+
+int oracle_multigroup_solve(const doma_problem *p, const doma_options *o, uint32_t num_threads,
+                            double *phi_out, uint32_t *iterations, double *residual)
+{
+  oracle_state s;
+  const unsigned T = num_threads ? num_threads : 1;
+  omp_set_num_threads((int)T);
+  if (state_init(&s, p, o, T)) { state_free(&s); return -1; }
+  const size_t N = s.N;
+  const unsigned G = s.G;
+  const double a = s.src_scale;
+  double *qall = calloc(N * G, sizeof(double)), *dall = calloc(N * G, sizeof(double));
+  double *q_own = s.q;
+  for (size_t c = 0; c < N; ++c) {
+    const unsigned m = p->cell_material[c];
+    for (unsigned g = 0; g < G; ++g)
+      qall[(size_t)g * N + c] = p->source ? a * p->source[(size_t)m * G + g] / M_PI : 0.0;
+  }
+  unsigned it = 0;
+  double res = 0.0;
+  do {
+    for (unsigned g = 0; g < G; ++g) {
+      s.q = qall + (size_t)g * N;
+      for (size_t c = 0; c < N; ++c) {
+        s.sigt[c] = p->total[(size_t)p->cell_material[c] * G + g];
+        s.cur[c] = 0.0;
+      }
+      sweep(&s);
+      memcpy(dall + (size_t)g * N, s.cur, sizeof(double) * N);
+    }
+    double diff = 0.0, tot = 0.0;
+    for (size_t c = 0; c < N; ++c) {
+      const unsigned m = p->cell_material[c];
+      for (unsigned g = 0; g < G; ++g) {
+        const double d = dall[(size_t)g * N + c];
+        const double t = s.phi[(size_t)g * N + c] + d;
+        diff = diff + (d * d) * s.vol[c];
+        tot = tot + (t * t) * s.vol[c];
+        s.phi[(size_t)g * N + c] = t;
+      }
+      const int fis = p->has_fission && p->has_fission[m];
+      for (unsigned h = 0; h < G; ++h) {
+        double acc = 0.0;
+        for (unsigned g = 0; g < G; ++g) {
+          double k = p->scatter[((size_t)m * G + h) * G + g];
+          if (fis) k = k + p->chi_p[(size_t)m * G + h] * p->nu_sigma_f[(size_t)m * G + g];
+          acc = acc + k * dall[(size_t)g * N + c];
+        }
+        qall[(size_t)h * N + c] = a * acc / M_PI;
+      }
+    }
+    res = tot > 1e-8 ? sqrt(diff) / sqrt(tot) : 0.0;
+    ++it;
+  } while (it < o->fs_max_it && o->fs_tol < res && isfinite(res));
+  s.q = q_own;
+  memcpy(phi_out, s.phi, sizeof(double) * N * G);
+  if (iterations) *iterations = it;
+  if (residual) *residual = res;
+  free(qall);
+  free(dall);
+  state_free(&s);
+  return it < o->fs_max_it ? 1 : 0;
+}

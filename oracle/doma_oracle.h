@@ -40,6 +40,13 @@ int oracle_source_iterations(const doma_problem *p, const doma_options *o,
                              uint32_t num_threads, uint32_t group, uint32_t count,
                              double *phi_out, double *residuals);
 
+/* Multigroup source iteration (the GPU library's DOMA_ITER_MULTIGROUP mode,
+ * which DOMA itself does not have): increment form over all groups at once,
+ * delta_q_h = s/pi * sum_g (S[h][g] + chi_h nu_sigma_f_g) delta_phi_g.  Same
+ * sweep as oracle_solve; returns 1 converged, 0 cap reached, -1 bad input. */
+int oracle_multigroup_solve(const doma_problem *p, const doma_options *o, uint32_t num_threads,
+                            double *phi_out, uint32_t *iterations, double *residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,11 @@ def oracle() -> ctypes.CDLL:
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
             ctypes.c_uint32, ctypes.c_uint32, _dp, _dp,
         ]
+        lib.oracle_multigroup_solve.restype = ctypes.c_int
+        lib.oracle_multigroup_solve.argtypes = [
+            ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
+            _dp, _u32p, _dp,
+        ]
         _oracle = lib
     return _oracle
 
@@ -122,6 +127,20 @@ def oracle_source_iterations(p: Problem, opts: abi.DomaOptions, group: int, coun
     if rc < 0:
         raise ValueError("oracle rejected the problem")
     return phi, res[:count]
+
+
+def oracle_multigroup_solve(p: Problem, opts: abi.DomaOptions, threads: int = 1):
+    """-> (phi[G][N], converged, iterations, residual)"""
+    phi = np.zeros((p.num_groups, p.num_cells))
+    it = ctypes.c_uint32(0)
+    res = ctypes.c_double(0)
+    cp = p.to_c()
+    rc = oracle().oracle_multigroup_solve(ctypes.byref(cp), ctypes.byref(opts), threads,
+                                          phi.ctypes.data_as(_dp), ctypes.byref(it),
+                                          ctypes.byref(res))
+    if rc < 0:
+        raise ValueError("oracle rejected the problem")
+    return phi, bool(rc), int(it.value), float(res.value)
 
 
 _SI_RE = re.compile(r"SI (?:converged|failed to converge) after (\d+) iterations")

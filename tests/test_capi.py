@@ -39,7 +39,7 @@ def test_header_declares_expected_entry_points():
 def test_library_exports_every_declared_symbol(lib):
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.doma_abi_version() == 1
+    assert lib.doma_abi_version() == abi.ABI_VERSION
 
 
 def test_default_options(lib):

@@ -226,3 +226,60 @@ def test_progress_lines_match_reference(monkeypatch, capfd, loop, name):
         opts.verbose = 2
         run(p, opts)
         assert capfd.readouterr().out == exp["log_verbose"]
+
+
+# ---- multigroup mode (every group in flight) -----------------------------------
+
+@pytest.mark.parametrize("dims", [2, 3])
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+def test_multigroup_matches_oracle_iteration(dims, scheme):
+    """FP64 multigroup mode against the CPU restatement of the same iteration:
+    same iteration count, same flux (1e-12), and FP32 within 1e-5 of it."""
+    p = P.random_problem(51, dims, 9, 8, 6, groups=4, np_=2, na=2, materials=3, fission=True)
+    o64 = P.make_options(scheme=scheme, theta=0.8, fs_tol=1e-11, fs_max_it=5000,
+                         iteration="multigroup")
+    o_phi, ok, o_it, _ = ol.oracle_multigroup_solve(p, o64)
+    phi, rep = run(p, o64)
+    assert rep.converged == ok and rep.mg_iterations == o_it
+    assert rel_linf(phi, o_phi) <= FP64_RTOL
+    o32 = P.make_options(scheme=scheme, theta=0.8, precision="fp32", fs_tol=1e-7,
+                         fs_max_it=5000, iteration="multigroup")
+    phi32, rep32 = run(p, o32)
+    assert rep32.converged and rel_l2(phi32, o_phi) <= FP32_RTOL, rel_l2(phi32, o_phi)
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_multigroup_dd_has_the_reference_fixed_point(dims):
+    """DD is linear, so multigroup iteration converges to DOMA's own solution.
+    (TW-DD is not: its weights act on increments, so each iteration path has
+    its own fixed point; DOMA's is reached only by the Gauss-Seidel mode.)"""
+    p = P.random_problem(53, dims, 9, 8, 6, groups=4, np_=2, na=2, materials=3, fission=True)
+    ref_opts = P.make_options(scheme="dd", fs_tol=1e-13, mg_tol=1e-13, fs_max_it=5000,
+                              mg_max_it=2000)
+    o_phi, ok, *_ = ol.oracle_solve(p, ref_opts)
+    assert ok
+    phi, rep = run(p, P.make_options(scheme="dd", fs_tol=1e-13, fs_max_it=5000,
+                                     iteration="multigroup"))
+    assert rep.converged and rel_l2(phi, o_phi) <= 1e-10, rel_l2(phi, o_phi)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_multigroup_graph_equals_host_loop_and_levels(monkeypatch, precision):
+    p = P.checkerboard(2, n=12, groups=3, np_=2, na=2, block=4)
+    opts = P.make_options(scheme="tw_dd", theta=0.7, precision=precision, fs_tol=1e-7,
+                          fs_max_it=2000, iteration="multigroup")
+    a, ra = run(p, opts)
+    monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    b, rb = run(p, opts)
+    monkeypatch.setenv("DOMA_SWEEP_SCHEDULE", "levels")
+    c, rc = run(p, opts)
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+    assert ra.mg_iterations == rb.mg_iterations == rc.mg_iterations
+    assert ra.si_iterations == ra.mg_iterations * p.num_groups
+
+
+def test_multigroup_cap_is_reported():
+    p = P.random_problem(52, 3, 6, 5, 4, groups=3, np_=1, na=2, materials=2)
+    opts = P.make_options(fs_tol=1e-14, fs_max_it=4, iteration="multigroup")
+    phi, rep = run(p, opts)
+    assert not rep.converged and rep.status == 1 and rep.mg_iterations == 4
