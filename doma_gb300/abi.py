@@ -125,6 +125,16 @@ SIGNATURES = {
         [ctypes.c_void_p, _u32p, _u32p, ctypes.POINTER(ctypes.c_uint64)],
     ),
     "doma_solver_destroy": (None, [ctypes.c_void_p]),
+    "doma_batch_create": (
+        ctypes.c_int,
+        [ctypes.POINTER(DomaProblem), ctypes.c_size_t, ctypes.POINTER(DomaOptions),
+         ctypes.POINTER(ctypes.c_void_p)],
+    ),
+    "doma_batch_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "doma_batch_tune": (ctypes.c_int, [ctypes.c_void_p, _u32p]),
+    "doma_batch_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport), ctypes.c_size_t]),
+    "doma_batch_get_scalar_flux": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _dp, ctypes.c_size_t]),
+    "doma_batch_destroy": (None, [ctypes.c_void_p]),
     "doma_sweep_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(DomaProblem), ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p,

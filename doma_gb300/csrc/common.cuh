@@ -39,6 +39,21 @@ struct Task {
   int oct, og, bi, bj, bk, grp;
 };
 
+// A task of a batched sweep: the problem it belongs to and its own task.
+struct BatchTask {
+  Task t;
+  int prob;
+};
+
+// Per-problem loop state of a batched solve (device memory).
+struct BatchLoop {
+  unsigned active;   // 1 while the problem iterates
+  unsigned it;       // iterations done
+  unsigned status;   // doma_status once finished
+  unsigned pad;
+  double res;        // last relative increment norm
+};
+
 // Everything a sweep launch needs.  Pointers are device pointers.
 template <typename T>
 struct SweepArgs {
@@ -113,6 +128,14 @@ size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx);
 doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem);
 // CTAs of the persistent sweep kernel that fit on the device at once.
 int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem);
+
+// One persistent sweep over every active problem of a batch (FP32).  The
+// counters are the batch's own; args[p] is problem p's sweep arguments.
+doma_status launch_sweep_batch(int dims, int scheme, int tx, int grid, int threads, size_t smem,
+                               const SweepArgs<float> * args, const BatchTask * tasks,
+                               int num_tasks, unsigned * ticket, unsigned * exit_count,
+                               unsigned * epoch, const BatchLoop * loops, cudaStream_t stream);
+int sweep_batch_resident_ctas(int dims, int scheme, int tx, int threads, size_t smem);
 
 // Host quadrature (quadrature.cpp).
 int gc_quadrature(unsigned np, unsigned na, unsigned dims, double * mu, double * eta,

@@ -250,51 +250,60 @@ __global__ void __launch_bounds__(kBlock) mgi_init_kernel(const IterArgs A, T * 
 //   q_h  = s / pi * sum_g (S[h][g] + chi[h] nu_sigma_f[g]) d_g   (next increment)
 // The G x G contraction per cell is small (G <= 16 in every workload here)
 // and memory-bound, so it stays on the CUDA cores.
+// One cell of the multigroup epilogue (shared by the single-problem and the
+// batched kernels): group increments from the partials, residual sums, flux
+// update, next increment's source.
+template <typename T>
+__device__ __forceinline__ void mgi_cell(const IterArgs & A, size_t c, T * q, double * dscratch,
+                                         double & diff, double & tot)
+{
+  const size_t N = A.N;
+  const int G = A.G;
+  const int per_group = 8 * A.ngroups;
+  const double V = A.vol[c];
+  for (int g = 0; g < G; ++g) {
+    double d = 0.0;
+    if (A.exact) {
+      // every ordinate in DOMA's single-thread order (octant, then ordinate)
+      const double * w = A.wpsi + ((size_t)g * N + c) * (size_t)A.D;
+      for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
+    } else {
+      for (int o = 0; o < 8; ++o)
+        if (A.oct_mask & (1 << o))
+          for (int og = 0; og < A.ngroups; ++og)
+            d = dA(d, A.octphi[((size_t)g * per_group + (size_t)o * A.ngroups + og) * N + c]);
+    }
+    double * ph = A.phi + (size_t)g * N + c;
+    const double t = dA(*ph, d);
+    diff = dA(diff, dM(dM(d, d), V));
+    tot = dA(tot, dM(dM(t, t), V));
+    *ph = t;
+    dscratch[(size_t)g * N + c] = d;
+  }
+  const unsigned m = A.mat[c];
+  const bool fis = A.fis && A.fis[m];
+  for (int h = 0; h < G; ++h) {
+    double acc = 0.0;
+    const double * Sh = A.scatter + ((size_t)m * G + h) * G;
+    const double chi = fis ? A.chi[(size_t)m * G + h] : 0.0;
+    for (int g = 0; g < G; ++g) {
+      double k = Sh[g];
+      if (fis) k = dA(k, dM(chi, A.nsf[(size_t)m * G + g]));
+      acc = dA(acc, dM(k, dscratch[(size_t)g * N + c]));
+    }
+    q[(size_t)h * N + c] = (T)dD(dM(A.src_scale, acc), kPi);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock) mgi_epilogue_kernel(const IterArgs A, T * q,
                                                              double * dscratch, double * norms,
                                                              const LoopParams L)
 {
-  const size_t N = A.N;
-  const int G = A.G;
-  const int per_group = 8 * A.ngroups;
   double diff = 0.0, tot = 0.0;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
-       c += (size_t)gridDim.x * blockDim.x) {
-    const double V = A.vol[c];
-    for (int g = 0; g < G; ++g) {
-      double d = 0.0;
-      if (A.exact) {
-        // every ordinate in DOMA's single-thread order (octant, then ordinate)
-        const double * w = A.wpsi + ((size_t)g * N + c) * (size_t)A.D;
-        for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
-      } else {
-        for (int o = 0; o < 8; ++o)
-          if (A.oct_mask & (1 << o))
-            for (int og = 0; og < A.ngroups; ++og)
-              d = dA(d, A.octphi[((size_t)g * per_group + (size_t)o * A.ngroups + og) * N + c]);
-      }
-      double * ph = A.phi + (size_t)g * N + c;
-      const double t = dA(*ph, d);
-      diff = dA(diff, dM(dM(d, d), V));
-      tot = dA(tot, dM(dM(t, t), V));
-      *ph = t;
-      dscratch[(size_t)g * N + c] = d;
-    }
-    const unsigned m = A.mat[c];
-    const bool fis = A.fis && A.fis[m];
-    for (int h = 0; h < G; ++h) {
-      double acc = 0.0;
-      const double * Sh = A.scatter + ((size_t)m * G + h) * G;
-      const double chi = fis ? A.chi[(size_t)m * G + h] : 0.0;
-      for (int g = 0; g < G; ++g) {
-        double k = Sh[g];
-        if (fis) k = dA(k, dM(chi, A.nsf[(size_t)m * G + g]));
-        acc = dA(acc, dM(k, dscratch[(size_t)g * N + c]));
-      }
-      q[(size_t)h * N + c] = (T)dD(dM(A.src_scale, acc), kPi);
-    }
-  }
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < A.N;
+       c += (size_t)gridDim.x * blockDim.x)
+    mgi_cell(A, c, q, dscratch, diff, tot);
   if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
     LoopCtl * C = L.ctl;
     const double res = norm_ratio(norms[0], norms[1]);
@@ -319,7 +328,84 @@ __global__ void __launch_bounds__(kBlock) mgi_epilogue_kernel(const IterArgs A, 
   }
 }
 
+// ---- batched multigroup solve ---------------------------------------------
+
+// Epilogue of every active problem of a batch: block b works on problem
+// block_prob[b] (its blocks are contiguous), writes its partial norms to that
+// problem's partials; batch_finalize_kernel reduces them.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) batch_epilogue_kernel(const BatchSlot * slots,
+                                                               const int * block_prob,
+                                                               const BatchLoop * loops)
+{
+  const int p = block_prob[blockIdx.x];
+  if (!loops[p].active) return;
+  const BatchSlot & S = slots[p];
+  const int lb = blockIdx.x - S.block0;
+  double diff = 0.0, tot = 0.0;
+  for (size_t c = (size_t)lb * blockDim.x + threadIdx.x; c < S.it.N;
+       c += (size_t)S.blocks * blockDim.x)
+    mgi_cell(S.it, c, static_cast<T *>(S.q), S.dscratch, diff, tot);
+  block_sum2(diff, tot);
+  if (threadIdx.x == 0) {
+    S.it.partials[2 * lb] = diff;
+    S.it.partials[2 * lb + 1] = tot;
+  }
+}
+
+// One block per problem: sum the problem's block partials in block order,
+// then DOMA-style loop test on its relative increment norm.
+__global__ void __launch_bounds__(kBlock) batch_finalize_kernel(const BatchSlot * slots,
+                                                               BatchLoop * loops, double tol,
+                                                               unsigned max_it,
+                                                               unsigned * still_active)
+{
+  const int p = blockIdx.x;
+  if (!loops[p].active) return;
+  const BatchSlot & S = slots[p];
+  double a = 0.0, b = 0.0;
+  for (int k = threadIdx.x; k < S.blocks; k += blockDim.x) {
+    a += S.it.partials[2 * k];
+    b += S.it.partials[2 * k + 1];
+  }
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    BatchLoop & L = loops[p];
+    const double res = norm_ratio(a, b);
+    L.it += 1;
+    L.res = res;
+    const bool ok = finite2(a, b);
+    const bool more = ok && L.it < max_it && tol < res;
+    if (!more) {
+      L.active = 0u;
+      L.status = !ok ? DOMA_NUMERIC_ERROR : (L.it < max_it ? DOMA_OK : DOMA_NOT_CONVERGED);
+    } else {
+      atomicAdd(still_active, 1u);
+    }
+  }
+}
+
 }  // namespace
+
+doma_status launch_batch_epilogue(const BatchSlot * slots, const int * block_prob, int blocks,
+                                  const BatchLoop * loops, int precision, cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    batch_epilogue_kernel<double><<<blocks, kBlock, 0, st>>>(slots, block_prob, loops);
+  else
+    batch_epilogue_kernel<float><<<blocks, kBlock, 0, st>>>(slots, block_prob, loops);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_batch_finalize(const BatchSlot * slots, BatchLoop * loops, int count,
+                                  double tol, unsigned max_it, unsigned * still_active,
+                                  cudaStream_t st)
+{
+  batch_finalize_kernel<<<count, kBlock, 0, st>>>(slots, loops, tol, max_it, still_active);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
 
 doma_status launch_mgi_init(const IterArgs & a, int precision, void * q, void * sigt,
                             cudaStream_t st)

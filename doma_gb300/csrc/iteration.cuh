@@ -75,6 +75,21 @@ doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * 
                                double * norms, const LoopParams & L, cudaStream_t st);
 doma_status launch_mg_residual(const IterArgs & a, double * norms, const LoopParams & L,
                                cudaStream_t st);
+// Batched multigroup solve: per-problem data of the batched epilogue.
+struct BatchSlot {
+  IterArgs it;            // the problem's cell data (partials sized >= blocks)
+  void * q;               // [G][N] next increment's source, sweep precision
+  double * dscratch;      // [G][N]
+  int block0;             // first block of this problem in the batched grid
+  int blocks;             // blocks of this problem
+};
+
+doma_status launch_batch_epilogue(const BatchSlot * slots, const int * block_prob, int blocks,
+                                  const BatchLoop * loops, int precision, cudaStream_t st);
+doma_status launch_batch_finalize(const BatchSlot * slots, BatchLoop * loops, int count,
+                                  double tol, unsigned max_it, unsigned * still_active,
+                                  cudaStream_t st);
+
 // Multigroup mode (every group in flight).
 doma_status launch_mgi_init(const IterArgs & a, int precision, void * q, void * sigt,
                             cudaStream_t st);

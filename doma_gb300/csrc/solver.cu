@@ -1113,3 +1113,334 @@ doma_status doma_solver_describe(const doma_solver * s, uint32_t tile[3],
 void doma_solver_destroy(doma_solver * s) { release(s); }
 
 }  // extern "C"
+
+
+// ============================================================================
+// Batched solve (C ABI doma_batch_*): many independent problems share one
+// persistent sweep launch per iteration.
+// ============================================================================
+
+namespace {
+
+struct BatchCtl {
+  unsigned ticket, exit_count, epoch;
+  int error;
+  unsigned still_active;
+};
+
+}  // namespace
+
+struct doma_batch {
+  std::vector<doma_solver *> solvers;
+  doma_options opts{};
+  int dims = 3;
+  int tx = 8, threads = 256, grid = 0;
+  size_t smem = 0;
+  int num_tasks = 0, epi_blocks = 0;
+  SweepArgs<float> * d_args = nullptr;
+  BatchTask * d_tasks = nullptr;
+  BatchSlot * d_slots = nullptr;
+  int * d_block_prob = nullptr;
+  BatchLoop * d_loops = nullptr;
+  BatchCtl * d_ctl = nullptr;
+  BatchCtl * h_ctl = nullptr;
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+  std::vector<void *> allocs;
+};
+
+namespace {
+
+template <typename T>
+doma_status balloc(doma_batch * b, T ** p, size_t count)
+{
+  void * v = nullptr;
+  DOMA_CUDA_TRY(cudaMalloc(&v, std::max<size_t>(1, count) * sizeof(T)));
+  b->allocs.push_back(v);
+  *p = static_cast<T *>(v);
+  return DOMA_OK;
+}
+
+void bfree(doma_batch * b, void * p)
+{
+  if (!p) return;
+  for (auto it = b->allocs.begin(); it != b->allocs.end(); ++it)
+    if (*it == p) {
+      b->allocs.erase(it);
+      break;
+    }
+  cudaFree(p);
+}
+
+void sfree(doma_solver * s, void * p)
+{
+  if (!p) return;
+  for (auto it = s->allocations.begin(); it != s->allocations.end(); ++it)
+    if (*it == p) {
+      s->allocations.erase(it);
+      break;
+    }
+  cudaFree(p);
+}
+
+// Rebuild one solver's sweep schedule for block length tx (fresh task list
+// and done flags; its single-problem launches follow the new shape too).
+doma_status reschedule(doma_solver * s, int tx)
+{
+  s->opts.tile_x = (uint32_t)tx;
+  pick_tile(s, &s->opts);
+  build_schedule(s);
+  DOMA_TRY(sweep_prepare(s->dims, s->opts.precision, s->opts.scheme, s->sched.tx, s->sched.smem));
+  sfree(s, s->d_tasks);
+  sfree(s, s->d_done);
+  DOMA_TRY(upload(s, &s->d_tasks, s->sched.tasks.data(), s->sched.tasks.size()));
+  const size_t flags = (size_t)s->gif * 8 * s->sched.ngroups * s->sched.nbx * s->sched.nby * s->sched.nbz;
+  DOMA_TRY(dalloc(s, &s->d_done, flags));
+  DOMA_CUDA_TRY(cudaMemset(s->d_done, 0, flags * sizeof(unsigned)));
+  const int fit = sweep_resident_ctas(s->dims, s->opts.precision, s->opts.scheme, s->sched.tx,
+                                      s->sched.threads, s->sched.smem);
+  s->sched.grid = std::max(1, std::min<int>(fit, (int)s->sched.tasks.size()));
+  for (auto * a : {&s->a32}) {
+    a->nbx = s->sched.nbx; a->nby = s->sched.nby; a->nbz = s->sched.nbz;
+    a->num_tasks = (int)s->sched.tasks.size();
+    a->tasks = s->d_tasks;
+    a->done = s->d_done;
+  }
+  return DOMA_OK;
+}
+
+// The batch's merged task list, sweep arguments and epilogue layout for the
+// current block length.
+doma_status build_batch_schedule(doma_batch * b)
+{
+  const size_t P = b->solvers.size();
+  b->smem = sweep_smem_bytes(b->dims, DOMA_PREC_FP32, b->opts.scheme, b->tx);
+  std::vector<BatchTask> tasks;
+  int max_levels = 0;
+  for (auto * s : b->solvers) max_levels = std::max(max_levels, (int)s->sched.level_begin.size() - 1);
+  for (int L = 0; L < max_levels; ++L)
+    for (size_t p = 0; p < P; ++p) {
+      const Schedule & sc = b->solvers[p]->sched;
+      if (L + 1 >= (int)sc.level_begin.size()) continue;
+      for (int t = sc.level_begin[L]; t < sc.level_begin[L + 1]; ++t)
+        tasks.push_back(BatchTask{sc.tasks[t], (int)p});
+    }
+  b->num_tasks = (int)tasks.size();
+  bfree(b, b->d_tasks);
+  DOMA_TRY(balloc(b, &b->d_tasks, tasks.size()));
+  DOMA_CUDA_TRY(cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(BatchTask),
+                           cudaMemcpyHostToDevice));
+  std::vector<SweepArgs<float>> args(P);
+  for (size_t p = 0; p < P; ++p) {
+    args[p] = b->solvers[p]->a32;
+    args[p].error = &b->d_ctl->error;
+    args[p].spin_limit = 1u << 22;
+    args[p].wait_bias = 0u;
+  }
+  DOMA_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), P * sizeof(SweepArgs<float>),
+                           cudaMemcpyHostToDevice));
+  const int fit = sweep_batch_resident_ctas(b->dims, b->opts.scheme, b->tx, b->threads, b->smem);
+  if (fit <= 0) return bad("the batched sweep block does not fit on this device");
+  b->grid = std::max(1, std::min(fit, b->num_tasks));
+  return DOMA_OK;
+}
+
+doma_status batch_sweep(doma_batch * b)
+{
+  return launch_sweep_batch(b->dims, b->opts.scheme, b->tx, b->grid, b->threads, b->smem, b->d_args,
+                            b->d_tasks, b->num_tasks, &b->d_ctl->ticket, &b->d_ctl->exit_count,
+                            &b->d_ctl->epoch, b->d_loops, b->stream);
+}
+
+doma_status batch_init_sources(doma_batch * b)
+{
+  for (auto * s : b->solvers)
+    DOMA_TRY(launch_mgi_init(s->it, DOMA_PREC_FP32, s->d_q, s->d_sigt, b->stream));
+  std::vector<BatchLoop> loops(b->solvers.size(), BatchLoop{1u, 0u, 0u, 0u, 0.0});
+  DOMA_CUDA_TRY(cudaMemcpyAsync(b->d_loops, loops.data(), loops.size() * sizeof(BatchLoop),
+                                cudaMemcpyHostToDevice, b->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->error, 0, sizeof(int), b->stream));
+  return DOMA_OK;
+}
+
+void batch_release(doma_batch * b)
+{
+  if (!b) return;
+  for (auto * s : b->solvers) release(s);
+  for (void * p : b->allocs) cudaFree(p);
+  if (b->h_ctl) cudaFreeHost(b->h_ctl);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+doma_status doma_batch_create(const doma_problem * problems, size_t count, const doma_options * opts,
+                              doma_batch ** out)
+{
+  if (!out) return bad("null output handle");
+  *out = nullptr;
+  if (!problems || !opts || count == 0) return bad("empty batch");
+  if (opts->precision != DOMA_PREC_FP32) return bad("batched solves sweep in FP32 (DOMA_PREC_FP32)");
+  doma_batch * b = new (std::nothrow) doma_batch();
+  if (!b) return bad("out of host memory");
+  b->opts = *opts;
+  b->opts.iteration = DOMA_ITER_MULTIGROUP;
+  b->dims = (int)problems[0].num_dims;
+  b->tx = sweep_tile_x(opts->tile_x ? (int)opts->tile_x
+                                    : (b->dims == 3 ? (opts->scheme == DOMA_SCHEME_TW_DD ? 16 : 8) : 32));
+  b->opts.tile_x = (uint32_t)b->tx;
+  auto fail = [&](doma_status st) {
+    batch_release(b);
+    return st;
+  };
+  for (size_t i = 0; i < count; ++i) {
+    if (problems[i].num_dims != (uint32_t)b->dims) return fail(bad("all problems of a batch share num_dims"));
+    doma_solver * s = nullptr;
+    const doma_status st = doma_solver_create(&problems[i], &b->opts, &s);
+    if (st != DOMA_OK) {
+      set_error("problem " + std::to_string(i) + ": " + get_error());
+      return fail(st);
+    }
+    b->solvers.push_back(s);
+  }
+  const size_t P = count;
+  doma_status st = DOMA_OK;
+  if ((st = balloc(b, &b->d_args, P)) != DOMA_OK) return fail(st);
+  if ((st = balloc(b, &b->d_slots, P)) != DOMA_OK) return fail(st);
+  if ((st = balloc(b, &b->d_loops, P)) != DOMA_OK) return fail(st);
+  if ((st = balloc(b, &b->d_ctl, 1)) != DOMA_OK) return fail(st);
+  if (cudaMemset(b->d_ctl, 0, sizeof(BatchCtl)) != cudaSuccess) return fail(DOMA_CUDA_ERROR);
+  if (cudaMallocHost(&b->h_ctl, sizeof(BatchCtl)) != cudaSuccess) return fail(DOMA_CUDA_ERROR);
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(DOMA_CUDA_ERROR);
+  b->stream = b->own_stream;
+  // batched epilogue layout: up to 64 blocks per problem, contiguous
+  std::vector<BatchSlot> slots(P);
+  std::vector<int> block_prob;
+  for (size_t p = 0; p < P; ++p) {
+    doma_solver * s = b->solvers[p];
+    slots[p].it = s->it;
+    slots[p].q = s->d_q;
+    slots[p].dscratch = s->d_dscratch;
+    slots[p].block0 = (int)block_prob.size();
+    slots[p].blocks = std::max(1, std::min(s->it.grid, 64));
+    block_prob.insert(block_prob.end(), slots[p].blocks, (int)p);
+  }
+  b->epi_blocks = (int)block_prob.size();
+  if ((st = balloc(b, &b->d_block_prob, block_prob.size())) != DOMA_OK) return fail(st);
+  if (cudaMemcpy(b->d_slots, slots.data(), P * sizeof(BatchSlot), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_block_prob, block_prob.data(), block_prob.size() * sizeof(int),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(DOMA_CUDA_ERROR);
+  if ((st = build_batch_schedule(b)) != DOMA_OK) return fail(st);
+  *out = b;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_set_stream(doma_batch * b, void * stream)
+{
+  if (!b) return bad("null batch");
+  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
+{
+  if (!b) return bad("null batch");
+  float best_ms = 0.0f;
+  int best = b->tx;
+  cudaEvent_t e0, e1;
+  DOMA_CUDA_TRY(cudaEventCreate(&e0));
+  DOMA_CUDA_TRY(cudaEventCreate(&e1));
+  for (int tx : {8, 16, 32}) {
+    for (auto * s : b->solvers) DOMA_TRY(reschedule(s, tx));
+    b->tx = tx;
+    DOMA_TRY(build_batch_schedule(b));
+    DOMA_TRY(batch_init_sources(b));
+    DOMA_TRY(batch_sweep(b));  // warm-up
+    DOMA_CUDA_TRY(cudaEventRecord(e0, b->stream));
+    for (int k = 0; k < 3; ++k) DOMA_TRY(batch_sweep(b));
+    DOMA_CUDA_TRY(cudaEventRecord(e1, b->stream));
+    DOMA_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    DOMA_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (best_ms == 0.0f || ms < best_ms) {
+      best_ms = ms;
+      best = tx;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (auto * s : b->solvers) DOMA_TRY(reschedule(s, best));
+  b->tx = best;
+  DOMA_TRY(build_batch_schedule(b));
+  if (tile_x) *tile_x = (uint32_t)best;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_solve(doma_batch * b, doma_report * reports, size_t count)
+{
+  if (!b) return bad("null batch");
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t P = b->solvers.size();
+  DOMA_TRY(batch_init_sources(b));
+  unsigned iters = 0;
+  for (;;) {
+    DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, sizeof(unsigned), b->stream));
+    DOMA_TRY(batch_sweep(b));
+    DOMA_TRY(launch_batch_epilogue(b->d_slots, b->d_block_prob, b->epi_blocks, b->d_loops,
+                                   DOMA_PREC_FP32, b->stream));
+    DOMA_TRY(launch_batch_finalize(b->d_slots, b->d_loops, (int)P, b->opts.fs_tol,
+                                   b->opts.fs_max_it, &b->d_ctl->still_active, b->stream));
+    DOMA_CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
+                                  b->stream));
+    DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    ++iters;
+    if (b->h_ctl->error) {
+      set_error("a batched sweep wait for an upstream block timed out");
+      return DOMA_DEVICE_WAIT_TIMEOUT;
+    }
+    if (b->h_ctl->still_active == 0 || iters > b->opts.fs_max_it) break;
+  }
+  std::vector<BatchLoop> loops(P);
+  DOMA_CUDA_TRY(cudaMemcpy(loops.data(), b->d_loops, P * sizeof(BatchLoop), cudaMemcpyDeviceToHost));
+  const auto t1 = std::chrono::steady_clock::now();
+  const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  doma_status first = DOMA_OK;
+  for (size_t p = 0; p < P; ++p) {
+    const doma_solver * s = b->solvers[p];
+    if (loops[p].status != DOMA_OK && first == DOMA_OK) first = (doma_status)loops[p].status;
+    if (reports && p < count) {
+      doma_report & r = reports[p];
+      r.status = loops[p].status;
+      r.mg_iterations = loops[p].it;
+      r.si_iterations = (uint64_t)loops[p].it * s->G;
+      r.updates = (uint64_t)loops[p].it * s->G * s->N * (uint64_t)s->D;
+      r.kernel_launches = 3ull * iters;
+      r.mg_residual = loops[p].res;
+      r.si_residual = loops[p].res;
+      r.solve_ms = ms;
+      r.si_counts_len = 1;
+      if (r.si_counts && r.si_counts_capacity) r.si_counts[0] = loops[p].it;
+    }
+  }
+  if (first != DOMA_OK) set_error("a problem of the batch did not converge");
+  return first;
+}
+
+doma_status doma_batch_get_scalar_flux(doma_batch * b, size_t index, double * out, size_t count)
+{
+  if (!b) return bad("null batch");
+  if (index >= b->solvers.size()) return bad("problem index out of range");
+  doma_solver * s = b->solvers[index];
+  if (!out || count < (size_t)s->G * s->N) return bad("output buffer too small");
+  DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  DOMA_CUDA_TRY(cudaMemcpy(out, s->d_phi, (size_t)s->G * s->N * sizeof(double), cudaMemcpyDeviceToHost));
+  return DOMA_OK;
+}
+
+void doma_batch_destroy(doma_batch * b) { batch_release(b); }
+
+}  // extern "C"

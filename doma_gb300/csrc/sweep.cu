@@ -576,6 +576,51 @@ __global__ void __launch_bounds__(kMaxSweepThreads) sweep_persistent_kernel(cons
   }
 }
 
+// Batched persistent sweep: one grid works through the level-merged tasks of
+// every problem of a batch.  Tasks of problems that have converged publish
+// their done flag and return, so a batch keeps one static task list.
+template <typename T, int DIMS, int SCHEME, int TX>
+__global__ void __launch_bounds__(kMaxSweepThreads)
+    sweep_batch_kernel(const SweepArgs<T> * args, const BatchTask * tasks, int num_tasks,
+                       unsigned * ticket, unsigned * exit_count, unsigned * epoch_ctr,
+                       const BatchLoop * loops)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned s_next;
+  const unsigned epoch = *epoch_ctr + 1u;
+  const unsigned claimer = blockDim.x - 1;
+  if (threadIdx.x == claimer) s_next = atomicAdd(ticket, 1u);
+  __syncthreads();
+  for (;;) {
+    const unsigned tk = s_next;
+    __syncthreads();
+    if (tk >= (unsigned)num_tasks) break;
+    if (threadIdx.x == claimer) s_next = atomicAdd(ticket, 1u);
+    const BatchTask bt = tasks[tk];
+    const SweepArgs<T> & A = args[bt.prob];
+    if (!loops[bt.prob].active) {  // uniform across the CTA: the flag changes between launches
+      if (threadIdx.x == 0) {
+        const size_t slot = (size_t)(bt.t.grp * 8 + bt.t.oct) * A.ngroups + bt.t.og;
+        st_release(A.done + ((slot * A.nbz + bt.t.bk) * A.nby + bt.t.bj) * A.nbx + bt.t.bi, epoch);
+      }
+      // the claimer's write of s_next must be ordered before everyone's next
+      // read of it (run_task's barriers do this on the other path)
+      __syncthreads();
+      continue;
+    }
+    run_task<T, DIMS, SCHEME, TX>(A, bt.t, smem_raw, true, epoch);
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(exit_count, 1u) == gridDim.x - 1) {
+      *ticket = 0u;
+      *exit_count = 0u;
+      __threadfence();
+      *epoch_ctr = epoch;
+    }
+  }
+}
+
 // One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
 template <typename T, int DIMS, int SCHEME, int TX>
 __global__ void __launch_bounds__(kMaxSweepThreads) sweep_level_kernel(const SweepArgs<T> A)
@@ -673,6 +718,42 @@ int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads
     constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T, D, S, X>,
+                                                      threads, smem) != cudaSuccess)
+      return 0;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return per_sm * sms;
+  });
+}
+
+doma_status launch_sweep_batch(int dims, int scheme, int tx, int grid, int threads, size_t smem,
+                               const SweepArgs<float> * args, const BatchTask * tasks,
+                               int num_tasks, unsigned * ticket, unsigned * exit_count,
+                               unsigned * epoch, const BatchLoop * loops, cudaStream_t stream)
+{
+  cudaError_t e = dispatch(dims, DOMA_PREC_FP32, scheme, tx, [&](auto, auto dims_c, auto sch_c, auto tx_c) {
+    constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
+    cudaError_t r = cudaFuncSetAttribute(sweep_batch_kernel<float, D, S, X>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (r != cudaSuccess) return r;
+    sweep_batch_kernel<float, D, S, X><<<grid, threads, smem, stream>>>(args, tasks, num_tasks, ticket,
+                                                                       exit_count, epoch, loops);
+    return cudaGetLastError();
+  });
+  DOMA_CUDA_TRY(e);
+  return DOMA_OK;
+}
+
+int sweep_batch_resident_ctas(int dims, int scheme, int tx, int threads, size_t smem)
+{
+  return dispatch(dims, DOMA_PREC_FP32, scheme, tx, [&](auto, auto dims_c, auto sch_c, auto tx_c) {
+    constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
+    if (cudaFuncSetAttribute(sweep_batch_kernel<float, D, S, X>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_batch_kernel<float, D, S, X>,
                                                       threads, smem) != cudaSuccess)
       return 0;
     int dev = 0, sms = 0;

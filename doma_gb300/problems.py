@@ -429,3 +429,17 @@ def square_2d(seed: int = 0, n: int = 32, groups: int = 2, np_: int = 2, na: int
     w = np.full(n, cell)
     return Problem(2, w, w.copy(), np.ones(1), mat.reshape(-1), total, S, src, np_, na,
                    name=f"square2d_n{n}_g{G}_s{seed}")
+
+
+def batch_mix(seed: int = 0, count: int = 256, n_range=(16, 96), groups=(1, 2, 4, 8, 16),
+              k_range=(2, 6)) -> list[Problem]:
+    """Batched-solve workload: `count` independent checkerboard problems, each
+    drawing its mesh n^3 with n ~ U{n_range}, its group count from `groups` and
+    its quadrature (2k polar x 4k azimuthal, np = na = k) with k ~ U{k_range};
+    materials, scattering and source drawn as in `checkerboard`."""
+    r = Rng(seed, "batch_mix")
+    ns = r.integers(count, n_range[0], n_range[1] + 1)
+    gs = r.integers(count, 0, len(groups))
+    ks = r.integers(count, k_range[0], k_range[1] + 1)
+    return [checkerboard(seed * 100003 + i, n=int(ns[i]), groups=int(groups[gs[i]]),
+                         np_=int(ks[i]), na=int(ks[i]), block=8) for i in range(count)]

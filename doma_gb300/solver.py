@@ -111,6 +111,70 @@ class Solver:
                 "kernel_launches": launches.value}
 
 
+class Batch:
+    """Many independent problems solved together (doma_batch_*): every group of
+    every unconverged problem is swept in one persistent launch per iteration.
+    Multigroup iteration in FP32 with FP64 norms; problems share dims/scheme."""
+
+    def __init__(self, problems: list[Problem], options: abi.DomaOptions | None = None, **kw):
+        self.lib = abi.load_library()
+        self.problems = list(problems)
+        kw.setdefault("precision", "fp32")
+        kw.setdefault("iteration", "multigroup")
+        self.options = options if options is not None else make_options(**kw)
+        self._cps = (abi.DomaProblem * len(self.problems))(*[p.to_c() for p in self.problems])
+        h = ctypes.c_void_p()
+        st = self.lib.doma_batch_create(self._cps, len(self.problems), ctypes.byref(self.options),
+                                        ctypes.byref(h))
+        abi.check(st, "doma_batch_create", self.lib)
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.doma_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        abi.check(self.lib.doma_batch_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)),
+                  "doma_batch_set_stream", self.lib)
+
+    def tune(self) -> int:
+        tx = ctypes.c_uint32(0)
+        abi.check(self.lib.doma_batch_tune(self._h, ctypes.byref(tx)), "doma_batch_tune", self.lib)
+        return tx.value
+
+    def solve(self) -> list[Report]:
+        n = len(self.problems)
+        reps = (abi.DomaReport * n)()
+        st = self.lib.doma_batch_solve(self._h, reps, n)
+        abi.check(st, "doma_batch_solve", self.lib, allow=(abi.DOMA_OK, abi.DOMA_NOT_CONVERGED))
+        return [Report(converged=r.status == abi.DOMA_OK, status=r.status,
+                       mg_iterations=r.mg_iterations, si_iterations=r.si_iterations,
+                       updates=r.updates, kernel_launches=r.kernel_launches,
+                       mg_residual=r.mg_residual, si_residual=r.si_residual, solve_ms=r.solve_ms,
+                       si_counts=np.array([r.mg_iterations], dtype=np.uint32)) for r in reps]
+
+    def scalar_flux(self, index: int) -> np.ndarray:
+        p = self.problems[index]
+        out = np.empty((p.num_groups, p.num_cells), dtype=np.float64)
+        abi.check(self.lib.doma_batch_get_scalar_flux(
+            self._h, index, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size),
+            "doma_batch_get_scalar_flux", self.lib)
+        return out
+
+
 def quadrature(num_polar: int, num_azimuthal: int, dims: int = 3):
     """(mu, eta, xi, w, counts) from the library's host quadrature (no GPU needed)."""
     lib = abi.load_library()

@@ -187,6 +187,29 @@ doma_status doma_solver_describe(const doma_solver *solver, uint32_t tile[3],
 
 void doma_solver_destroy(doma_solver *solver);
 
+/* ---- Batched solve: many independent problems, one persistent sweep ----
+ * No counterpart in DOMA (it solves one deck per process).  Every problem is
+ * solved with DOMA_ITER_MULTIGROUP in FP32; each batch iteration sweeps every
+ * group of every unconverged problem in ONE persistent launch (the problems'
+ * tasks merged level by level), then updates all of them in one batched
+ * epilogue; a problem stops when its own relative increment norm is <=
+ * fs_tol (or at fs_max_it).  All problems share dims and scheme. */
+typedef struct doma_batch doma_batch;
+
+doma_status doma_batch_create(const doma_problem *problems, size_t count,
+                              const doma_options *opts, doma_batch **out);
+doma_status doma_batch_set_stream(doma_batch *batch, void *stream);
+/* Time a few batched sweeps with each supported block length (8, 16, 32
+ * cells along x) on this batch and keep the fastest; *tile_x gets it. */
+doma_status doma_batch_tune(doma_batch *batch, uint32_t *tile_x);
+/* Solve every problem; reports[i] (count entries, may be NULL) get each
+ * problem's status, iterations (mg_iterations) and updates.  Returns DOMA_OK
+ * when all converged, else the first failing status. */
+doma_status doma_batch_solve(doma_batch *batch, doma_report *reports, size_t count);
+doma_status doma_batch_get_scalar_flux(doma_batch *batch, size_t index, double *out,
+                                       size_t count);
+void doma_batch_destroy(doma_batch *batch);
+
 /* One FP32 sweep that allocates no memory -- no counterpart in DOMA.
  * For callers that cannot call cudaMalloc (code inside another framework's
  * memory pool or allocator budget, or that must keep its device footprint
