@@ -385,7 +385,27 @@ __global__ void __launch_bounds__(kBlock) batch_finalize_kernel(const BatchSlot 
   }
 }
 
+// End of one batched iteration: count it, clear the active counter for the
+// next one and decide whether the graph's loop goes on.  One thread.
+__global__ void batch_continue_kernel(unsigned * still_active, const int * error, unsigned * iters,
+                                      unsigned max_iters, unsigned long long handle)
+{
+  const unsigned n = *still_active;
+  *still_active = 0u;
+  const unsigned it = ++*iters;
+  const bool more = n > 0u && *error == 0 && it <= max_iters;
+  cudaGraphSetConditional(handle, more ? 1u : 0u);
+}
+
 }  // namespace
+
+doma_status launch_batch_continue(unsigned * still_active, const int * error, unsigned * iters,
+                                  unsigned max_iters, unsigned long long handle, cudaStream_t st)
+{
+  batch_continue_kernel<<<1, 1, 0, st>>>(still_active, error, iters, max_iters, handle);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
 
 doma_status launch_batch_epilogue(const BatchSlot * slots, const int * block_prob, int blocks,
                                   const BatchLoop * loops, int precision, cudaStream_t st)

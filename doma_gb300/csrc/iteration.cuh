@@ -86,6 +86,11 @@ struct BatchSlot {
 
 doma_status launch_batch_epilogue(const BatchSlot * slots, const int * block_prob, int blocks,
                                   const BatchLoop * loops, int precision, cudaStream_t st);
+// Graph-driven batched loop: counts the iteration, resets *still_active and
+// sets the WHILE node's condition (handle) to go on while any problem is
+// active, no sweep wait failed and fewer than max_iters iterations ran.
+doma_status launch_batch_continue(unsigned * still_active, const int * error, unsigned * iters,
+                                  unsigned max_iters, unsigned long long handle, cudaStream_t st);
 doma_status launch_batch_finalize(const BatchSlot * slots, BatchLoop * loops, int count,
                                   double tol, unsigned max_it, unsigned * still_active,
                                   cudaStream_t st);

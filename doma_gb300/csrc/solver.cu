@@ -133,12 +133,6 @@ doma_status upload(doma_solver * s, T ** p, const T * host, size_t count)
   return DOMA_OK;
 }
 
-#define DOMA_TRY(expr)                    \
-  do {                                    \
-    doma_status _s = (expr);              \
-    if (_s != DOMA_OK) return _s;         \
-  } while (0)
-
 doma_status bad(const std::string & msg)
 {
   set_error(msg);
@@ -1125,7 +1119,8 @@ namespace {
 struct BatchCtl {
   unsigned ticket, exit_count, epoch;
   int error;
-  unsigned still_active;
+  unsigned still_active;  // problems still iterating after this iteration
+  unsigned iters;         // batched iterations run (graph loop)
 };
 
 }  // namespace
@@ -1145,6 +1140,9 @@ struct doma_batch {
   BatchCtl * d_ctl = nullptr;
   BatchCtl * h_ctl = nullptr;
   cudaStream_t stream = nullptr, own_stream = nullptr;
+  bool use_graph = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
   std::vector<void *> allocs;
 };
 
@@ -1169,6 +1167,14 @@ void bfree(doma_batch * b, void * p)
       break;
     }
   cudaFree(p);
+}
+
+void drop_batch_graph(doma_batch * b)
+{
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
 }
 
 void sfree(doma_solver * s, void * p)
@@ -1225,6 +1231,7 @@ doma_status build_batch_schedule(doma_batch * b)
         tasks.push_back(BatchTask{sc.tasks[t], (int)p});
     }
   b->num_tasks = (int)tasks.size();
+  drop_batch_graph(b);
   bfree(b, b->d_tasks);
   DOMA_TRY(balloc(b, &b->d_tasks, tasks.size()));
   DOMA_CUDA_TRY(cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(BatchTask),
@@ -1262,9 +1269,64 @@ doma_status batch_init_sources(doma_batch * b)
   return DOMA_OK;
 }
 
+// One batched iteration: the all-problem sweep, every active problem's
+// epilogue, the per-problem loop test.
+doma_status batch_iteration(doma_batch * b, cudaStream_t st)
+{
+  const size_t P = b->solvers.size();
+  DOMA_TRY(launch_sweep_batch(b->dims, b->opts.scheme, b->tx, b->grid, b->threads, b->smem,
+                              b->d_args, b->d_tasks, b->num_tasks, &b->d_ctl->ticket,
+                              &b->d_ctl->exit_count, &b->d_ctl->epoch, b->d_loops, st));
+  DOMA_TRY(launch_batch_epilogue(b->d_slots, b->d_block_prob, b->epi_blocks, b->d_loops,
+                                 DOMA_PREC_FP32, st));
+  DOMA_TRY(launch_batch_finalize(b->d_slots, b->d_loops, (int)P, b->opts.fs_tol,
+                                 b->opts.fs_max_it, &b->d_ctl->still_active, st));
+  return DOMA_OK;
+}
+
+// The whole batched solve as one graph: WHILE(any active) { iteration ;
+// continue }.  Rebuilt whenever the schedule changes (tuning).
+doma_status build_batch_graph(doma_batch * b)
+{
+  drop_batch_graph(b);
+  cudaStream_t c0 = nullptr, c1 = nullptr;
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c1, cudaStreamNonBlocking));
+  auto run = [&]() -> doma_status {
+    DOMA_CUDA_TRY(cudaGraphCreate(&b->graph, 0));
+    cudaGraphConditionalHandle h;
+    DOMA_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, b->graph, 1u, cudaGraphCondAssignDefault));
+    DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c0, b->graph, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t body = nullptr;
+    doma_status st = add_while(c0, h, &body);
+    if (st == DOMA_OK) {
+      DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c1, body, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+      st = batch_iteration(b, c1);
+      if (st == DOMA_OK)
+        st = launch_batch_continue(&b->d_ctl->still_active, &b->d_ctl->error, &b->d_ctl->iters,
+                                   b->opts.fs_max_it + 1u, (unsigned long long)h, c1);
+      cudaGraph_t out = nullptr;
+      DOMA_CUDA_TRY(cudaStreamEndCapture(c1, &out));
+    }
+    cudaGraph_t out = nullptr;
+    DOMA_CUDA_TRY(cudaStreamEndCapture(c0, &out));
+    if (st != DOMA_OK) return st;
+    DOMA_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    return DOMA_OK;
+  };
+  const doma_status st = run();
+  cudaStreamDestroy(c0);
+  cudaStreamDestroy(c1);
+  if (st != DOMA_OK) drop_batch_graph(b);
+  return st;
+}
+
 void batch_release(doma_batch * b)
 {
   if (!b) return;
+  drop_batch_graph(b);
   for (auto * s : b->solvers) release(s);
   for (void * p : b->allocs) cudaFree(p);
   if (b->h_ctl) cudaFreeHost(b->h_ctl);
@@ -1316,6 +1378,10 @@ doma_status doma_batch_create(const doma_problem * problems, size_t count, const
   if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(DOMA_CUDA_ERROR);
   b->stream = b->own_stream;
+  {
+    const char * env = std::getenv("DOMA_SOLVE_LOOP");
+    b->use_graph = !(env && std::string(env) == "host");
+  }
   // batched epilogue layout: up to 64 blocks per problem, contiguous
   std::vector<BatchSlot> slots(P);
   std::vector<int> block_prob;
@@ -1386,23 +1452,29 @@ doma_status doma_batch_solve(doma_batch * b, doma_report * reports, size_t count
   const auto t0 = std::chrono::steady_clock::now();
   const size_t P = b->solvers.size();
   DOMA_TRY(batch_init_sources(b));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, 2 * sizeof(unsigned), b->stream));
   unsigned iters = 0;
-  for (;;) {
-    DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, sizeof(unsigned), b->stream));
-    DOMA_TRY(batch_sweep(b));
-    DOMA_TRY(launch_batch_epilogue(b->d_slots, b->d_block_prob, b->epi_blocks, b->d_loops,
-                                   DOMA_PREC_FP32, b->stream));
-    DOMA_TRY(launch_batch_finalize(b->d_slots, b->d_loops, (int)P, b->opts.fs_tol,
-                                   b->opts.fs_max_it, &b->d_ctl->still_active, b->stream));
+  if (b->use_graph) {
+    if (!b->exec) DOMA_TRY(build_batch_graph(b));
+    DOMA_CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
     DOMA_CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
                                   b->stream));
     DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
-    ++iters;
-    if (b->h_ctl->error) {
-      set_error("a batched sweep wait for an upstream block timed out");
-      return DOMA_DEVICE_WAIT_TIMEOUT;
+    iters = b->h_ctl->iters;
+  } else {
+    for (;;) {
+      DOMA_TRY(batch_iteration(b, b->stream));
+      DOMA_CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
+                                    b->stream));
+      DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
+      ++iters;
+      if (b->h_ctl->error || b->h_ctl->still_active == 0 || iters > b->opts.fs_max_it) break;
+      DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, sizeof(unsigned), b->stream));
     }
-    if (b->h_ctl->still_active == 0 || iters > b->opts.fs_max_it) break;
+  }
+  if (b->h_ctl->error) {
+    set_error("a batched sweep wait for an upstream block timed out");
+    return DOMA_DEVICE_WAIT_TIMEOUT;
   }
   std::vector<BatchLoop> loops(P);
   DOMA_CUDA_TRY(cudaMemcpy(loops.data(), b->d_loops, P * sizeof(BatchLoop), cudaMemcpyDeviceToHost));
@@ -1418,7 +1490,7 @@ doma_status doma_batch_solve(doma_batch * b, doma_report * reports, size_t count
       r.mg_iterations = loops[p].it;
       r.si_iterations = (uint64_t)loops[p].it * s->G;
       r.updates = (uint64_t)loops[p].it * s->G * s->N * (uint64_t)s->D;
-      r.kernel_launches = 3ull * iters;
+      r.kernel_launches = (b->use_graph ? 4ull : 3ull) * iters;
       r.mg_residual = loops[p].res;
       r.si_residual = loops[p].res;
       r.solve_ms = ms;

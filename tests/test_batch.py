@@ -60,3 +60,32 @@ def test_batch_tuner_keeps_results():
         c = [b.scalar_flux(i) for i in range(len(ps))]
     assert first == second
     assert all(np.array_equal(x, y) for x, y in zip(a, c))
+
+
+@pytest.mark.gpu
+def test_batch_graph_loop_equals_host_loop(monkeypatch):
+    """The captured WHILE loop and the host-driven loop run the same kernels."""
+    from doma_gb300.solver import Batch
+    ps = small_batch()
+    kw = dict(scheme="tw_dd", theta=0.7, precision="fp32", fs_tol=1e-6, fs_max_it=3000,
+              iteration="multigroup")
+    with Batch(ps, **kw) as b:
+        graph_reps = b.solve()
+        graph_phi = [b.scalar_flux(i) for i in range(len(ps))]
+    monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    with Batch(ps, **kw) as b:
+        host_reps = b.solve()
+        host_phi = [b.scalar_flux(i) for i in range(len(ps))]
+    assert [r.mg_iterations for r in graph_reps] == [r.mg_iterations for r in host_reps]
+    assert graph_reps[0].kernel_launches == 4 * max(r.mg_iterations for r in graph_reps)
+    assert all(np.array_equal(x, y) for x, y in zip(graph_phi, host_phi))
+
+
+@pytest.mark.gpu
+def test_batch_iteration_cap_reports_not_converged():
+    from doma_gb300.solver import Batch
+    ps = small_batch()[:2]
+    with Batch(ps, scheme="dd", precision="fp32", fs_tol=1e-12, fs_max_it=5,
+               iteration="multigroup") as b:
+        reps = b.solve()
+    assert all(not r.converged and r.mg_iterations == 5 for r in reps)
