@@ -43,6 +43,7 @@ ABI_VERSION = 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _u32p = ctypes.POINTER(ctypes.c_uint32)
+_fp = ctypes.POINTER(ctypes.c_float)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 
 
@@ -140,6 +141,23 @@ SIGNATURES = {
         [ctypes.POINTER(DomaProblem), ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     ),
+    "doma_unet_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    "doma_unet_destroy": (None, [ctypes.c_void_p]),
+    "doma_unet_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "doma_unet_num_params": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "doma_unet_get_params": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_size_t]),
+    "doma_unet_set_params": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_size_t]),
+    "doma_unet_get_grads": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_size_t]),
+    "doma_unet_forward": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 4,
+    ),
+    "doma_unet_backward": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 4,
+    ),
+    "doma_unet_last_loss": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "doma_unet_adam": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_float] * 4),
 }
 
 _LIB = None

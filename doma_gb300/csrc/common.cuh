@@ -29,6 +29,12 @@ const char * get_error();
     }                                                                                          \
   } while (0)
 
+#define DOMA_TRY(expr)                    \
+  do {                                    \
+    doma_status _s = (expr);              \
+    if (_s != DOMA_OK) return _s;         \
+  } while (0)
+
 // Ordinates of one octant handled by one sweep task (two per warp).
 constexpr int kGroup = 16;
 

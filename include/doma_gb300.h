@@ -231,6 +231,36 @@ doma_status doma_sweep_noalloc(const doma_problem *problem, uint32_t scheme, dou
                                const float *q, const float *sigma_t, double *phi_out,
                                void *stream);
 
+/* ---- Learned source-iteration accelerator -- no counterpart in DOMA ------
+ * doma_unet: a 3D convolutional U-Net (4 levels, 32/64/128/256 channels,
+ * 3x3x3 convolutions, average pooling down, nearest upsampling with additive
+ * skips up, a linear 1-channel FP32 head) with BF16 weights and activations
+ * and FP32 accumulation, run and trained by this library's kernels.
+ * Tensors are device memory, channels-last: input [batch][nz][ny][nx][16]
+ * bf16 (channels beyond those used must be zero), output and target
+ * [batch][nz][ny][nx] float.  nz, ny, nx must be multiples of 8.
+ * Parameters are one flat FP32 array: per convolution (14, encoder then
+ * decoder) weights [27][cout][cin] then biases [cout]; then the head's
+ * weights [32] and bias [1].  Tap index = (dz+1)*9 + (dy+1)*3 + (dx+1). */
+typedef struct doma_unet doma_unet;
+#define DOMA_UNET_IN_CHANNELS 16u
+doma_status doma_unet_create(uint64_t seed, doma_unet **out);
+void doma_unet_destroy(doma_unet *net);
+doma_status doma_unet_set_stream(doma_unet *net, void *stream);
+size_t doma_unet_num_params(const doma_unet *net);
+doma_status doma_unet_get_params(doma_unet *net, float *out, size_t count);
+doma_status doma_unet_set_params(doma_unet *net, const float *in, size_t count);
+doma_status doma_unet_get_grads(doma_unet *net, float *out, size_t count);
+doma_status doma_unet_forward(doma_unet *net, const void *input, float *output, uint32_t batch,
+                              uint32_t nz, uint32_t ny, uint32_t nx);
+/* Forward pass, mean-square loss against target, and the gradient of that
+ * loss for every parameter (read with doma_unet_get_grads). */
+doma_status doma_unet_backward(doma_unet *net, const void *input, const float *target,
+                               uint32_t batch, uint32_t nz, uint32_t ny, uint32_t nx);
+doma_status doma_unet_last_loss(doma_unet *net, double *loss);
+/* One Adam step (bias-corrected) with the last gradients. */
+doma_status doma_unet_adam(doma_unet *net, float lr, float beta1, float beta2, float eps);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif
