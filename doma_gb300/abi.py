@@ -39,6 +39,9 @@ DOMA_PREC_FP64 = 0
 DOMA_PREC_FP32 = 1
 DOMA_ITER_GAUSS_SEIDEL = 0
 DOMA_ITER_MULTIGROUP = 1
+DOMA_CONV_AUTO = 0
+DOMA_CONV_MMA = 1
+DOMA_CONV_TENSOR_MEMORY = 2
 ABI_VERSION = 2
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -104,6 +107,17 @@ class DomaReport(ctypes.Structure):
 
 
 # Every entry point declared in include/doma_gb300.h: name -> (restype, argtypes).
+class DomaAccelOptions(ctypes.Structure):
+    _fields_ = [("first", ctypes.c_uint32), ("interval", ctypes.c_uint32),
+                ("max_corrections", ctypes.c_uint32), ("guard", ctypes.c_uint32)]
+
+
+class DomaAccelStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_uint32), ("corrections_accepted", ctypes.c_uint32),
+                ("corrections_rejected", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("error", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+
+
 SIGNATURES = {
     "doma_default_options": (None, [ctypes.POINTER(DomaOptions)]),
     "doma_last_error": (ctypes.c_char_p, []),
@@ -141,6 +155,19 @@ SIGNATURES = {
         [ctypes.POINTER(DomaProblem), ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     ),
+    "doma_batch_begin": (ctypes.c_int, [ctypes.c_void_p]),
+    "doma_batch_iterate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p]),
+    "doma_batch_state": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p),
+         ctypes.POINTER(ctypes.c_void_p)],
+    ),
+    "doma_batch_reports": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport), ctypes.c_size_t]),
+    "doma_solver_set_accelerator": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(DomaAccelOptions)]),
+    "doma_solver_set_reference": (
+        ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_size_t, ctypes.c_double]),
+    "doma_solver_accel_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaAccelStats)]),
     "doma_unet_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
     "doma_unet_destroy": (None, [ctypes.c_void_p]),
     "doma_unet_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -158,6 +185,14 @@ SIGNATURES = {
     ),
     "doma_unet_last_loss": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "doma_unet_adam": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_float] * 4),
+    "doma_conv3_forward": (
+        ctypes.c_int,
+        [ctypes.c_void_p] + [ctypes.c_uint32] * 5 + [ctypes.c_void_p, ctypes.c_void_p,
+                                                      ctypes.c_uint32, ctypes.c_uint32,
+                                                      ctypes.c_void_p, ctypes.c_uint32,
+                                                      ctypes.c_void_p],
+    ),
+    "doma_conv_wait_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
 }
 
 _LIB = None

@@ -27,7 +27,7 @@ LIB = OUT / "libdoma_gb300.so"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["sweep.cu", "iteration.cu", "solver.cu", "noalloc.cu", "conv.cu", "unet.cu"]
+CU_SOURCES = ["sweep.cu", "iteration.cu", "solver.cu", "noalloc.cu", "conv.cu", "conv_tc.cu", "unet.cu", "accel.cu"]
 CPP_SOURCES = ["quadrature.cpp"]
 
 # C++ drop-in layer (DOMA's TransportSolver3D/2D, BrickMesh3D/2D and

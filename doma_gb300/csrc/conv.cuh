@@ -25,6 +25,19 @@ doma_status conv3_forward(const ConvShape & s, const __nv_bfloat16 * x, int cin,
                           const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
                           __nv_bfloat16 * y, cudaStream_t st);
 
+// The tensor-memory (tcgen05 + TMA) variant of conv3_forward (conv_tc.cu),
+// for shapes whose 128-voxel boxes tile the volume exactly; conv3_forward
+// uses it for those unless DOMA_CONV_PATH=mma.  conv3_tc_error reads the
+// flag its bounded waits set when one gave up.
+bool conv3_tc_supported(const ConvShape & s, int cin, int cout);
+doma_status conv3_forward_tc(const ConvShape & s, const __nv_bfloat16 * x, int cin,
+                             const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
+                             __nv_bfloat16 * y, cudaStream_t st);
+doma_status conv3_forward_mma(const ConvShape & s, const __nv_bfloat16 * x, int cin,
+                              const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
+                              __nv_bfloat16 * y, cudaStream_t st);
+doma_status conv3_tc_error(int * flag);
+
 // Weight gradient: dw[tap][cout][cin] = sum over voxels m of
 // dz[m][cout] * x[m + offset(tap)][cin], reduced over voxel splits in a fixed
 // order (deterministic).  partial: scratch of conv3_wgrad_scratch() floats.

@@ -1,0 +1,461 @@
+// conv_tc.cu -- the 3x3x3 BF16 convolution on the 5th-generation tensor
+// cores: tcgen05.mma with the FP32 accumulator in tensor memory, operands
+// staged by TMA.
+//
+// One CTA computes a 128-voxel x cout tile (M = 128, N = cout <= 256) of
+// y = act(conv(x, w) + b).  The reduction runs over 27 taps x input-channel
+// chunks of KC (64, 32 or 16 channels = one 128/64/32-byte swizzle row):
+//   * A, the shifted input tile of one (tap, chunk) step, is one TMA load of
+//     a 5D box {KC channels, bx, by, bz, bb} of the channels-last tensor at
+//     the tile origin plus the tap's offset.  Boxes that reach outside the
+//     volume are zero-filled by TMA -- that is the convolution's padding.
+//     The box lands as 128 rows (voxels, x fastest) of KC channels in the
+//     swizzled K-major layout the MMA reads.
+//   * B, the tap's weight slab w[tap][n0 .. n0+N][chunk], is a 2D TMA load.
+//   * KC / 16 tcgen05.mma (kind::f16, M=128, N, K=16) per step accumulate
+//     into N TMEM columns; each step's commit releases its smem stage.
+// Warp roles: warp 0 issues TMA, warp 1 owns TMEM and issues the MMAs, warps
+// 2-5 (one per TMEM lane quarter) drain the accumulator: tcgen05.ld, bias,
+// ReLU, bf16 pack, store.  Every mbarrier wait is bounded; a wait that gives
+// up sets an error flag (read by conv3_tc_error) and the CTA still releases
+// its tensor memory before it exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "conv.cuh"
+
+namespace doma {
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+__device__ int g_tc_error = 0;
+
+constexpr int kThreads = 192;
+constexpr int kSmemBudget = 100 * 1024;  // two CTAs per SM
+
+__device__ __forceinline__ uint32_t saddr(const void * p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t * bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t * bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t * bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the completion of phase `parity`; false after about a
+// second of polling (then the error flag is set).
+__device__ bool mbar_wait(uint64_t * bar, uint32_t parity)
+{
+  for (uint32_t i = 0; i < (1u << 24); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i >= 64) __nanosleep(64);
+  }
+  atomicExch(&g_tc_error, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_5d(void * dst, const CUtensorMap * map, uint64_t * bar,
+                                            int c0, int c1, int c2, int c3, int c4)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5, %6, %7}], [%2];" ::"r"(saddr(dst)),
+      "l"(map), "r"(saddr(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void * dst, const CUtensorMap * map, uint64_t * bar,
+                                            int c0, int c1)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4}], [%2];" ::"r"(saddr(dst)),
+      "l"(map), "r"(saddr(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major swizzled tile: start address,
+// leading byte offset 16 (unused by swizzled K-major layouts), stride byte
+// offset between 8-row groups, descriptor version 1, swizzle mode.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo, uint32_t mode)
+{
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)mode << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate)
+{
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t * bar)
+{
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          saddr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TcArgs {
+  const float * bias;
+  bf16 * y;
+  int nz, ny, nx;             // volume extents
+  int bx, by, bz, bb;         // voxel box of one tile (bx*by*bz*bb = 128)
+  int tx, ty, tz;             // tiles per axis
+  int cin, cout;
+};
+
+template <int N, int KC, bool RELU>
+__global__ void __launch_bounds__(kThreads, 1)
+    conv3_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    const TcArgs a)
+{
+  constexpr int BM = 128;
+  constexpr int A_BYTES = BM * KC * 2, B_BYTES = N * KC * 2, STAGE = A_BYTES + B_BYTES;
+  constexpr int STAGES = std::max(2, std::min(8, kSmemBudget / STAGE));
+  constexpr uint32_t SW = KC * 2;                       // swizzle span in bytes
+  constexpr uint32_t MODE = KC == 64 ? 2u : (KC == 32 ? 4u : 6u);  // 128B / 64B / 32B
+  constexpr uint32_t SBO = 8 * SW;
+  constexpr uint32_t TMEM_COLS = N;
+  constexpr uint32_t IDESC = idesc_bf16(BM, N);
+  static_assert(N >= 32 && N <= 256 && (N & (N - 1)) == 0, "N");
+  static_assert(A_BYTES % 1024 == 0 && B_BYTES % 1024 == 0, "tile alignment");
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t * smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+  uint64_t * full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE);
+  uint64_t * empty = full + STAGES;
+  uint64_t * tmem_full = empty + STAGES;
+  uint32_t * tmem_slot = reinterpret_cast<uint32_t *>(tmem_full + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0 && lane == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(tmem_full, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __shared__ int s_issued, s_consumed;
+  if (threadIdx.x == 0) s_issued = s_consumed = 0;
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  // tile origin
+  int t = blockIdx.x;
+  const int x0 = (t % a.tx) * a.bx;
+  t /= a.tx;
+  const int y0 = (t % a.ty) * a.by;
+  t /= a.ty;
+  const int z0 = (t % a.tz) * a.bz;
+  const int b0 = (t / a.tz) * a.bb;
+  const int steps_per_tap = a.cin / KC;
+  const int k_steps = 27 * steps_per_tap;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(&tmA) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(&tmB) : "memory");
+      int ks = 0;
+      for (; ks < k_steps; ++ks) {
+        const int s = ks % STAGES;
+        const uint32_t use = (uint32_t)(ks / STAGES);
+        if (ks >= STAGES && !mbar_wait(empty + s, (use & 1u) ^ 1u)) break;
+        const int tap = ks / steps_per_tap, c0 = (ks % steps_per_tap) * KC;
+        const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+        uint8_t * As = smem + s * STAGE;
+        mbar_expect_tx(full + s, (uint32_t)STAGE);
+        tma_load_5d(As, &tmA, full + s, c0, x0 + dx, y0 + dy, z0 + dz, b0);
+        tma_load_2d(As + A_BYTES, &tmB, full + s, c0, tap * a.cout + (int)blockIdx.y * N);
+      }
+      s_issued = ks;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int ks = 0;
+      for (; ks < k_steps; ++ks) {
+        const int s = ks % STAGES;
+        const uint32_t use = (uint32_t)(ks / STAGES);
+        if (!mbar_wait(full + s, use & 1u)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a_addr = saddr(smem + s * STAGE);
+        const uint32_t b_addr = a_addr + A_BYTES;
+#pragma unroll
+        for (int k = 0; k < KC / 16; ++k) {
+          const uint64_t ad = smem_desc(a_addr + k * 32, SBO, MODE);
+          const uint64_t bd = smem_desc(b_addr + k * 32, SBO, MODE);
+          umma_bf16(tmem, ad, bd, IDESC, (ks | k) != 0 ? 1u : 0u);
+        }
+        umma_commit(empty + s);
+      }
+      s_consumed = ks;
+      umma_commit(tmem_full);  // also after a failed wait, so the epilogue is released
+    }
+  } else {
+    // epilogue: warps 2..5 cover TMEM lane quarters 2, 3, 0, 1
+    const int q = warp & 3;
+    int ok = 0;
+    if (lane == 0) ok = mbar_wait(tmem_full, 0) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int row = q * 32 + lane;
+    int r = row;
+    const int x = r % a.bx;
+    r /= a.bx;
+    const int yy = r % a.by;
+    r /= a.by;
+    const int zz = r % a.bz;
+    const int bb = r / a.bz;
+    const long long vox =
+        (((long long)(b0 + bb) * a.nz + (z0 + zz)) * a.ny + (y0 + yy)) * a.nx + (x0 + x);
+    bf16 * out = a.y + vox * a.cout + (int)blockIdx.y * N;
+    const float * bias = a.bias ? a.bias + (int)blockIdx.y * N : nullptr;
+#pragma unroll 1
+    for (int c0 = 0; ok && c0 < N; c0 += 32) {
+      uint32_t v[32];
+      tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+      uint4 pk[4];
+      uint32_t * pw = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+        if (bias) {
+          f0 += __ldg(bias + c0 + 2 * j);
+          f1 += __ldg(bias + c0 + 2 * j + 1);
+        }
+        if (RELU) {
+          f0 = fmaxf(f0, 0.0f);
+          f1 = fmaxf(f1, 0.0f);
+        }
+        const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+        pw[j] = *reinterpret_cast<const uint32_t *>(&h);
+      }
+      uint4 * dst = reinterpret_cast<uint4 *>(out + c0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dst[j] = pk[j];
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  // Teardown after a failed wait: let this CTA's own copies and MMAs in
+  // flight land (bounded) before its shared and tensor memory go away.
+  if (threadIdx.x == 0)
+    for (int i = s_consumed; i < s_issued; ++i)
+      mbar_wait(full + i % STAGES, (uint32_t)(i / STAGES) & 1u);
+  if (threadIdx.x == 32) mbar_wait(tmem_full, 0);
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encoder()
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void * p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+CUtensorMapSwizzle swizzle_for(int kc)
+{
+  return kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B
+                  : (kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B);
+}
+
+template <int N, int KC, bool RELU>
+doma_status launch_tc(const CUtensorMap & ma, const CUtensorMap & mb, const TcArgs & a, int tiles,
+                      cudaStream_t st)
+{
+  constexpr int STAGE = 128 * KC * 2 + N * KC * 2;
+  constexpr int STAGES = std::max(2, std::min(8, kSmemBudget / STAGE));
+  constexpr int smem = STAGES * STAGE + 1024 + (2 * STAGES + 2) * 8;
+  static bool configured = false;
+  if (!configured) {
+    DOMA_CUDA_TRY(cudaFuncSetAttribute(conv3_tc_kernel<N, KC, RELU>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = true;
+  }
+  conv3_tc_kernel<N, KC, RELU><<<dim3((unsigned)tiles, (unsigned)(a.cout / N)), kThreads, smem, st>>>(
+      ma, mb, a);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+template <int N, int KC>
+doma_status launch_tc_act(const CUtensorMap & ma, const CUtensorMap & mb, const TcArgs & a,
+                          int tiles, bool relu, cudaStream_t st)
+{
+  return relu ? launch_tc<N, KC, true>(ma, mb, a, tiles, st)
+              : launch_tc<N, KC, false>(ma, mb, a, tiles, st);
+}
+
+template <int KC>
+doma_status dispatch_n(const CUtensorMap & ma, const CUtensorMap & mb, const TcArgs & a, int tiles,
+                       bool relu, cudaStream_t st)
+{
+  switch (a.cout) {
+    case 32: return launch_tc_act<32, KC>(ma, mb, a, tiles, relu, st);
+    case 64: return launch_tc_act<64, KC>(ma, mb, a, tiles, relu, st);
+    case 128: return launch_tc_act<128, KC>(ma, mb, a, tiles, relu, st);
+    default: return launch_tc_act<256, KC>(ma, mb, a, tiles, relu, st);
+  }
+}
+
+}  // namespace
+
+bool conv3_tc_supported(const ConvShape & s, int cin, int cout)
+{
+  if (!(cin == 16 || cin == 32 || cin % 64 == 0) || cin > 256) return false;
+  if (!(cout == 32 || cout == 64 || cout == 128 || cout == 256)) return false;
+  if (s.voxels() % 128 != 0) return false;
+  // the 128-voxel box must tile the volume exactly
+  const int bx = std::min(s.nx, 128);
+  if (s.nx % bx) return false;
+  const int by = std::min(s.ny, 128 / bx);
+  if (s.ny % by || (128 / bx) % by) return false;
+  const int bz = std::min(s.nz, 128 / (bx * by));
+  if (s.nz % bz || (128 / (bx * by)) % bz) return false;
+  const int bb = 128 / (bx * by * bz);
+  if (bx * by * bz * bb != 128 || s.batch % bb) return false;
+  return encoder() != nullptr;
+}
+
+doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const bf16 * w,
+                             const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st)
+{
+  if (!conv3_tc_supported(s, cin, cout)) {
+    set_error("conv3_forward_tc: shape not supported by the tensor-memory kernel");
+    return DOMA_BAD_INPUT;
+  }
+  const int kc = cin >= 64 ? 64 : cin;
+  TcArgs a{};
+  a.bias = bias;
+  a.y = y;
+  a.nz = s.nz;
+  a.ny = s.ny;
+  a.nx = s.nx;
+  a.bx = std::min(s.nx, 128);
+  a.by = std::min(s.ny, 128 / a.bx);
+  a.bz = std::min(s.nz, 128 / (a.bx * a.by));
+  a.bb = 128 / (a.bx * a.by * a.bz);
+  a.tx = s.nx / a.bx;
+  a.ty = s.ny / a.by;
+  a.tz = s.nz / a.bz;
+  a.cin = cin;
+  a.cout = cout;
+  const int tiles = a.tx * a.ty * a.tz * (s.batch / a.bb);
+
+  CUtensorMap ma, mb;
+  const cuuint64_t gdim_a[5] = {(cuuint64_t)cin, (cuuint64_t)s.nx, (cuuint64_t)s.ny,
+                                (cuuint64_t)s.nz, (cuuint64_t)s.batch};
+  const cuuint64_t row = (cuuint64_t)cin * 2;
+  const cuuint64_t gstr_a[4] = {row, row * s.nx, row * s.nx * s.ny, row * s.nx * s.ny * s.nz};
+  const cuuint32_t box_a[5] = {(cuuint32_t)kc, (cuuint32_t)a.bx, (cuuint32_t)a.by,
+                               (cuuint32_t)a.bz, (cuuint32_t)a.bb};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUresult r = encoder()(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x), gdim_a,
+                         gstr_a, box_a, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(kc),
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (activations) failed: " + std::to_string((int)r));
+    return DOMA_CUDA_ERROR;
+  }
+  const cuuint64_t gdim_b[2] = {(cuuint64_t)cin, (cuuint64_t)27 * cout};
+  const cuuint64_t gstr_b[1] = {row};
+  const cuuint32_t box_b[2] = {(cuuint32_t)kc, (cuuint32_t)cout};
+  r = encoder()(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(w), gdim_b, gstr_b,
+                box_b, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(kc),
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled (weights) failed: " + std::to_string((int)r));
+    return DOMA_CUDA_ERROR;
+  }
+  if (kc == 64) return dispatch_n<64>(ma, mb, a, tiles, relu, st);
+  if (kc == 32) return dispatch_n<32>(ma, mb, a, tiles, relu, st);
+  return dispatch_n<16>(ma, mb, a, tiles, relu, st);
+}
+
+doma_status conv3_tc_error(int * flag)
+{
+  DOMA_CUDA_TRY(cudaMemcpyFromSymbol(flag, g_tc_error, sizeof(int)));
+  return DOMA_OK;
+}
+
+}  // namespace doma

@@ -275,6 +275,7 @@ __device__ __forceinline__ void mgi_cell(const IterArgs & A, size_t c, T * q, do
     }
     double * ph = A.phi + (size_t)g * N + c;
     const double t = dA(*ph, d);
+    if (A.corr) d = dA(d, -(double)A.corr[(size_t)g * N + c]);
     diff = dA(diff, dM(dM(d, d), V));
     tot = dA(tot, dM(dM(t, t), V));
     *ph = t;

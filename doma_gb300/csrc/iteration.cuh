@@ -29,6 +29,10 @@ struct IterArgs {
   const double * octphi = nullptr;    // fp32: [8 * ngroups][N]
   double * partials = nullptr;        // [grid][2]
   unsigned * ticket = nullptr;        // last-block ticket (kept at 0 between launches)
+  // Multigroup mode, the iteration after a learned correction Delta ([G][N]):
+  // the sweep's result minus Delta is the increment from the corrected
+  // iterate (the flux itself takes the full sweep result).  Null otherwise.
+  const float * corr = nullptr;
 };
 
 // Device-side solve state (one per solver, in device memory; mirrored in

@@ -28,8 +28,10 @@
 #include <string>
 #include <vector>
 
+#include "accel.cuh"
 #include "common.cuh"
 #include "iteration.cuh"
+#include "unet.cuh"
 
 namespace doma {
 
@@ -103,6 +105,21 @@ struct doma_solver {
   SweepArgs<float> a32{};
   IterArgs it{};
   std::vector<void *> allocations;
+
+  // learned accelerator and reference-error stop (multigroup mode)
+  doma_unet * accel = nullptr;
+  doma_accel_options accel_opts{};
+  float *d_fsig = nullptr, *d_fabs = nullptr, *d_kappa = nullptr;   // [G][N]
+  float *d_corr = nullptr;                                            // [G][N]
+  float *d_r = nullptr, *d_ya = nullptr, *d_yb = nullptr, *d_nn_out = nullptr;  // [N]
+  void * d_nn_in = nullptr;                                           // [N][16] bf16
+  double * d_rms = nullptr;                                           // [G]
+  double *d_phi_save = nullptr, *d_delta_save = nullptr;              // [G][N]
+  double * d_acc_partials = nullptr;                                  // [grid]
+  unsigned * d_acc_ticket = nullptr;
+  double * d_ref = nullptr;                                           // [G][N]
+  double ref_norm2 = 0.0, ref_target = 0.0;
+  doma_accel_stats stats{};
 };
 
 namespace {
@@ -870,8 +887,144 @@ doma_status solve_multigroup(doma_solver * s, doma_report * r)
   return status;
 }
 
+// ---- guided multigroup solve: learned corrections and/or a reference stop --
+
+// Network corrections for every group in order (y chain), then the next
+// sweep's source from delta + Delta.
+doma_status accel_correction(doma_solver * s, cudaStream_t st)
+{
+  const size_t N = s->N;
+  float * y_prev = nullptr;
+  float * ya = s->d_ya;
+  float * yb = s->d_yb;
+  for (int g = 0; g < s->G; ++g) {
+    DOMA_TRY(accel_residual(s->it, g, s->d_dscratch, s->d_kappa, y_prev, s->d_r, s->d_acc_partials,
+                            s->d_acc_ticket, s->d_rms + g, st));
+    DOMA_TRY(accel_input(N, g, s->d_r, s->d_rms + g, s->d_fsig, s->d_fabs,
+                         static_cast<__nv_bfloat16 *>(s->d_nn_in), st));
+    DOMA_TRY(unet_forward(s->accel, static_cast<const __nv_bfloat16 *>(s->d_nn_in), s->d_nn_out, 1,
+                          s->nz, s->ny, s->nx, st));
+    DOMA_TRY(accel_correct(N, g, s->d_nn_out, s->d_rms + g, s->d_r, s->d_kappa, y_prev, s->d_corr,
+                           ya, st));
+    y_prev = ya;
+    std::swap(ya, yb);
+  }
+  return accel_source(s->it, s->opts.precision, s->d_dscratch, s->d_corr, s->d_q, st);
+}
+
+// Host-driven multigroup loop.  After iteration `first` and then every
+// `interval` iterations the network proposes a correction; the iteration
+// that follows is swept from it, and with the guard on a correction after
+// which the relative increment norm rose is undone (flux, increment and
+// source restored; that sweep is spent).  With a reference flux the loop
+// stops on the relative L2 error against it instead of the increment norm.
+doma_status solve_multigroup_guided(doma_solver * s, doma_report * r)
+{
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t G = s->G, N = s->N;
+  const size_t bytes = G * N * sizeof(double);
+  const doma_options & o = s->opts;
+  cudaStream_t st = s->stream;
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, bytes, st));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), st));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_ctl->norms, 0, sizeof(s->d_ctl->norms), st));
+  DOMA_TRY(launch_mgi_init(s->it, o.precision, s->d_q, s->d_sigt, st));
+  const bool use_ref = s->d_ref != nullptr;
+  const doma_accel_options A = s->accel_opts;
+  uint64_t launches = 1;
+  unsigned iters = 0, tries = 0, next_try = std::max(1u, A.first);
+  unsigned accepted = 0, rejected = 0;
+  double res = 0.0, err = -1.0, res_before = 0.0, err_before = -1.0;
+  bool pending = false;
+  doma_status status = DOMA_OK;
+  for (;;) {
+    s->it.corr = pending ? s->d_corr : nullptr;
+    const doma_status ist = mgi_iteration(s, LoopParams{}, st);
+    s->it.corr = nullptr;
+    DOMA_TRY(ist);
+    launches += 2;
+    if (use_ref) {
+      DOMA_TRY(ref_error(s->it, s->d_ref, s->d_acc_partials, s->d_acc_ticket, &s->d_ctl->norms[2], st));
+      ++launches;
+    }
+    double diff, tot;
+    DOMA_TRY(read_norms(s, 0, &diff, &tot));
+    const double e2 = s->h_ctl->norms[2];
+    ++iters;
+    if (!std::isfinite(diff) || !std::isfinite(tot) || !std::isfinite(e2)) {
+      status = DOMA_NUMERIC_ERROR;
+      break;
+    }
+    res = ratio(diff, tot);
+    if (use_ref) err = std::sqrt(e2 / s->ref_norm2);
+    if (pending) {
+      pending = false;
+      const bool reached = use_ref && err <= s->ref_target;
+      if (!reached && A.guard && res > res_before) {
+        DOMA_CUDA_TRY(cudaMemcpyAsync(s->d_phi, s->d_phi_save, bytes, cudaMemcpyDeviceToDevice, st));
+        DOMA_CUDA_TRY(cudaMemcpyAsync(s->d_dscratch, s->d_delta_save, bytes,
+                                      cudaMemcpyDeviceToDevice, st));
+        DOMA_TRY(accel_source(s->it, o.precision, s->d_dscratch, nullptr, s->d_q, st));
+        ++launches;
+        ++rejected;
+        res = res_before;
+        err = err_before;
+      } else {
+        ++accepted;
+      }
+    }
+    if (use_ref ? err <= s->ref_target : !(o.fs_tol < res)) break;
+    if (iters >= o.fs_max_it) {
+      status = DOMA_NOT_CONVERGED;
+      break;
+    }
+    if (s->accel && tries < A.max_corrections && iters >= next_try) {
+      DOMA_CUDA_TRY(cudaMemcpyAsync(s->d_phi_save, s->d_phi, bytes, cudaMemcpyDeviceToDevice, st));
+      DOMA_CUDA_TRY(cudaMemcpyAsync(s->d_delta_save, s->d_dscratch, bytes,
+                                    cudaMemcpyDeviceToDevice, st));
+      DOMA_TRY(accel_correction(s, st));
+      launches += 1 + 4 * G;
+      pending = true;
+      res_before = res;
+      err_before = err;
+      ++tries;
+      next_try = iters + 1 + A.interval;
+    }
+  }
+  DOMA_CUDA_TRY(cudaStreamSynchronize(st));
+  if (status == DOMA_NOT_CONVERGED) set_error("the guided multigroup solve reached fs_max_it");
+  else if (status == DOMA_NUMERIC_ERROR) set_error("a residual norm is not finite");
+  s->launches += launches;
+  const auto t1 = std::chrono::steady_clock::now();
+  const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s->stats.iterations = iters;
+  s->stats.corrections_accepted = accepted;
+  s->stats.corrections_rejected = rejected;
+  s->stats.error = err;
+  s->stats.solve_ms = ms;
+  if (o.verbose)
+    std::printf("Guided multigroup iteration %s after %u iterations (%u corrections kept, %u undone), "
+                "residual %g, error %g\n",
+                status == DOMA_OK ? "converged" : "failed to converge", iters, accepted, rejected, res,
+                err);
+  if (r) {
+    r->status = status;
+    r->mg_iterations = iters;
+    r->si_iterations = (uint64_t)iters * G;
+    r->updates = (uint64_t)iters * G * N * (uint64_t)s->D;
+    r->kernel_launches = launches;
+    r->mg_residual = res;
+    r->si_residual = res;
+    r->solve_ms = ms;
+    r->si_counts_len = 1;
+    if (r->si_counts && r->si_counts_capacity) r->si_counts[0] = iters;
+  }
+  return status;
+}
+
 doma_status solve_impl(doma_solver * s, doma_report * r)
 {
+  if (s->mgi && (s->accel || s->d_ref)) return solve_multigroup_guided(s, r);
   if (s->mgi) return solve_multigroup(s, r);
   if (s->use_graph) return solve_graph(s, r);
   const doma_options & o = s->opts;
@@ -1104,6 +1257,84 @@ doma_status doma_solver_describe(const doma_solver * s, uint32_t tile[3],
   return DOMA_OK;
 }
 
+doma_status doma_solver_set_accelerator(doma_solver * s, doma_unet * net,
+                                        const doma_accel_options * opts)
+{
+  if (!s) return bad("null solver");
+  if (!net) {
+    s->accel = nullptr;
+    return DOMA_OK;
+  }
+  if (!opts) return bad("null accelerator options");
+  if (!s->mgi) return bad("the accelerator works in multigroup iteration (DOMA_ITER_MULTIGROUP)");
+  if (s->dims != 3 || s->nx % 8 || s->ny % 8 || s->nz % 8)
+    return bad("the accelerator needs a 3D mesh with extents that are multiples of 8");
+  if (s->opts.scheme != DOMA_SCHEME_DD)
+    return bad("the accelerator needs the linear diamond-difference scheme (DOMA_SCHEME_DD)");
+  const size_t G = s->G, N = s->N;
+  if (!s->d_fsig) {
+    DOMA_TRY(dalloc(s, &s->d_fsig, G * N));
+    DOMA_TRY(dalloc(s, &s->d_fabs, G * N));
+    DOMA_TRY(dalloc(s, &s->d_kappa, G * N));
+    DOMA_TRY(dalloc(s, &s->d_corr, G * N));
+    DOMA_TRY(dalloc(s, &s->d_r, N));
+    DOMA_TRY(dalloc(s, &s->d_ya, N));
+    DOMA_TRY(dalloc(s, &s->d_yb, N));
+    DOMA_TRY(dalloc(s, &s->d_nn_out, N));
+    uint16_t * in = nullptr;
+    DOMA_TRY(dalloc(s, &in, N * 16));
+    s->d_nn_in = in;
+    DOMA_TRY(dalloc(s, &s->d_rms, G));
+    DOMA_TRY(dalloc(s, &s->d_phi_save, G * N));
+    DOMA_TRY(dalloc(s, &s->d_delta_save, G * N));
+  }
+  if (!s->d_acc_partials) {
+    DOMA_TRY(dalloc(s, &s->d_acc_partials, (size_t)s->it.grid));
+    DOMA_TRY(dalloc(s, &s->d_acc_ticket, 1));
+    DOMA_CUDA_TRY(cudaMemset(s->d_acc_ticket, 0, sizeof(unsigned)));
+  }
+  DOMA_TRY(accel_features(s->it, s->d_fsig, s->d_fabs, s->d_kappa, s->stream));
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->accel = net;
+  s->accel_opts = *opts;
+  return DOMA_OK;
+}
+
+doma_status doma_solver_set_reference(doma_solver * s, const double * phi_ref, size_t count,
+                                      double target_error)
+{
+  if (!s) return bad("null solver");
+  if (!phi_ref) {
+    s->d_ref = nullptr;
+    return DOMA_OK;
+  }
+  if (!s->mgi) return bad("the reference stop works in multigroup iteration (DOMA_ITER_MULTIGROUP)");
+  const size_t n = (size_t)s->G * s->N;
+  if (count != n) return bad("reference flux must hold num_groups * num_cells values");
+  if (!(target_error > 0.0)) return bad("target error must be positive");
+  double norm2 = 0.0;
+  for (size_t i = 0; i < n; ++i) norm2 += phi_ref[i] * phi_ref[i];
+  if (!(norm2 > 0.0) || !std::isfinite(norm2)) return bad("reference flux is zero or not finite");
+  if (!s->d_acc_partials) {
+    DOMA_TRY(dalloc(s, &s->d_acc_partials, (size_t)s->it.grid));
+    DOMA_TRY(dalloc(s, &s->d_acc_ticket, 1));
+    DOMA_CUDA_TRY(cudaMemset(s->d_acc_ticket, 0, sizeof(unsigned)));
+  }
+  double * ref = nullptr;
+  DOMA_TRY(upload(s, &ref, phi_ref, n));
+  s->d_ref = ref;
+  s->ref_norm2 = norm2;
+  s->ref_target = target_error;
+  return DOMA_OK;
+}
+
+doma_status doma_solver_accel_stats(const doma_solver * s, doma_accel_stats * out)
+{
+  if (!s || !out) return bad("null solver or output");
+  *out = s->stats;
+  return DOMA_OK;
+}
+
 void doma_solver_destroy(doma_solver * s) { release(s); }
 
 }  // extern "C"
@@ -1143,6 +1374,8 @@ struct doma_batch {
   bool use_graph = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  unsigned iters = 0;   // batched iterations since doma_batch_begin
+  std::chrono::steady_clock::time_point t_begin{};
   std::vector<void *> allocs;
 };
 
@@ -1446,51 +1679,70 @@ doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
   return DOMA_OK;
 }
 
-doma_status doma_batch_solve(doma_batch * b, doma_report * reports, size_t count)
+doma_status doma_batch_begin(doma_batch * b)
 {
   if (!b) return bad("null batch");
-  const auto t0 = std::chrono::steady_clock::now();
-  const size_t P = b->solvers.size();
   DOMA_TRY(batch_init_sources(b));
   DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, 2 * sizeof(unsigned), b->stream));
-  unsigned iters = 0;
-  if (b->use_graph) {
-    if (!b->exec) DOMA_TRY(build_batch_graph(b));
-    DOMA_CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
+  b->iters = 0;
+  b->t_begin = std::chrono::steady_clock::now();
+  return DOMA_OK;
+}
+
+doma_status doma_batch_iterate(doma_batch * b, uint32_t iterations, uint32_t * active)
+{
+  if (!b) return bad("null batch");
+  unsigned still = 1;
+  for (uint32_t k = 0; k < iterations; ++k) {
+    DOMA_TRY(batch_iteration(b, b->stream));
     DOMA_CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
                                   b->stream));
     DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
-    iters = b->h_ctl->iters;
-  } else {
-    for (;;) {
-      DOMA_TRY(batch_iteration(b, b->stream));
-      DOMA_CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
-                                    b->stream));
-      DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
-      ++iters;
-      if (b->h_ctl->error || b->h_ctl->still_active == 0 || iters > b->opts.fs_max_it) break;
-      DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, sizeof(unsigned), b->stream));
+    ++b->iters;
+    if (b->h_ctl->error) {
+      set_error("a batched sweep wait for an upstream block timed out");
+      return DOMA_DEVICE_WAIT_TIMEOUT;
     }
+    still = b->h_ctl->still_active;
+    DOMA_CUDA_TRY(cudaMemsetAsync(&b->d_ctl->still_active, 0, sizeof(unsigned), b->stream));
+    if (still == 0) break;
   }
-  if (b->h_ctl->error) {
-    set_error("a batched sweep wait for an upstream block timed out");
-    return DOMA_DEVICE_WAIT_TIMEOUT;
-  }
+  if (active) *active = still;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_state(doma_batch * b, size_t index, const double ** phi,
+                             const double ** increment)
+{
+  if (!b) return bad("null batch");
+  if (index >= b->solvers.size()) return bad("problem index out of range");
+  DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (phi) *phi = b->solvers[index]->d_phi;
+  if (increment) *increment = b->solvers[index]->d_dscratch;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_reports(doma_batch * b, doma_report * reports, size_t count)
+{
+  if (!b) return bad("null batch");
+  const size_t P = b->solvers.size();
   std::vector<BatchLoop> loops(P);
+  DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
   DOMA_CUDA_TRY(cudaMemcpy(loops.data(), b->d_loops, P * sizeof(BatchLoop), cudaMemcpyDeviceToHost));
   const auto t1 = std::chrono::steady_clock::now();
-  const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  const double ms = std::chrono::duration<double, std::milli>(t1 - b->t_begin).count();
   doma_status first = DOMA_OK;
   for (size_t p = 0; p < P; ++p) {
     const doma_solver * s = b->solvers[p];
-    if (loops[p].status != DOMA_OK && first == DOMA_OK) first = (doma_status)loops[p].status;
+    const doma_status ps = loops[p].active ? DOMA_NOT_CONVERGED : (doma_status)loops[p].status;
+    if (ps != DOMA_OK && first == DOMA_OK) first = ps;
     if (reports && p < count) {
       doma_report & r = reports[p];
-      r.status = loops[p].status;
+      r.status = ps;
       r.mg_iterations = loops[p].it;
       r.si_iterations = (uint64_t)loops[p].it * s->G;
       r.updates = (uint64_t)loops[p].it * s->G * s->N * (uint64_t)s->D;
-      r.kernel_launches = (b->use_graph ? 4ull : 3ull) * iters;
+      r.kernel_launches = (b->use_graph ? 4ull : 3ull) * b->iters;
       r.mg_residual = loops[p].res;
       r.si_residual = loops[p].res;
       r.solve_ms = ms;
@@ -1500,6 +1752,28 @@ doma_status doma_batch_solve(doma_batch * b, doma_report * reports, size_t count
   }
   if (first != DOMA_OK) set_error("a problem of the batch did not converge");
   return first;
+}
+
+doma_status doma_batch_solve(doma_batch * b, doma_report * reports, size_t count)
+{
+  if (!b) return bad("null batch");
+  DOMA_TRY(doma_batch_begin(b));
+  if (b->use_graph) {
+    if (!b->exec) DOMA_TRY(build_batch_graph(b));
+    DOMA_CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
+    DOMA_CUDA_TRY(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
+                                  b->stream));
+    DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->iters = b->h_ctl->iters;
+    if (b->h_ctl->error) {
+      set_error("a batched sweep wait for an upstream block timed out");
+      return DOMA_DEVICE_WAIT_TIMEOUT;
+    }
+  } else {
+    uint32_t active = 1;
+    DOMA_TRY(doma_batch_iterate(b, b->opts.fs_max_it + 1u, &active));
+  }
+  return doma_batch_reports(b, reports, count);
 }
 
 doma_status doma_batch_get_scalar_flux(doma_batch * b, size_t index, double * out, size_t count)

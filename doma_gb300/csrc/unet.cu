@@ -405,6 +405,29 @@ doma_status doma_unet_last_loss(doma_unet * n, double * loss)
   return DOMA_OK;
 }
 
+doma_status doma_conv3_forward(const void * x, uint32_t batch, uint32_t nz, uint32_t ny,
+                               uint32_t nx, uint32_t cin, const void * w, const float * bias,
+                               uint32_t cout, uint32_t relu, void * y, uint32_t path, void * stream)
+{
+  if (!x || !w || !y) return bad_net("null tensor");
+  const ConvShape s{(int)batch, (int)nz, (int)ny, (int)nx};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bf16 * xb = static_cast<const bf16 *>(x);
+  const bf16 * wb = static_cast<const bf16 *>(w);
+  bf16 * yb = static_cast<bf16 *>(y);
+  if (path == DOMA_CONV_MMA)
+    return conv3_forward_mma(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
+  if (path == DOMA_CONV_TENSOR_MEMORY)
+    return conv3_forward_tc(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
+  return conv3_forward(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
+}
+
+doma_status doma_conv_wait_error(int * flag)
+{
+  if (!flag) return bad_net("null flag");
+  return conv3_tc_error(flag);
+}
+
 doma_status doma_unet_adam(doma_unet * n, float lr, float beta1, float beta2, float eps)
 {
   if (!n) return bad_net("null network");

@@ -1,0 +1,128 @@
+"""Training pairs for the learned accelerator, generated by the GPU solver.
+
+For each seeded problem the batched FP32 solver runs multigroup source
+iterations from a zero flux, recording the increment delta_k and flux phi_k
+after iterations k = 1..K, then continues to convergence (phi*).  With
+e_k = phi* - phi_k and y = e_k + delta_k, the per-group pair is
+
+    r_g = delta_g + kappa_g * y_{g-1}      (network input, before scaling)
+    z_g = e_g     - kappa_g * y_{g-1}      (network target, before scaling)
+
+kappa_g = S[g][g-1] / sigma_t,g.  This is the split the solver's correction
+step uses (doma_gb300/csrc/accel.cuh): the network maps r_g / rms(r_g) and
+the cell features to z_g / rms(r_g).  Pairs are linear in the increment, so
+any linear combination of one problem's pairs is again a valid pair (used to
+augment the training set).
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .. import problems as P
+from ..solver import Batch
+
+# Feature scaling, identical to kFeatSigma / kFeatAbs* in csrc/accel.cuh.
+FEAT_SIGMA = 0.8
+FEAT_ABS_FLOOR = 1e-6
+FEAT_ABS_SHIFT = -4.6
+FEAT_ABS_SCALE = 1.5
+
+
+def features(p: P.Problem) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(f_sigma, f_abs, kappa), each [G][N] float32, per cell through its material."""
+    m = p.cell_material
+    st = p.total[m]                                  # [N][G]
+    G = p.num_groups
+    diag = p.scatter[m][:, np.arange(G), np.arange(G)]
+    c = diag / st
+    fsig = (np.log(st) / FEAT_SIGMA).T
+    fabs_ = ((np.log(np.maximum(1.0 - c, FEAT_ABS_FLOOR)) - FEAT_ABS_SHIFT) / FEAT_ABS_SCALE).T
+    kappa = np.zeros_like(st)
+    for g in range(1, G):
+        kappa[:, g] = p.scatter[m][:, g, g - 1] / st[:, g]
+    return (fsig.astype(np.float32), fabs_.astype(np.float32), kappa.T.astype(np.float32).copy())
+
+
+class _DeviceArray:
+    """A device buffer owned by the library, seen by torch without a copy."""
+
+    def __init__(self, ptr: int, count: int):
+        self.__cuda_array_interface__ = {"shape": (count,), "typestr": "<f8",
+                                         "data": (ptr, False), "version": 3}
+
+
+def device_view(ptr: int, count: int) -> torch.Tensor:
+    return torch.as_tensor(_DeviceArray(ptr, count), device="cuda")
+
+
+@dataclass
+class PairSet:
+    """R, Z: [P][K][G][N] float32; F: [P][G][2][N] float32 (f_sigma, f_abs);
+    all on the GPU.  n: mesh extent (n^3 cells)."""
+    R: torch.Tensor
+    Z: torch.Tensor
+    F: torch.Tensor
+    n: int
+    iterations: list
+    seconds: float
+
+    @property
+    def num_problems(self) -> int:
+        return int(self.R.shape[0])
+
+
+def generate(problems: list[P.Problem], k_max: int = 10, tol: float = 1e-6,
+             max_it: int = 20000, chunk: int = 256, log=print) -> PairSet:
+    """Solve every problem on the GPU (batched, FP32 multigroup DD) and return
+    the pairs of the converged ones."""
+    t0 = time.perf_counter()
+    n = problems[0].nx
+    G = problems[0].num_groups
+    N = n ** 3
+    stream = torch.cuda.Stream()
+    Rs, Zs, Fs, iters = [], [], [], []
+    with torch.cuda.stream(stream):
+        for c0 in range(0, len(problems), chunk):
+            part = problems[c0:c0 + chunk]
+            b = Batch(part, scheme="dd", precision="fp32", fs_tol=tol, fs_max_it=max_it,
+                      iteration="multigroup")
+            b.set_stream(stream.cuda_stream)
+            b.begin()
+            phis = torch.empty((len(part), k_max, G, N), dtype=torch.float32, device="cuda")
+            deltas = torch.empty_like(phis)
+            for k in range(k_max):
+                b.iterate(1)
+                for i in range(len(part)):
+                    pp, dp = b.state_pointers(i)
+                    phis[i, k] = device_view(pp, G * N).view(G, N).float()
+                    deltas[i, k] = device_view(dp, G * N).view(G, N).float()
+            b.iterate(max_it)
+            reps = b.reports()
+            for i, p in enumerate(part):
+                if not reps[i].converged:
+                    log(f"  {p.name}: not converged ({reps[i].mg_residual:.2e}), skipped")
+                    continue
+                pp, _ = b.state_pointers(i)
+                star = device_view(pp, G * N).view(G, N).float()
+                fsig, fab, kap = features(p)
+                kappa = torch.from_numpy(kap).cuda()
+                e = star[None] - phis[i]                  # [K][G][N]
+                y = e + deltas[i]
+                yprev = torch.zeros_like(y)
+                yprev[:, 1:] = y[:, :-1]
+                coup = kappa[None] * yprev
+                Rs.append(deltas[i] + coup)
+                Zs.append(e - coup)
+                Fs.append(torch.from_numpy(np.stack([fsig, fab], axis=1)).cuda())
+                iters.append(reps[i].mg_iterations)
+            b.close()
+            torch.cuda.current_stream().synchronize()
+            log(f"  generated {min(c0 + chunk, len(problems))}/{len(problems)} problems, "
+                f"{time.perf_counter() - t0:.1f} s")
+    stream.synchronize()
+    return PairSet(torch.stack(Rs), torch.stack(Zs), torch.stack(Fs), n, iters,
+                   time.perf_counter() - t0)

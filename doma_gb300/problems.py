@@ -443,3 +443,58 @@ def batch_mix(seed: int = 0, count: int = 256, n_range=(16, 96), groups=(1, 2, 4
     ks = r.integers(count, k_range[0], k_range[1] + 1)
     return [checkerboard(seed * 100003 + i, n=int(ns[i]), groups=int(groups[gs[i]]),
                          np_=int(ks[i]), na=int(ks[i]), block=8) for i in range(count)]
+
+
+# ---------------------------------------------------------------------------
+# Learned-accelerator workload
+
+def gaussian_field(rng: np.random.Generator, n: int, corr: float = 4.0) -> np.ndarray:
+    """Unit-variance periodic Gaussian random field on an n^3 grid: white
+    normal noise convolved (by FFT) with exp(-d^2 / corr^2), d the periodic
+    distance in cells, so the field's covariance is exp(-d^2 / (2 corr^2))."""
+    d = np.minimum(np.arange(n), n - np.arange(n)).astype(np.float64)
+    k1 = np.exp(-(d * d) / (corr * corr))
+    kern = k1[:, None, None] * k1[None, :, None] * k1[None, None, :]
+    w = rng.standard_normal((n, n, n))
+    ax = (0, 1, 2)
+    f = np.fft.irfftn(np.fft.rfftn(w, axes=ax) * np.fft.rfftn(kern, axes=ax), s=(n, n, n), axes=ax)
+    return f / np.sqrt(np.sum(kern * kern))
+
+
+def learned_problem(seed: int = 0, n: int = 32, groups: int = 4, np_: int = 3, na: int = 3,
+                    log_sigma: float = 0.8, corr: float = 4.0, c_range=(0.9, 0.999),
+                    downscatter: float = 0.5, max_blocks: int = 3) -> Problem:
+    """High-scattering heterogeneous problem of the learned accelerator.
+
+    n^3 cells of 1 cm.  Per cell and group, sigma_t = exp(log_sigma * Z) with Z
+    a unit-variance Gaussian random field of correlation length `corr` cells
+    (median 1 cm^-1), and a scattering ratio c ~ U[c_range] drawn per cell.
+    Group g keeps c * sigma_t in-group and sends downscatter * (1 - c) *
+    sigma_t to group g+1 (the last group keeps only its in-group part), so
+    the problem is subcritical and dominated by in-group scattering.  Sources:
+    1..max_blocks unit blocks of (n/8)^3 cells at seeded positions, each in a
+    seeded group.  Every cell is its own material.  Inputs come from numpy's
+    PCG64 generator: deterministic for a seed, meant for training and
+    evaluation data, not for bitwise fixtures."""
+    rng = np.random.default_rng([int(seed), 0x6C65_6172])
+    N, G = n ** 3, groups
+    total = np.empty((N, G))
+    c = rng.uniform(c_range[0], c_range[1], (N, G))
+    for g in range(G):
+        total[:, g] = np.exp(log_sigma * gaussian_field(rng, n, corr)).reshape(-1)
+    scatter = np.zeros((N, G, G))
+    for g in range(G):
+        scatter[:, g, g] = c[:, g] * total[:, g]
+        if g + 1 < G:
+            scatter[:, g + 1, g] = downscatter * (1.0 - c[:, g]) * total[:, g]
+    source = np.zeros((n, n, n, G))
+    b = max(2, n // 8)
+    for _ in range(int(rng.integers(1, max_blocks + 1))):
+        z, y, x = (int(v) for v in rng.integers(0, n - b + 1, 3))
+        source[z:z + b, y:y + b, x:x + b, int(rng.integers(0, G))] = 1.0
+    return Problem(
+        num_dims=3, dx=np.ones(n), dy=np.ones(n), dz=np.ones(n),
+        cell_material=np.arange(N, dtype=np.uint32), total=total, scatter=scatter,
+        source=source.reshape(N, G), num_polar=np_, num_azimuthal=na,
+        name=f"learned_s{seed}_n{n}_g{G}", meta={"seed": seed, "c_range": c_range},
+    )

@@ -100,6 +100,34 @@ class Solver:
         abi.check(self.lib.doma_solver_sweeps(self._h, group, count), "doma_solver_sweeps",
                   self.lib)
 
+    def set_accelerator(self, net, first: int = 3, interval: int = 3, max_corrections: int = 32,
+                        guard: bool = True) -> None:
+        """Learned corrections (net: doma_gb300.learned.net.UNet, or None to detach)."""
+        o = abi.DomaAccelOptions(first=first, interval=interval, max_corrections=max_corrections,
+                                 guard=1 if guard else 0)
+        self._net = net
+        abi.check(self.lib.doma_solver_set_accelerator(self._h, net.handle if net else None,
+                                                       ctypes.byref(o)),
+                  "doma_solver_set_accelerator", self.lib)
+
+    def set_reference(self, phi_ref: np.ndarray | None, target: float = 1e-5) -> None:
+        """Stop on relative L2 error <= target against phi_ref ([G][N])."""
+        if phi_ref is None:
+            abi.check(self.lib.doma_solver_set_reference(self._h, None, 0, 0.0),
+                      "doma_solver_set_reference", self.lib)
+            return
+        ref = np.ascontiguousarray(phi_ref, dtype=np.float64).reshape(-1)
+        abi.check(self.lib.doma_solver_set_reference(
+            self._h, ref.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ref.size, target),
+            "doma_solver_set_reference", self.lib)
+
+    def accel_stats(self) -> dict:
+        st = abi.DomaAccelStats()
+        abi.check(self.lib.doma_solver_accel_stats(self._h, ctypes.byref(st)),
+                  "doma_solver_accel_stats", self.lib)
+        return {"iterations": st.iterations, "accepted": st.corrections_accepted,
+                "rejected": st.corrections_rejected, "error": st.error, "solve_ms": st.solve_ms}
+
     def describe(self) -> dict:
         tile = (ctypes.c_uint32 * 3)()
         lps = ctypes.c_uint32()
@@ -160,6 +188,34 @@ class Batch:
         reps = (abi.DomaReport * n)()
         st = self.lib.doma_batch_solve(self._h, reps, n)
         abi.check(st, "doma_batch_solve", self.lib, allow=(abi.DOMA_OK, abi.DOMA_NOT_CONVERGED))
+        return [Report(converged=r.status == abi.DOMA_OK, status=r.status,
+                       mg_iterations=r.mg_iterations, si_iterations=r.si_iterations,
+                       updates=r.updates, kernel_launches=r.kernel_launches,
+                       mg_residual=r.mg_residual, si_residual=r.si_residual, solve_ms=r.solve_ms,
+                       si_counts=np.array([r.mg_iterations], dtype=np.uint32)) for r in reps]
+
+    def begin(self) -> None:
+        abi.check(self.lib.doma_batch_begin(self._h), "doma_batch_begin", self.lib)
+
+    def iterate(self, iterations: int) -> int:
+        """Run up to `iterations` batched iterations; returns problems still active."""
+        active = ctypes.c_uint32()
+        abi.check(self.lib.doma_batch_iterate(self._h, iterations, ctypes.byref(active)),
+                  "doma_batch_iterate", self.lib)
+        return active.value
+
+    def state_pointers(self, index: int) -> tuple[int, int]:
+        """Device addresses of problem `index`'s flux and last increment ([G][N] doubles)."""
+        phi, inc = ctypes.c_void_p(), ctypes.c_void_p()
+        abi.check(self.lib.doma_batch_state(self._h, index, ctypes.byref(phi), ctypes.byref(inc)),
+                  "doma_batch_state", self.lib)
+        return phi.value, inc.value
+
+    def reports(self) -> list[Report]:
+        n = len(self.problems)
+        reps = (abi.DomaReport * n)()
+        st = self.lib.doma_batch_reports(self._h, reps, n)
+        abi.check(st, "doma_batch_reports", self.lib, allow=(abi.DOMA_OK, abi.DOMA_NOT_CONVERGED))
         return [Report(converged=r.status == abi.DOMA_OK, status=r.status,
                        mg_iterations=r.mg_iterations, si_iterations=r.si_iterations,
                        updates=r.updates, kernel_launches=r.kernel_launches,

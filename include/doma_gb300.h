@@ -208,6 +208,17 @@ doma_status doma_batch_tune(doma_batch *batch, uint32_t *tile_x);
 doma_status doma_batch_solve(doma_batch *batch, doma_report *reports, size_t count);
 doma_status doma_batch_get_scalar_flux(doma_batch *batch, size_t index, double *out,
                                        size_t count);
+/* Stepping (what doma_batch_solve does, in parts): begin sets every problem
+ * to a zero flux with its external source; iterate runs up to `iterations`
+ * batched iterations (fewer once no problem is active; *active gets the count
+ * still iterating); state returns DEVICE pointers to a problem's scalar flux
+ * and last increment ([G][N] doubles each, valid until the next call that
+ * iterates); reports fills per-problem reports as doma_batch_solve does. */
+doma_status doma_batch_begin(doma_batch *batch);
+doma_status doma_batch_iterate(doma_batch *batch, uint32_t iterations, uint32_t *active);
+doma_status doma_batch_state(doma_batch *batch, size_t index, const double **phi,
+                             const double **increment);
+doma_status doma_batch_reports(doma_batch *batch, doma_report *reports, size_t count);
 void doma_batch_destroy(doma_batch *batch);
 
 /* One FP32 sweep that allocates no memory -- no counterpart in DOMA.
@@ -260,6 +271,52 @@ doma_status doma_unet_backward(doma_unet *net, const void *input, const float *t
 doma_status doma_unet_last_loss(doma_unet *net, double *loss);
 /* One Adam step (bias-corrected) with the last gradients. */
 doma_status doma_unet_adam(doma_unet *net, float lr, float beta1, float beta2, float eps);
+/* One 3x3x3 convolution of the network's kind (zero padding, stride 1):
+ * y = act(conv(x, w) + bias), x [batch][nz][ny][nx][cin] bf16, w
+ * [27][cout][cin] bf16, bias [cout] float or NULL, y [..][cout] bf16, all
+ * device memory; cin in {16,32,64,128,256}, cout in {32,64,128,256}.  path
+ * selects the kernel: DOMA_CONV_AUTO (tensor-memory kernel where the shape
+ * tiles into 128-voxel boxes, else the warp-MMA kernel), DOMA_CONV_MMA or
+ * DOMA_CONV_TENSOR_MEMORY (tcgen05 + TMA; BAD_INPUT for shapes it does not
+ * tile).  Asynchronous on `stream`.  doma_conv_wait_error reads the flag the
+ * tensor-memory kernel sets if one of its bounded waits gave up. */
+enum { DOMA_CONV_AUTO = 0, DOMA_CONV_MMA = 1, DOMA_CONV_TENSOR_MEMORY = 2 };
+doma_status doma_conv3_forward(const void *x, uint32_t batch, uint32_t nz, uint32_t ny,
+                               uint32_t nx, uint32_t cin, const void *w, const float *bias,
+                               uint32_t cout, uint32_t relu, void *y, uint32_t path, void *stream);
+doma_status doma_conv_wait_error(int *flag);
+
+/* Learned corrections inside a multigroup solve (3D, DD, extents multiples
+ * of 8).  After `first` iterations, and then every `interval` iterations,
+ * the network proposes a correction of the flux from the last increment,
+ * group by group; the next iteration sweeps from the corrected iterate.  With
+ * `guard` set, a correction after which the relative increment norm rose is
+ * undone (the flux, increment and source of the iterate before it come back;
+ * that sweep is spent), so the plain iteration stays the fallback and the
+ * fixed point is the plain solver's.  The network must outlive the solver's
+ * solves (net NULL detaches it). */
+typedef struct {
+  uint32_t first;            /* iterations before the first correction (>= 1) */
+  uint32_t interval;         /* plain iterations between corrections */
+  uint32_t max_corrections;  /* corrections tried at most */
+  uint32_t guard;            /* 1: undo corrections that raise the residual */
+} doma_accel_options;
+doma_status doma_solver_set_accelerator(doma_solver *solver, doma_unet *net,
+                                        const doma_accel_options *opts);
+/* Stop a multigroup solve once the relative L2 error of the flux against
+ * phi_ref ([G][N] host values) is <= target_error, instead of on the
+ * increment norm (time-to-accuracy measurements).  phi_ref NULL removes it. */
+doma_status doma_solver_set_reference(doma_solver *solver, const double *phi_ref, size_t count,
+                                      double target_error);
+typedef struct {
+  uint32_t iterations;
+  uint32_t corrections_accepted;
+  uint32_t corrections_rejected;
+  uint32_t reserved;
+  double error;     /* last relative L2 error against the reference, or -1 */
+  double solve_ms;  /* wall time of the last guided solve */
+} doma_accel_stats;
+doma_status doma_solver_accel_stats(const doma_solver *solver, doma_accel_stats *out);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -1,0 +1,77 @@
+"""The tensor-memory convolution (tcgen05 + TMA) against the warp-MMA kernel
+and the FP64 oracle, over the channel counts and box shapes the U-Net uses."""
+import ctypes
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+import unet_oracle as U  # noqa: E402
+
+CASES = [
+    # (batch, nz, ny, nx, cin, cout)
+    (1, 32, 32, 32, 16, 32),    # first layer: 32-byte swizzle
+    (2, 16, 16, 16, 32, 64),    # 64-byte swizzle
+    (1, 16, 16, 16, 64, 128),   # 128-byte swizzle
+    (2, 8, 8, 8, 128, 256),     # box spans z
+    (4, 4, 4, 4, 256, 128),     # box spans the batch
+    (1, 8, 16, 32, 256, 256),   # non-cubic
+    (1, 16, 16, 16, 64, 32),
+]
+
+
+def run(case, path, relu, seed=0):
+    import torch
+    from doma_gb300 import abi
+    b, z, y, x, cin, cout = case
+    rng = np.random.default_rng(seed)
+    xs = rng.normal(0, 1, (b, z, y, x, cin)).astype(np.float32)
+    ws = rng.normal(0, 1 / np.sqrt(27 * cin), (27, cout, cin)).astype(np.float32)
+    bias = rng.normal(0, 0.1, cout).astype(np.float32)
+    dev = torch.device("cuda:0")
+    xd = torch.from_numpy(xs).to(dev).to(torch.bfloat16).contiguous()
+    wd = torch.from_numpy(ws).to(dev).to(torch.bfloat16).contiguous()
+    bd = torch.from_numpy(bias).to(dev)
+    yd = torch.full((b, z, y, x, cout), float("nan"), device=dev).to(torch.bfloat16)
+    lib = abi.load_library()
+    st = lib.doma_conv3_forward(ctypes.c_void_p(xd.data_ptr()), b, z, y, x, cin,
+                                ctypes.c_void_p(wd.data_ptr()),
+                                ctypes.cast(ctypes.c_void_p(bd.data_ptr()), ctypes.c_void_p),
+                                cout, int(relu), ctypes.c_void_p(yd.data_ptr()), path, None)
+    abi.check(st, "doma_conv3_forward", lib)
+    torch.cuda.synchronize()
+    flag = ctypes.c_int(-1)
+    abi.check(lib.doma_conv_wait_error(ctypes.byref(flag)), "doma_conv_wait_error", lib)
+    assert flag.value == 0
+    got = yd.float().cpu().numpy().astype(np.float64)
+    want = U.conv(U.round_bf16(xs), U.round_bf16(ws), bias.astype(np.float64))
+    if relu:
+        want = np.maximum(want, 0.0)
+    return got, want
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_tensor_memory_conv_matches_the_oracle(case):
+    from doma_gb300 import abi
+    got, want = run(case, abi.DOMA_CONV_TENSOR_MEMORY, relu=True)
+    assert np.all(np.isfinite(got))
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err < 5e-3, err
+
+
+@pytest.mark.gpu
+def test_tensor_memory_and_mma_kernels_agree():
+    from doma_gb300 import abi
+    case = (2, 16, 16, 16, 64, 64)
+    a, want = run(case, abi.DOMA_CONV_TENSOR_MEMORY, relu=False, seed=3)
+    b, _ = run(case, abi.DOMA_CONV_MMA, relu=False, seed=3)
+    assert np.linalg.norm(a - b) / np.linalg.norm(want) < 5e-3
+    assert np.linalg.norm(b - want) / np.linalg.norm(want) < 5e-3
+
+
+def test_conv_path_constants_are_exported():
+    from doma_gb300 import abi
+    assert (abi.DOMA_CONV_AUTO, abi.DOMA_CONV_MMA, abi.DOMA_CONV_TENSOR_MEMORY) == (0, 1, 2)
