@@ -187,6 +187,50 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+WEIGHTS = ROOT / "doma_gb300" / "learned" / "weights" / "unet_c32.npz"
+
+
+def learned_leg(args):
+    """Time to args.learned_target relative L2 error against the FP64 solution,
+    plain multigroup FP32 source iteration vs the same with learned corrections,
+    on held-out learned-accelerator problems (64^3, 8 groups, 6x12 directions,
+    c ~ U[0.9, 0.999])."""
+    from doma_gb300 import problems as P
+    from doma_gb300.learned import evaluate as E
+    from doma_gb300.learned.net import UNet
+
+    if not WEIGHTS.exists():
+        return {"unavailable": "no trained weights file"}
+    net = UNet(seed=0)
+    net.load(WEIGHTS)
+    rows = []
+    for i in range(args.learned_problems):
+        p = P.learned_problem(1_000_001 + i, n=args.learned_n, groups=8)
+        t0 = time.perf_counter()
+        ref, info = E.reference_flux(p, tol=1e-10)
+        ref_s = time.perf_counter() - t0
+        plain = E.time_to_error(p, ref, args.learned_target, max_it=20000)
+        lrn = E.time_to_error(p, ref, args.learned_target, net=net, first=args.accel_first,
+                              interval=args.accel_interval, max_corrections=64, max_it=20000)
+        rows.append({"problem": p.name, "fp64_reference_s": ref_s,
+                     "fp64_reference_iterations": info["iterations"],
+                     "plain_ms": plain["ms"], "plain_iterations": plain["iterations"],
+                     "plain_error": plain["error"],
+                     "learned_ms": lrn["ms"], "learned_iterations": lrn["iterations"],
+                     "learned_error": lrn["error"], "corrections_kept": lrn["accepted"],
+                     "corrections_undone": lrn["rejected"]})
+    net.close()
+    plain_ms = sum(r["plain_ms"] for r in rows)
+    learned_ms = sum(r["learned_ms"] for r in rows)
+    return {"target_rel_l2": args.learned_target,
+            "workload": f"{args.learned_n}^3 cells, 8 groups, 6x12 directions, DD, sigma_t lognormal "
+                        "field (log-sigma 0.8, correlation 4 cells), c ~ U[0.9, 0.999]",
+            "plain_ms": plain_ms, "learned_ms": learned_ms,
+            "speedup": plain_ms / learned_ms if learned_ms > 0 else None,
+            "accel": {"first": args.accel_first, "interval": args.accel_interval, "guard": True},
+            "problems": rows}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -310,6 +354,8 @@ def run_ours(args):
                "sample": f"{args.ref_iters} source iterations of group 0 ({upd / 1e6:.1f} M updates, "
                          f"{dt:.1f} s), {threads} OpenMP threads over ordinates"}
 
+    learned = learned_leg(args) if args.learned_problems > 0 else None
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -330,6 +376,7 @@ def run_ours(args):
                      "bytes_per_update": b_upd, "sweep_ms": sweep_ms,
                      "sweep_launches": desc["launches_per_sweep"]},
         "cpu_baseline": cpu,
+        "learned": learned,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
@@ -353,6 +400,11 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-check", type=int, default=1)
+    ap.add_argument("--learned-problems", type=int, default=1)
+    ap.add_argument("--learned-n", type=int, default=64)
+    ap.add_argument("--learned-target", type=float, default=1e-5)
+    ap.add_argument("--accel-first", type=int, default=3)
+    ap.add_argument("--accel-interval", type=int, default=3)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

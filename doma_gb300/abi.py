@@ -163,6 +163,7 @@ SIGNATURES = {
          ctypes.POINTER(ctypes.c_void_p)],
     ),
     "doma_batch_reports": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport), ctypes.c_size_t]),
+    "doma_batch_set_increment": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "doma_solver_set_accelerator": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(DomaAccelOptions)]),
     "doma_solver_set_reference": (

@@ -1722,6 +1722,17 @@ doma_status doma_batch_state(doma_batch * b, size_t index, const double ** phi,
   return DOMA_OK;
 }
 
+doma_status doma_batch_set_increment(doma_batch * b, size_t index, const double * increment)
+{
+  if (!b) return bad("null batch");
+  if (index >= b->solvers.size()) return bad("problem index out of range");
+  if (!increment) return bad("null increment");
+  doma_solver * s = b->solvers[index];
+  DOMA_CUDA_TRY(cudaMemcpyAsync(s->d_dscratch, increment, (size_t)s->G * s->N * sizeof(double),
+                                cudaMemcpyDeviceToDevice, b->stream));
+  return accel_source(s->it, DOMA_PREC_FP32, s->d_dscratch, nullptr, s->d_q, b->stream);
+}
+
 doma_status doma_batch_reports(doma_batch * b, doma_report * reports, size_t count)
 {
   if (!b) return bad("null batch");

@@ -59,6 +59,77 @@ def device_view(ptr: int, count: int) -> torch.Tensor:
     return torch.as_tensor(_DeviceArray(ptr, count), device="cuda")
 
 
+def random_error_fields(gen: torch.Generator, count: int, n: int) -> torch.Tensor:
+    """`count` random smooth fields on an n^3 periodic grid ([count][n^3]
+    float64, on the GPU): a Gaussian random field of correlation length
+    l ~ logU[1, 16] cells plus a mean offset m ~ U[-0.5, 2], times an
+    amplitude a ~ U[0.1, 1], negative for a quarter of the fields.
+    gen is a CUDA generator."""
+    dev = torch.device("cuda")
+    d = torch.arange(n, dtype=torch.float64, device=dev)
+    d = torch.minimum(d, n - d)
+    ell = torch.exp(torch.rand((count, 1), generator=gen, device=dev, dtype=torch.float64)
+                    * np.log(16.0))
+    k1 = torch.exp(-(d[None, :] ** 2) / (ell * ell))                      # [count][n]
+    kern = k1[:, :, None, None] * k1[:, None, :, None] * k1[:, None, None, :]
+    norm = torch.sqrt((kern * kern).sum(dim=(1, 2, 3)))
+    w = torch.randn((count, n, n, n), generator=gen, device=dev, dtype=torch.float64)
+    ax = (1, 2, 3)
+    f = torch.fft.irfftn(torch.fft.rfftn(w, dim=ax) * torch.fft.rfftn(kern, dim=ax), s=(n, n, n),
+                         dim=ax) / norm[:, None, None, None]
+    m = torch.rand((count, 1, 1, 1), generator=gen, device=dev, dtype=torch.float64) * 2.5 - 0.5
+    a = torch.rand((count, 1, 1, 1), generator=gen, device=dev, dtype=torch.float64) * 0.9 + 0.1
+    sign = torch.where(torch.rand((count, 1, 1, 1), generator=gen, device=dev) < 0.75, 1.0, -1.0)
+    return (sign * a * (m + f)).reshape(count, n ** 3)
+
+
+def generate_random(problems: list[P.Problem], rounds: int = 16, seed: int = 0,
+                    chunk: int = 256, log=print) -> tuple[torch.Tensor, torch.Tensor]:
+    """Pairs from arbitrary error fields: for an iterate with error x, one
+    source iteration gives the increment (I - K) x and leaves the error K x,
+    so sweeping x itself (doma_batch_set_increment) yields the pair for any x.
+    Returns R, Z [P][rounds][G][N] float32 in the same split as generate()
+    (y = e + delta = x)."""
+    t0 = time.perf_counter()
+    n = problems[0].nx
+    G = problems[0].num_groups
+    N = n ** 3
+    gen = torch.Generator(device="cuda").manual_seed(int(seed))
+    stream = torch.cuda.Stream()
+    Rs, Zs = [], []
+    with torch.cuda.stream(stream):
+        for c0 in range(0, len(problems), chunk):
+            part = problems[c0:c0 + chunk]
+            b = Batch(part, scheme="dd", precision="fp32", fs_tol=0.0, fs_max_it=1 << 30,
+                      iteration="multigroup")
+            b.set_stream(stream.cuda_stream)
+            b.begin()
+            kap = torch.stack([torch.from_numpy(features(p)[2]) for p in part]).cuda()  # [P][G][N]
+            R = torch.empty((len(part), rounds, G, N), dtype=torch.float32, device="cuda")
+            Z = torch.empty_like(R)
+            for r in range(rounds):
+                xs = random_error_fields(gen, len(part) * G, n).view(len(part), G, N)
+                for i in range(len(part)):
+                    b.set_increment(i, xs[i].data_ptr())
+                b.iterate(1)
+                for i in range(len(part)):
+                    _, ip = b.state_pointers(i)
+                    kx = device_view(ip, G * N).view(G, N)
+                    x = xs[i]
+                    xprev = torch.zeros_like(x)
+                    xprev[1:] = x[:-1]
+                    coup = kap[i].double() * xprev
+                    R[i, r] = (x - kx + coup).float()
+                    Z[i, r] = (kx - coup).float()
+            b.close()
+            Rs.append(R)
+            Zs.append(Z)
+            log(f"  random pairs {min(c0 + chunk, len(problems))}/{len(problems)} problems, "
+                f"{time.perf_counter() - t0:.1f} s")
+    stream.synchronize()
+    return torch.cat(Rs), torch.cat(Zs)
+
+
 @dataclass
 class PairSet:
     """R, Z: [P][K][G][N] float32; F: [P][G][2][N] float32 (f_sigma, f_abs);
@@ -69,6 +140,7 @@ class PairSet:
     n: int
     iterations: list
     seconds: float
+    kept: list = None    # indices (into the problem list) of the problems in the set
 
     @property
     def num_problems(self) -> int:
@@ -84,7 +156,7 @@ def generate(problems: list[P.Problem], k_max: int = 10, tol: float = 1e-6,
     G = problems[0].num_groups
     N = n ** 3
     stream = torch.cuda.Stream()
-    Rs, Zs, Fs, iters = [], [], [], []
+    Rs, Zs, Fs, iters, kept = [], [], [], [], []
     with torch.cuda.stream(stream):
         for c0 in range(0, len(problems), chunk):
             part = problems[c0:c0 + chunk]
@@ -119,10 +191,11 @@ def generate(problems: list[P.Problem], k_max: int = 10, tol: float = 1e-6,
                 Zs.append(e - coup)
                 Fs.append(torch.from_numpy(np.stack([fsig, fab], axis=1)).cuda())
                 iters.append(reps[i].mg_iterations)
+                kept.append(c0 + i)
             b.close()
             torch.cuda.current_stream().synchronize()
             log(f"  generated {min(c0 + chunk, len(problems))}/{len(problems)} problems, "
                 f"{time.perf_counter() - t0:.1f} s")
     stream.synchronize()
     return PairSet(torch.stack(Rs), torch.stack(Zs), torch.stack(Fs), n, iters,
-                   time.perf_counter() - t0)
+                   time.perf_counter() - t0, kept)

@@ -79,6 +79,7 @@ def main():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--random-rounds", type=int, default=16)
     ap.add_argument("--out", default="accel_weights.npz")
     a = ap.parse_args()
     torch.cuda.set_device(0)
@@ -87,6 +88,10 @@ def main():
     ps = D.generate(probs)
     print(f"pairs from {ps.num_problems} problems in {ps.seconds:.1f} s; "
           f"iterations to converge {int(np.median(ps.iterations))} (median)")
+    if a.random_rounds > 0:
+        R, Z = D.generate_random([probs[i] for i in ps.kept], rounds=a.random_rounds, seed=a.seed)
+        ps = D.PairSet(torch.cat([ps.R, R], dim=1), torch.cat([ps.Z, Z], dim=1), ps.F, ps.n,
+                       ps.iterations, ps.seconds, ps.kept)
     net, _ = train(ps, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed)
     net.save(a.out)
     print(f"weights written to {a.out}")

@@ -211,6 +211,11 @@ class Batch:
                   "doma_batch_state", self.lib)
         return phi.value, inc.value
 
+    def set_increment(self, index: int, ptr: int) -> None:
+        """Sweep the device field at `ptr` ([G][N] doubles) in the next iteration."""
+        abi.check(self.lib.doma_batch_set_increment(self._h, index, ctypes.c_void_p(ptr)),
+                  "doma_batch_set_increment", self.lib)
+
     def reports(self) -> list[Report]:
         n = len(self.problems)
         reps = (abi.DomaReport * n)()

@@ -219,6 +219,11 @@ doma_status doma_batch_iterate(doma_batch *batch, uint32_t iterations, uint32_t 
 doma_status doma_batch_state(doma_batch *batch, size_t index, const double **phi,
                              const double **increment);
 doma_status doma_batch_reports(doma_batch *batch, doma_report *reports, size_t count);
+/* Replace problem `index`'s last increment by `increment` (DEVICE [G][N]
+ * doubles) and form the next sweep's source from it: the following
+ * iteration then sweeps that field (the transport operator applied to an
+ * arbitrary error field; used to generate training pairs). */
+doma_status doma_batch_set_increment(doma_batch *batch, size_t index, const double *increment);
 void doma_batch_destroy(doma_batch *batch);
 
 /* One FP32 sweep that allocates no memory -- no counterpart in DOMA.
