@@ -280,9 +280,10 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   const size_t o_cy = cv.take(sizeof(float) * (size_t)D * ny);
   const size_t o_cz = cv.take(sizeof(float) * (size_t)D * nz);
   const size_t o_wf = cv.take(sizeof(float) * (size_t)(nx + ny + nz));
-  const size_t o_xf = cv.take(sizeof(float) * 8 * (size_t)nz * ny * d_oct);
-  const size_t o_yf = cv.take(sizeof(float) * 8 * (size_t)nz * nx * d_oct);
-  const size_t o_zf = cv.take(sizeof(float) * 8 * (size_t)ny * nx * d_oct);
+  const size_t slots = (size_t)ngroups * kGroup;  // face slots per face (padded ordinate groups)
+  const size_t o_xf = cv.take(sizeof(float) * 8 * (size_t)nz * ny * slots);
+  const size_t o_yf = cv.take(sizeof(float) * 8 * (size_t)nz * nx * slots);
+  const size_t o_zf = cv.take(sizeof(float) * 8 * (size_t)ny * nx * slots);
   const size_t o_oct = cv.take(sizeof(double) * 8 * (size_t)ngroups * N);
   if (cv.off > (size_t)DOMA_NOALLOC_SCRATCH_BYTES)
     return fail("the no-alloc sweep needs " + std::to_string(cv.off) + " bytes of scratch; it has " +

@@ -358,7 +358,9 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   DOMA_TRY(dalloc(s, &qb, 2 * gif * N * ts));
   s->d_q = qb;
   s->d_sigt = qb + gif * N * ts;
-  const size_t Do = s->d_oct;
+  // face planes: kGroup slots per face for each ordinate group (the last
+  // group padded), so a task's faces along a row are contiguous
+  const size_t Do = (size_t)((s->d_oct + kGroup - 1) / kGroup) * kGroup;
   unsigned char * fb = nullptr;
   const size_t xf = gif * 8 * (size_t)s->nz * s->ny * Do, yf = gif * 8 * (size_t)s->nz * s->nx * Do,
                zf = gif * 8 * (size_t)s->ny * s->nx * Do;

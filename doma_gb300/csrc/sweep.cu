@@ -42,6 +42,10 @@
 
 #include "common.cuh"
 
+#ifndef DOMA_SWEEP_MIN_CTAS
+#define DOMA_SWEEP_MIN_CTAS 3
+#endif
+
 namespace doma {
 namespace {
 
@@ -161,78 +165,102 @@ __device__ __forceinline__ double twdd2_exact(double q, double st, double amu, d
 // Every operation is an explicit intrinsic (separately rounded add/mul, fused
 // multiply-add where written), so the compiler has no contraction choices and
 // the bits do not depend on which kernel the solve is inlined into.
+//
+// The cell balance is written divided by the cell volume, with the per-axis
+// streaming coefficients hx = |mu|/dx, hy = |eta|/dy, hz = |xi|/dz (DD uses
+// their doubles 2|mu|/dx, ...).  This is the same equation as DOMA's
+// (include/DiamondDifference3D.h:28-48, include/TWDiamondDifference3D.h:32-91),
+// rearranged so that the volume and face areas cancel.
 
 __device__ __forceinline__ float fA(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fS(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fM(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fF(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-// Approximate reciprocal (one MUFU op); the TW-DD weights it inverts lie in [0.5, 1].
-__device__ __forceinline__ float fR(float a) { return __fdividef(1.0f, a); }
 
-// DD with cx = 2|mu|/lx etc.: psi = (q + cx x + cy y + cz z) / (cx + cy + cz + st).
-__device__ __forceinline__ float dd_f32(float q, float st, float cx, float cy, float cz,
-                                        float & x, float & y, float & z)
+// One MUFU reciprocal (approximate, flush-to-zero; every argument here is a
+// normal number).
+__device__ __forceinline__ float rcp_approx(float a)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+
+// DD: psi = (q + cx x + cy y + cz z) / (cx + cy + cz + st), cyz = cy + cz.
+__device__ __forceinline__ float dd3_fast(float q, float st, float cx, float cy, float cz,
+                                          float cyz, float & x, float & y, float & z)
 {
   const float num = fF(cz, z, fF(cy, y, fF(cx, x, q)));
-  const float c = __fdividef(num, fA(fA(fA(cx, cy), cz), st));
+  const float c = fM(num, rcp_approx(fA(fA(cx, cyz), st)));
   x = fF(2.0f, c, -x);
   y = fF(2.0f, c, -y);
   z = fF(2.0f, c, -z);
   return c;
 }
 
-// TW-DD weight: 1 - num / (den * flux), clamped to [0.5, 1]; 0.5 when the
-// upwind flux is <= 1e-8 (include/TWDiamondDifference3D.h:43-75).
-__device__ __forceinline__ float tw_weight(float num, float den_in, float flux)
+__device__ __forceinline__ float dd2_fast(float q, float st, float cx, float cy, float & x,
+                                          float & y)
 {
-  float a = 0.5f;
-  if (flux > 1e-8f) a = fS(1.0f, __fdividef(num, fM(den_in, flux)));
-  return fminf(fmaxf(a, 0.5f), 1.0f);
-}
-
-__device__ __forceinline__ float twdd3_f32(float q, float st, float amu, float aeta, float axi,
-                                           float lx, float ly, float lz, float th, float & x,
-                                           float & y, float & z)
-{
-  const float A = fM(ly, lz), B = fM(lx, lz), C = fM(lx, ly), V = fM(fM(lx, ly), lz);
-  const float muA = fM(amu, A), etB = fM(aeta, B), xiC = fM(axi, C);
-  const float qV = fM(q, V), qVt = fM(qV, th), sV = fM(st, V);
-  const float mx = fM(muA, x), ey = fM(etB, y), xz = fM(xiC, z);
-  const float a = tw_weight(fF(fA(ey, xz), th, fA(qVt, mx)), fF(2.0f, fA(etB, xiC), sV), x);
-  const float b = tw_weight(fF(fA(mx, xz), th, fA(qVt, ey)), fF(2.0f, fA(muA, xiC), sV), y);
-  const float c3 = tw_weight(fF(fA(mx, ey), th, fA(qVt, xz)), fF(2.0f, fA(muA, etB), sV), z);
-  const float ra = fR(a), rb = fR(b), rc = fR(c3);
-  const float ta = fM(muA, ra), tb = fM(etB, rb), tc = fM(xiC, rc);
-  const float c = __fdividef(fF(tc, z, fF(tb, y, fF(ta, x, qV))), fA(fA(fA(sV, ta), tb), tc));
-  x = fM(fF(fS(a, 1.0f), x, c), ra);   // (c - (1 - a) x) / a
-  y = fM(fF(fS(b, 1.0f), y, c), rb);
-  z = fM(fF(fS(c3, 1.0f), z, c), rc);
-  return c;
-}
-
-__device__ __forceinline__ float dd2_f32(float q, float st, float cx, float cy, float & x,
-                                         float & y)
-{
-  const float c = __fdividef(fF(cy, y, fF(cx, x, q)), fA(fA(cx, cy), st));
+  const float c = fM(fF(cy, y, fF(cx, x, q)), rcp_approx(fA(fA(cx, cy), st)));
   x = fF(2.0f, c, -x);
   y = fF(2.0f, c, -y);
   return c;
 }
 
-__device__ __forceinline__ float twdd2_f32(float q, float st, float amu, float aeta, float axi,
-                                           float lx, float ly, float th, float & x, float & y)
+// Reciprocal r = 1/a of one TW-DD axis weight.  DOMA's weight is
+// a = 1 - n / (D flux) when the upwind flux exceeds 1e-8 (else 0.5), clamped
+// to [0.5, 1] (include/TWDiamondDifference3D.h:43-75).  With Dx = D flux > 0,
+// 1/a = Dx / (Dx - n): a >= 1 <-> r <= 1, a in [0.5, 1] <-> r in [1, 2],
+// a < 0.5 (including a <= 0, Dx - n <= 0) <-> r = 2 after the clamp; the
+// floor 1e-30 on Dx - n sends a <= 0 to the r = 2 side.  r is clamped to
+// [1, 2] as 1 + sat(r - 1).
+__device__ __forceinline__ float tw_rweight(float n, float D, float flux)
 {
-  const float A = ly, B = lx, V = fM(lx, ly);
-  const float muA = fM(amu, A), etB = fM(aeta, B);
-  const float qV = fM(q, V), qVt = fM(qV, th), sV = fM(st, V);
-  const float mx = fM(muA, x), ey = fM(etB, y);
-  const float a = tw_weight(fF(ey, th, fA(qVt, mx)), fF(2.0f, etB, sV), x);
-  const float b = tw_weight(fF(fA(mx, axi), th, fA(qVt, ey)), fF(2.0f, muA, sV), y);
-  const float ra = fR(a), rb = fR(b);
-  const float ta = fM(muA, ra), tb = fM(etB, rb);
-  const float c = __fdividef(fF(tb, y, fF(ta, x, qV)), fA(fA(sV, ta), tb));
-  x = fM(fF(fS(a, 1.0f), x, c), ra);
-  y = fM(fF(fS(b, 1.0f), y, c), rb);
+  const float dx = fM(D, flux);
+  const float den = fmaxf(fS(dx, n), 1e-30f);
+  const float r = fA(1.0f, __saturatef(fF(dx, rcp_approx(den), -1.0f)));
+  return flux > 1e-8f ? r : 2.0f;
+}
+
+// TW-DD, volume-normalized.  With X = hx x, Y = hy y, Z = hz z and
+// B = theta (q + X + Y + Z), the weight numerators are B + (1 - theta) X etc.
+// and the denominators (st + 2 hy + 2 hz) x etc. (DOMA's, divided by V).
+// psi = (q + rx X + ry Y + rz Z) / (st + hx rx + hy ry + hz rz) and the
+// outgoing faces x' = (psi - (1 - a) x) / a = x + rx (psi - x).
+// sz = st + 2 hz and sy = st + 2 hy, syz = st + 2 hy + 2 hz.
+__device__ __forceinline__ float twdd3_fast(float q, float st, float hx, float hy, float hz,
+                                            float th, float om, float & x, float & y, float & z)
+{
+  const float X = fM(hx, x), Y = fM(hy, y), Z = fM(hz, z);
+  const float B = fF(th, fA(fA(X, Y), Z), fM(th, q));
+  const float h2x = fA(hx, hx), h2y = fA(hy, hy), h2z = fA(hz, hz);
+  const float ra = tw_rweight(fF(om, X, B), fA(fA(st, h2y), h2z), x);
+  const float rb = tw_rweight(fF(om, Y, B), fA(fA(st, h2z), h2x), y);
+  const float rc = tw_rweight(fF(om, Z, B), fA(fA(st, h2y), h2x), z);
+  const float num = fF(rc, Z, fF(rb, Y, fF(ra, X, q)));
+  const float den = fF(hz, rc, fF(hy, rb, fF(hx, ra, st)));
+  const float c = fM(num, rcp_approx(den));
+  x = fF(ra, fS(c, x), x);
+  y = fF(rb, fS(c, y), y);
+  z = fF(rc, fS(c, z), z);
+  return c;
+}
+
+// 2D TW-DD keeps DOMA's bare |xi| term in the y weight
+// (include/TWDiamondDifference2D.h:51), volume-normalized: theta |xi| / V,
+// passed in as txv.
+__device__ __forceinline__ float twdd2_fast(float q, float st, float hx, float hy, float txv,
+                                            float th, float om, float & x, float & y)
+{
+  const float X = fM(hx, x), Y = fM(hy, y);
+  const float B = fF(th, fA(X, Y), fM(th, q));
+  const float ra = tw_rweight(fF(om, X, B), fA(st, fA(hy, hy)), x);
+  const float rb = tw_rweight(fA(fF(om, Y, B), txv), fA(st, fA(hx, hx)), y);
+  const float num = fF(rb, Y, fF(ra, X, q));
+  const float den = fF(hy, rb, fF(hx, ra, st));
+  const float c = fM(num, rcp_approx(den));
+  x = fF(ra, fS(c, x), x);
+  y = fF(rb, fS(c, y), y);
   return c;
 }
 
@@ -257,8 +285,8 @@ __device__ __forceinline__ int ld_relaxed(const int * p)
   return v;
 }
 
-// Wait until *flag == epoch.  Bounded: the first polls are back to back,
-// then exponential back-off up to ~0.5 us; after `limit` polls it records
+// Wait until *flag == epoch.  Bounded: the first 32 polls are back to back,
+// then back-off of 32..128 ns; after `limit` polls it records
 // DOMA_DEVICE_WAIT_TIMEOUT in *error and returns false.  It also gives up at
 // once when another CTA has already failed.
 __device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, int * error)
@@ -267,9 +295,9 @@ __device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, 
   for (unsigned it = 0; it < limit; ++it) {
     if (ld_acquire(flag) == epoch) return true;
     if (ld_relaxed(error) != 0) return false;
-    if (it >= 8) {
+    if (it >= 32) {
       __nanosleep(ns);
-      if (ns < 512) ns *= 2;
+      if (ns < 128) ns *= 2;
     }
   }
   atomicCAS(error, 0, (int)DOMA_DEVICE_WAIT_TIMEOUT);
@@ -284,30 +312,68 @@ __device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, 
 // A cell's y-upwind neighbour is then lane - 1 and its z-upwind neighbour
 // lane - PY, both computed on the previous step, so faces move between
 // lanes with __shfl_up_sync and the warps advance with no block barrier.
-// Shared memory carries only the block-boundary faces (staged in and out
-// coalesced) and, in fp32 mode, the w*psi values for the angular reduction.
+//
+// Face planes (sweep frame, ordinate-group major, kGroup slots per face so
+// that one task's faces along a row are contiguous):
+//   x [G*8][ngroups][nz][ny][kGroup], y [G*8][ngroups][nz][nx][kGroup],
+//   z [G*8][ngroups][ny][nx][kGroup].
 
 template <int DIMS> struct Pencils;
 template <> struct Pencils<3> { static constexpr int PY = 4, PZ = 4; };
 template <> struct Pencils<2> { static constexpr int PY = 16, PZ = 1; };
 
-template <typename T, int DIMS, int TX>
-struct TaskSmem {
+template <typename T>
+struct FacePlanes {
+  const SweepArgs<T> & A;
+  size_t plane;  // (group in flight, octant, ordinate group)
+  __device__ FacePlanes(const SweepArgs<T> & a, int of, int og) : A(a), plane((size_t)of * a.ngroups + og) {}
+  __device__ size_t x(int k, int j) const { return ((plane * A.nz + k) * A.ny + j) * kGroup; }
+  __device__ size_t y(int k, int i) const { return ((plane * A.nz + k) * A.nx + i) * kGroup; }
+  __device__ size_t z(int j, int i) const { return ((plane * A.ny + j) * A.nx + i) * kGroup; }
+};
+
+// Done flag of block (bk, bj, bi) of a (group, octant, ordinate group) slot.
+template <typename T>
+__device__ __forceinline__ unsigned * done_flag(const SweepArgs<T> & A, size_t slot, int bk, int bj, int bi)
+{
+  return A.done + ((slot * A.nbz + bk) * A.nby + bj) * A.nbx + bi;
+}
+
+// Wait for the upstream blocks of a task: threads 0, 1, 2 poll the x, y and
+// z neighbours' flags concurrently, then the CTA synchronises.
+template <typename T, int DIMS>
+__device__ __forceinline__ void wait_upstream(const SweepArgs<T> & A, const Task & task, size_t slot,
+                                              unsigned epoch)
+{
+  const int t = threadIdx.x;
+  if (t < DIMS) {
+    const unsigned * f = nullptr;
+    if (t == 0 && task.bi > 0) f = done_flag(A, slot, task.bk, task.bj, task.bi - 1);
+    if (t == 1 && task.bj > 0) f = done_flag(A, slot, task.bk, task.bj - 1, task.bi);
+    if (t == 2 && task.bk > 0) f = done_flag(A, slot, task.bk - 1, task.bj, task.bi);
+    if (f) wait_for(f, epoch + A.wait_bias, A.spin_limit, A.error);
+  }
+  __syncthreads();
+}
+
+// ---- double precision (exact, DOMA's arithmetic) ------------------------------
+
+template <int DIMS, int TX>
+struct TaskSmemExact {
   static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
   static constexpr int CELLS = TX * PY * PZ;
   static constexpr int YF = PZ * TX * kGroup;                  // y faces [PZ][TX][kGroup]
   static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
   static constexpr int NT = 2 * YF + 2 * ZF + 2 * CELLS + TX + PY + PZ + kGroup * (TX + PY + PZ);
-  static constexpr bool EXACT = std::is_same<T, double>::value;
-  static constexpr size_t bytes = NT * sizeof(T) + (EXACT ? 0 : (size_t)(kGroup / 2) * CELLS * sizeof(float));
+  static constexpr size_t bytes = NT * sizeof(double);
 };
 
-template <typename T, int DIMS, int SCHEME, int TX>
-__device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task,
-                                         unsigned char * smem_raw, bool dataflow, unsigned epoch)
+template <int DIMS, int SCHEME, int TX>
+__device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, const Task task,
+                                               unsigned char * smem_raw, bool dataflow, unsigned epoch)
 {
-  using SM = TaskSmem<T, DIMS, TX>;
-  constexpr bool EXACT = SM::EXACT;
+  using T = double;
+  using SM = TaskSmemExact<DIMS, TX>;
   constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
   constexpr unsigned FULL = 0xffffffffu;
   const int og = task.og;
@@ -323,6 +389,7 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   const int gs = min(kGroup, Do - n0);
   const int i0 = task.bi * TX, j0 = task.bj * PY, k0 = task.bk * PZ;
   const int vx = min(TX, nx - i0), vy = min(PY, ny - j0), vz = min(PZ, nz - k0);
+  const FacePlanes<T> F(A, of, og);
 
   const int t = threadIdx.x;
   const int lane = t & 31;
@@ -346,7 +413,6 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   T * cxs = lzs + PZ;                 // [kGroup][TX]
   T * cys = cxs + kGroup * TX;        // [kGroup][PY]
   T * czs = cys + kGroup * PY;        // [kGroup][PZ]
-  float * P = reinterpret_cast<float *>(czs + kGroup * PZ);  // fp32: [kGroup / 2][CELLS] pair sums
 
   auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
   auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
@@ -378,59 +444,33 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
       const int nn = e / PZ, kk = e % PZ;
       czs[e] = (nn < gs && kk < vz) ? A.cz[(size_t)(ob + nn) * nz + phys_k(kk)] : (T)0;
     }
-  T amu, aeta, axi;
-  if (EXACT) {
-    amu = (T)A.amu[ord]; aeta = (T)A.aeta[ord]; axi = (T)A.axi[ord];
-  } else {
-    amu = (T)A.amu_f[ord]; aeta = (T)A.aeta_f[ord]; axi = (T)A.axi_f[ord];
-  }
+  const T amu = A.amu[ord], aeta = A.aeta[ord], axi = A.axi[ord];
   const double wgt = A.wgt[ord];
-  const float wgt_f = (float)wgt;
-  const T th = (T)A.theta;
+  const T th = A.theta;
   const size_t slot = (size_t)of * A.ngroups + og;   // (group, octant, ordinate group) slot
 
-  // -- wait for the upstream blocks (dataflow mode) --------------------------------
-  if (dataflow) {
-    if (t == 0) {
-      const int nbx = A.nbx, nby = A.nby, nbz = A.nbz;
-      const size_t base = slot * nbz;
-      const unsigned want = epoch + A.wait_bias;
-      if (task.bi > 0)
-        wait_for(A.done + ((base + task.bk) * nby + task.bj) * nbx + task.bi - 1, want,
-                 A.spin_limit, A.error);
-      if (task.bj > 0)
-        wait_for(A.done + ((base + task.bk) * nby + task.bj - 1) * nbx + task.bi, want,
-                 A.spin_limit, A.error);
-      if (DIMS == 3 && task.bk > 0)
-        wait_for(A.done + ((base + task.bk - 1) * nby + task.bj) * nbx + task.bi, want,
-                 A.spin_limit, A.error);
-    }
-    __syncthreads();
-  }
+  if (dataflow) wait_upstream<T, DIMS>(A, task, slot, epoch);
 
   // -- incoming faces (written by other CTAs: read through L2) -----------------------
   for (int e = t; e < SM::YF; e += blockDim.x) {
     const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
     T v = (T)0;
-    if (task.bj > 0 && nn < gs && il < vx && kk < vz)
-      v = __ldcg(A.yf + (((size_t)of * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn);
+    if (task.bj > 0 && nn < gs && il < vx && kk < vz) v = __ldcg(A.yf + F.y(k0 + kk, i0 + il) + nn);
     yin[e] = v;
   }
   if (DIMS == 3)
     for (int e = t; e < SM::ZF; e += blockDim.x) {
       const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
       T v = (T)0;
-      if (task.bk > 0 && nn < gs && il < vx && jj < vy)
-        v = __ldcg(A.zf + (((size_t)of * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn);
+      if (task.bk > 0 && nn < gs && il < vx && jj < vy) v = __ldcg(A.zf + F.z(j0 + jj, i0 + il) + nn);
       zin[e] = v;
     }
   T xin = (T)0;
-  const size_t xslot = (((size_t)of * nz + (k0 + kl)) * ny + (j0 + jl)) * Do + n0 + nl;
+  const size_t xslot = F.x(k0 + kl, j0 + jl) + nl;
   if (active && task.bi > 0) xin = __ldcg(A.xf + xslot);
   __syncthreads();
 
   // -- wavefront: step s solves the cells with il + jl + kl == s, warp-synchronously --
-  // per-thread constants of the pencil (valid for every active thread)
   const int ebase = (kl * PY + jl) * TX;          // cell index of il = 0
   const int ybase = kl * TX * kGroup + nl;        // y-face slot of il = 0
   const int zbase = jl * TX * kGroup + nl;        // z-face slot of il = 0
@@ -446,108 +486,310 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
   for (int s = 0; s < STEPS; ++s) {
     const int il = s - jl - kl;
     const bool valid = active && (unsigned)il < (unsigned)vx;
-    float wp = 0.0f;
-    int e = 0;
     if (valid) {
       T y = jl == 0 ? yin[ybase + il * kGroup] : ysh;
       T z = (T)0;
       if (DIMS == 3) z = kl == 0 ? zin[zbase + il * kGroup] : zsh;
-      e = ebase + il;
+      const int e = ebase + il;
       const T q = qs[e], st = ss[e];
       T psi;
-      if constexpr (EXACT) {
-        if constexpr (DIMS == 3) {
-          if constexpr (SCHEME == DOMA_SCHEME_DD) {
-            const double geo = dA(dA(cxs[cxbase + il], cy_t), cz_t);
-            psi = dd3_exact(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, geo, xin, y, z);
-          } else {
-            psi = twdd3_exact(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, th, xin, y, z);
-          }
+      if constexpr (DIMS == 3) {
+        if constexpr (SCHEME == DOMA_SCHEME_DD) {
+          const double geo = dA(dA(cxs[cxbase + il], cy_t), cz_t);
+          psi = dd3_exact(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, geo, xin, y, z);
         } else {
-          if constexpr (SCHEME == DOMA_SCHEME_DD) {
-            const double geo = dA(cxs[cxbase + il], cy_t);
-            psi = dd2_exact(q, st, amu, aeta, lxs[il], ly_t, geo, xin, y);
-          } else {
-            psi = twdd2_exact(q, st, amu, aeta, axi, lxs[il], ly_t, th, xin, y);
-          }
+          psi = twdd3_exact(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, th, xin, y, z);
         }
-        const size_t cg = ((size_t)phys_k(kl) * ny + phys_j(jl)) * nx + phys_i(il);
-        A.wpsi[((size_t)task.grp * N + cg) * A.d_total + ord] = dM(wgt, psi);
       } else {
-        if constexpr (DIMS == 3) {
-          if constexpr (SCHEME == DOMA_SCHEME_DD)
-            psi = dd_f32(q, st, cxs[cxbase + il], cy_t, cz_t, xin, y, z);
-          else
-            psi = twdd3_f32(q, st, amu, aeta, axi, lxs[il], ly_t, lz_t, th, xin, y, z);
+        if constexpr (SCHEME == DOMA_SCHEME_DD) {
+          const double geo = dA(cxs[cxbase + il], cy_t);
+          psi = dd2_exact(q, st, amu, aeta, lxs[il], ly_t, geo, xin, y);
         } else {
-          if constexpr (SCHEME == DOMA_SCHEME_DD)
-            psi = dd2_f32(q, st, cxs[cxbase + il], cy_t, xin, y);
-          else
-            psi = twdd2_f32(q, st, amu, aeta, axi, lxs[il], ly_t, th, xin, y);
+          psi = twdd2_exact(q, st, amu, aeta, axi, lxs[il], ly_t, th, xin, y);
         }
-        wp = fM(wgt_f, psi);
       }
+      const size_t cg = ((size_t)phys_k(kl) * ny + phys_j(jl)) * nx + phys_i(il);
+      A.wpsi[((size_t)task.grp * N + cg) * A.d_total + ord] = dM(wgt, psi);
       yo = y;
       zo = z;
       if (jl == vy - 1) yout[ybase + il * kGroup] = y;
       if (DIMS == 3 && kl == vz - 1) zout[zbase + il * kGroup] = z;
-    }
-    if constexpr (!EXACT) {
-      // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1:
-      // sum the pair in-warp, store one value per pair
-      const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
-      if (valid && lane < 16) P[(nl >> 1) * CELLS + e] = pair;
     }
     ysh = __shfl_up_sync(FULL, yo, 1);
     if (DIMS == 3) zsh = __shfl_up_sync(FULL, zo, PY);
   }
   __syncthreads();
 
-  // -- outgoing faces and (fp32) the group's scalar-flux partial ------------------------
+  // -- outgoing faces -----------------------------------------------------------------
   if (active) A.xf[xslot] = xin;
   for (int e = t; e < SM::YF; e += blockDim.x) {
     const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
-    if (nn < gs && il < vx && kk < vz)
-      A.yf[(((size_t)of * nz + (k0 + kk)) * nx + (i0 + il)) * Do + n0 + nn] = yout[e];
+    if (nn < gs && il < vx && kk < vz) A.yf[F.y(k0 + kk, i0 + il) + nn] = yout[e];
   }
   if (DIMS == 3)
     for (int e = t; e < SM::ZF; e += blockDim.x) {
       const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
-      if (nn < gs && il < vx && jj < vy)
-        A.zf[(((size_t)of * ny + (j0 + jj)) * nx + (i0 + il)) * Do + n0 + nn] = zout[e];
+      if (nn < gs && il < vx && jj < vy) A.zf[F.z(j0 + jj, i0 + il) + nn] = zout[e];
     }
-  if constexpr (!EXACT) {
-    for (int e = t; e < CELLS; e += blockDim.x) {
-      const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
-      if (il < vx && jj < vy && kk < vz) {
-        float sum = 0.0f, comp = 0.0f;
-        const int npairs = (gs + 1) >> 1;
-        for (int nn = 0; nn < npairs; ++nn) {  // Kahan over ordinate pairs, fixed order
-          const float yv = fS(P[nn * CELLS + e], comp);
-          const float tv = fA(sum, yv);
-          comp = fS(fS(tv, sum), yv);
-          sum = tv;
-        }
-        const size_t cg = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
-        A.octphi[slot * N + cg] = (double)sum - (double)comp;
-      }
-    }
-  }
 
   // -- publish completion (dataflow mode) ---------------------------------------------
   if (dataflow) {
-    __threadfence();
     __syncthreads();
-    if (t == 0)
-      st_release(A.done + ((slot * A.nbz + task.bk) * A.nby + task.bj) * A.nbx + task.bi, epoch);
+    if (t == 0) {
+      __threadfence();
+      st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
+    }
   }
+}
+
+// ---- single precision -----------------------------------------------------------
+
+template <int DIMS, int TX>
+struct TaskSmemF32 {
+  static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
+  static constexpr int CELLS = TX * PY * PZ;
+  static constexpr int YF = PZ * TX * kGroup;                  // y faces [PZ][TX][kGroup]
+  static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
+  // floats: faces, {q, sigma_t} per cell, x coefficients [kGroup][TX], 1/dx [TX] (2D TW-DD),
+  // ordinate-pair sums of w psi [kGroup / 2][CELLS]
+  static constexpr size_t floats = YF + ZF + 2 * CELLS + kGroup * TX + TX + (kGroup / 2) * CELLS;
+  static constexpr size_t bytes = floats * sizeof(float);
+};
+
+// Coalesced, all-loads-first copy of `count` float4s: in each round every
+// load of a thread is issued before its first shared-memory store, so the
+// round trips overlap.  A full-size CTA (kMaxSweepThreads) needs one round.
+template <int COUNT, typename L>
+__device__ __forceinline__ void stage_f4(float4 * dst, L load)
+{
+  constexpr int IT = (COUNT + kMaxSweepThreads - 1) / kMaxSweepThreads;
+  for (int base = 0; base < COUNT; base += IT * (int)blockDim.x) {
+    float4 v[IT];
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      const int e = base + (int)threadIdx.x + u * (int)blockDim.x;
+      v[u] = e < COUNT ? load(e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      const int e = base + (int)threadIdx.x + u * (int)blockDim.x;
+      if (e < COUNT) dst[e] = v[u];
+    }
+  }
+}
+
+template <int DIMS, int SCHEME, int TX>
+__device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const Task task,
+                                             unsigned char * smem_raw, bool dataflow, unsigned epoch)
+{
+  using SM = TaskSmemF32<DIMS, TX>;
+  constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr bool TW = SCHEME == DOMA_SCHEME_TW_DD;
+  // TW-DD works with |mu|/dx, DD with 2|mu|/dx (the tables hold the latter)
+  constexpr float HS = TW ? 0.5f : 1.0f;
+  const int og = task.og;
+  const int o = task.oct;
+  const int of = task.grp * 8 + o;
+  const bool rx = (o & 4) != 0, ry = (o & 2) != 0, rz = (o & 1) != 0;
+  const int nx = A.nx, ny = A.ny, nz = DIMS == 3 ? A.nz : 1;
+  const size_t N = (size_t)nx * ny * nz;
+  const float * gq = A.q + (size_t)task.grp * N;
+  const float * gsig = A.sigt + (size_t)task.grp * N;
+  const int n0 = og * kGroup;
+  const int gs = min(kGroup, A.d_oct - n0);
+  const int i0 = task.bi * TX, j0 = task.bj * PY, k0 = task.bk * PZ;
+  const int vx = min(TX, nx - i0), vy = min(PY, ny - j0), vz = min(PZ, nz - k0);
+  const FacePlanes<float> F(A, of, og);
+  const size_t slot = F.plane;
+
+  const int t = threadIdx.x;
+  const int lane = t & 31;
+  const int p = lane & 15;
+  const int nl = (t >> 5) * 2 + (lane >> 4);
+  const int jl = DIMS == 3 ? (p & 3) : p;
+  const int kl = DIMS == 3 ? (p >> 2) : 0;
+  const bool active = nl < gs && jl < vy && kl < vz;
+  const int ob = A.oct_offset[o] + n0;
+  const int ord = ob + min(nl, gs - 1);
+
+  float * yin = reinterpret_cast<float *>(smem_raw);
+  float * zin = yin + SM::YF;
+  float2 * cell = reinterpret_cast<float2 *>(zin + SM::ZF);     // {q, sigma_t}
+  float * hxs = reinterpret_cast<float *>(cell + CELLS);         // [kGroup][TX]
+  float * rlx = hxs + kGroup * TX;                               // [TX] 1/dx
+  float * P = rlx + TX;                                          // [kGroup / 2][CELLS]
+
+  auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
+  auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
+  auto phys_k = [&](int kk) { return rz ? nz - 1 - (k0 + kk) : k0 + kk; };
+
+  // -- stage what does not depend on upstream blocks ----------------------------
+  {
+    constexpr int IT = (CELLS + kMaxSweepThreads - 1) / kMaxSweepThreads;
+    for (int base = 0; base < CELLS; base += IT * (int)blockDim.x) {
+      float2 v[IT];
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        const int e = base + t + u * (int)blockDim.x;
+        const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
+        v[u] = make_float2(0.f, 1.f);
+        if (e < CELLS && il < vx && jj < vy && kk < vz) {
+          const size_t c = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
+          v[u] = make_float2(gq[c], gsig[c]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < IT; ++u) {
+        const int e = base + t + u * (int)blockDim.x;
+        if (e < CELLS) cell[e] = v[u];
+      }
+    }
+  }
+  for (int e = t; e < kGroup * TX; e += blockDim.x) {
+    const int nn = e / TX, il = e % TX;
+    hxs[e] = (nn < gs && il < vx) ? fM(HS, A.cx[(size_t)(ob + nn) * nx + phys_i(il)]) : 0.f;
+  }
+  if (DIMS == 2 && TW)
+    for (int e = t; e < TX; e += blockDim.x) rlx[e] = e < vx ? __frcp_rn(A.wx[phys_i(e)]) : 0.f;
+  // per-thread constants of the pencil (clamped indices for inactive lanes)
+  const float cy_t = fM(HS, A.cy[(size_t)ord * ny + phys_j(min(jl, vy - 1))]);
+  const float cz_t = DIMS == 3 ? fM(HS, A.cz[(size_t)ord * nz + phys_k(min(kl, vz - 1))]) : 0.f;
+  const float cyz = fA(cy_t, cz_t);
+  const float wgt = (float)A.wgt[ord];
+  const float th = (float)A.theta, om = fS(1.0f, th);
+  // 2D TW-DD: theta |xi| / (dx dy) = txy / dx
+  const float txy = DIMS == 2 && TW ? fM(fM(th, A.axi_f[ord]), __frcp_rn(A.wy[phys_j(min(jl, vy - 1))])) : 0.f;
+
+  if (dataflow) wait_upstream<float, DIMS>(A, task, slot, epoch);
+
+  // -- incoming faces: every load issued before the first store ----------------------
+  {
+    constexpr int Y4 = SM::YF / 4, R4 = TX * kGroup / 4;   // float4s per block / per row
+    float xin_v = 0.f;
+    const size_t xslot = F.x(k0 + kl, j0 + jl) + nl;
+    if (active && task.bi > 0) xin_v = __ldcg(A.xf + xslot);
+    stage_f4<Y4>(reinterpret_cast<float4 *>(yin), [&](int e) {
+      const int kk = e / R4, r = e % R4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (task.bj > 0 && kk < vz && r / (kGroup / 4) < vx)
+        v = __ldcg(reinterpret_cast<const float4 *>(A.yf + F.y(k0 + kk, i0)) + r);
+      return v;
+    });
+    if constexpr (DIMS == 3)
+      stage_f4<SM::ZF / 4>(reinterpret_cast<float4 *>(zin), [&](int e) {
+        const int jj = e / R4, r = e % R4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (task.bk > 0 && jj < vy && r / (kGroup / 4) < vx)
+          v = __ldcg(reinterpret_cast<const float4 *>(A.zf + F.z(j0 + jj, i0)) + r);
+        return v;
+      });
+    __syncthreads();
+
+    // -- wavefront: step s solves the cells with il + jl + kl == s ---------------------
+    // Every lane runs every step (no divergence); steps outside the lane's
+    // pencil compute on clamped indices and keep nothing.  A lane's upwind
+    // neighbours are invalid exactly when it is, so no lane consumes a value
+    // from an invalid step.
+    const int d = jl + kl;
+    const int ebase = (kl * PY + jl) * TX;
+    const int ybase = kl * TX * kGroup + nl;
+    const int zbase = jl * TX * kGroup + nl;
+    const int hbase = nl * TX;
+    const bool ybound = active && jl == vy - 1;
+    const bool zbound = DIMS == 3 && active && kl == vz - 1;
+    float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
+    float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl : nullptr;
+    float * P_lane = P + (nl >> 1) * CELLS + ebase;
+    float x = xin_v, ysh = 0.f, zsh = 0.f;
+    constexpr int STEPS = TX + PY + PZ - 2;
+    // 3D: fully unrolled; 2D (long skew) partly, which keeps it out of local memory
+#pragma unroll (DIMS == 3 ? STEPS : 4)
+    for (int s = 0; s < STEPS; ++s) {
+      const int il = s - d;
+      const bool valid = active && (unsigned)il < (unsigned)vx;
+      const int ic = min(max(il, 0), TX - 1);
+      float y = jl == 0 ? yin[ybase + ic * kGroup] : ysh;
+      float z = DIMS == 3 ? (kl == 0 ? zin[zbase + ic * kGroup] : zsh) : 0.f;
+      const float2 qc = cell[ebase + ic];
+      const float hx = hxs[hbase + ic];
+      float xo = x, psi;
+      if constexpr (DIMS == 3) {
+        if constexpr (TW) psi = twdd3_fast(qc.x, qc.y, hx, cy_t, cz_t, th, om, xo, y, z);
+        else psi = dd3_fast(qc.x, qc.y, hx, cy_t, cz_t, cyz, xo, y, z);
+      } else {
+        if constexpr (TW) psi = twdd2_fast(qc.x, qc.y, hx, cy_t, fM(txy, rlx[ic]), th, om, xo, y);
+        else psi = dd2_fast(qc.x, qc.y, hx, cy_t, xo, y);
+      }
+      x = valid ? xo : x;
+      const float wp = valid ? fM(wgt, psi) : 0.f;
+      if (valid && ybound) yout_g[il * kGroup] = y;
+      if (DIMS == 3 && valid && zbound) zout_g[il * kGroup] = z;
+      // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
+      const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
+      if (valid && lane < 16) P_lane[il] = pair;
+      ysh = __shfl_up_sync(FULL, y, 1);
+      if (DIMS == 3) zsh = __shfl_up_sync(FULL, z, PY);
+    }
+    if (active) A.xf[xslot] = x;
+  }
+  __syncthreads();
+
+  // -- publish completion first: nothing downstream reads the scalar flux -------------
+  if (dataflow && t == 0) {
+    __threadfence();
+    st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
+  }
+
+  // -- the slot's scalar-flux partial: Kahan over ordinate pairs, fixed order ----------
+  for (int e = t; e < CELLS; e += blockDim.x) {
+    const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
+    if (il < vx && jj < vy && kk < vz) {
+      float sum = 0.0f, comp = 0.0f;
+      const int npairs = (gs + 1) >> 1;
+      for (int nn = 0; nn < npairs; ++nn) {
+        const float yv = fS(P[nn * CELLS + e], comp);
+        const float tv = fA(sum, yv);
+        comp = fS(fS(tv, sum), yv);
+        sum = tv;
+      }
+      const size_t cg = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
+      A.octphi[slot * N + cg] = (double)sum - (double)comp;
+    }
+  }
+}
+
+template <typename T, int DIMS, int SCHEME, int TX>
+__device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task,
+                                         unsigned char * smem_raw, bool dataflow, unsigned epoch)
+{
+  if constexpr (std::is_same<T, double>::value)
+    run_task_exact<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
+  else
+    run_task_f32<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
+}
+
+// Resident CTAs per SM the kernels are compiled for (caps the registers of
+// the single-precision body, whose unrolled wavefront would otherwise take
+// every register it can).
+template <typename T>
+constexpr int sweep_min_ctas()
+{
+  return std::is_same<T, double>::value ? 1 : DOMA_SWEEP_MIN_CTAS;
+}
+
+template <typename T, int DIMS, int TX>
+constexpr size_t task_smem_bytes()
+{
+  if constexpr (std::is_same<T, double>::value) return TaskSmemExact<DIMS, TX>::bytes;
+  else return TaskSmemF32<DIMS, TX>::bytes;
 }
 
 // Persistent dataflow sweep: CTAs claim tasks in topological order from a
 // ticket counter; a claimed task waits only on tasks with smaller tickets,
 // which running CTAs already hold, so progress never depends on residency.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads) sweep_persistent_kernel(const SweepArgs<T> A)
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>()) sweep_persistent_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_next;
@@ -580,7 +822,7 @@ __global__ void __launch_bounds__(kMaxSweepThreads) sweep_persistent_kernel(cons
 // every problem of a batch.  Tasks of problems that have converged publish
 // their done flag and return, so a batch keeps one static task list.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads)
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>())
     sweep_batch_kernel(const SweepArgs<T> * args, const BatchTask * tasks, int num_tasks,
                        unsigned * ticket, unsigned * exit_count, unsigned * epoch_ctr,
                        const BatchLoop * loops)
@@ -623,7 +865,7 @@ __global__ void __launch_bounds__(kMaxSweepThreads)
 
 // One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads) sweep_level_kernel(const SweepArgs<T> A)
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>()) sweep_level_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   run_task<T, DIMS, SCHEME, TX>(A, A.tasks[A.task_offset + blockIdx.x], smem_raw, false, 0u);
@@ -692,7 +934,7 @@ size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx)
 {
   return dispatch(dims, precision, scheme, tx, [](auto tag_t, auto dims_c, auto, auto tx_c) {
     using T = typename decltype(tag_t)::type;
-    return TaskSmem<T, decltype(dims_c)::value, decltype(tx_c)::value>::bytes;
+    return task_smem_bytes<T, decltype(dims_c)::value, decltype(tx_c)::value>();
   });
 }
 
