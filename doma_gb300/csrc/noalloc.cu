@@ -280,11 +280,10 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   const size_t o_cy = cv.take(sizeof(float) * (size_t)D * ny);
   const size_t o_cz = cv.take(sizeof(float) * (size_t)D * nz);
   const size_t o_wf = cv.take(sizeof(float) * (size_t)(nx + ny + nz));
-  // face planes: one 8-byte tagged word per face slot (padded ordinate groups)
-  const size_t slots = (size_t)ngroups * kGroup;
-  const size_t o_xf = cv.take(sizeof(unsigned long long) * 8 * (size_t)nz * ny * slots);
-  const size_t o_yf = cv.take(sizeof(unsigned long long) * 8 * (size_t)nz * nx * slots);
-  const size_t o_zf = cv.take(sizeof(unsigned long long) * 8 * (size_t)ny * nx * slots);
+  const size_t slots = (size_t)ngroups * kGroup;  // face slots per face (padded ordinate groups)
+  const size_t o_xf = cv.take(sizeof(float) * 8 * (size_t)nz * ny * slots);
+  const size_t o_yf = cv.take(sizeof(float) * 8 * (size_t)nz * nx * slots);
+  const size_t o_zf = cv.take(sizeof(float) * 8 * (size_t)ny * nx * slots);
   const size_t o_oct = cv.take(sizeof(double) * 8 * (size_t)ngroups * N);
   if (cv.off > (size_t)DOMA_NOALLOC_SCRATCH_BYTES)
     return fail("the no-alloc sweep needs " + std::to_string(cv.off) + " bytes of scratch; it has " +
@@ -303,8 +302,6 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   for (int a = 0; a < 4; ++a) std::memcpy(g_quad_flat + a * D, g_quad[a], sizeof(double) * D);
   DOMA_CUDA_TRY(cudaMemsetAsync(base + o_ctl, 0, sizeof(NoallocCtl), s));
   DOMA_CUDA_TRY(cudaMemsetAsync(base + o_done, 0, sizeof(unsigned) * 8 * (size_t)ngroups * nbx * nby * nbz, s));
-  // every call restarts the sweep epoch at 1: clear the tags the previous call left
-  DOMA_CUDA_TRY(cudaMemsetAsync(base + o_xf, 0, o_zf + sizeof(unsigned long long) * 8 * (size_t)ny * nx * slots - o_xf, s));
   DOMA_CUDA_TRY(cudaMemcpyAsync(base + o_tasks, g_tasks, sizeof(Task) * num_tasks, cudaMemcpyHostToDevice, s));
   DOMA_CUDA_TRY(cudaMemcpyAsync(base + o_offs, offs, sizeof(offs), cudaMemcpyHostToDevice, s));
   // (pageable sources: each copy has read its host buffer when it returns)

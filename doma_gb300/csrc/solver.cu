@@ -73,7 +73,6 @@ struct doma_solver {
   double *d_phi = nullptr, *d_prev = nullptr;
   void *d_q = nullptr, *d_sigt = nullptr;
   void *d_xf = nullptr, *d_yf = nullptr, *d_zf = nullptr;
-  size_t face_bytes = 0;   // the three face planes, contiguous from d_xf
   double * d_wpsi = nullptr;
   double * d_octphi = nullptr;
   void *d_wx = nullptr, *d_wy = nullptr, *d_wz = nullptr;   // widths, sweep precision
@@ -365,15 +364,10 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   unsigned char * fb = nullptr;
   const size_t xf = gif * 8 * (size_t)s->nz * s->ny * Do, yf = gif * 8 * (size_t)s->nz * s->nx * Do,
                zf = gif * 8 * (size_t)s->ny * s->nx * Do;
-  // 8 bytes per face slot in both precisions: a double, or (single
-  // precision) a float tagged with the epoch of the sweep that wrote it.
-  // Zeroed: no tag of a later sweep is 0.
-  DOMA_TRY(dalloc(s, &fb, (xf + yf + zf) * sizeof(double)));
-  DOMA_CUDA_TRY(cudaMemset(fb, 0, (xf + yf + zf) * sizeof(double)));
-  s->face_bytes = (xf + yf + zf) * sizeof(double);
+  DOMA_TRY(dalloc(s, &fb, (xf + yf + zf) * ts));
   s->d_xf = fb;
-  s->d_yf = fb + xf * sizeof(double);
-  s->d_zf = fb + (xf + yf) * sizeof(double);
+  s->d_yf = fb + xf * ts;
+  s->d_zf = fb + (xf + yf) * ts;
   if (exact)
     DOMA_TRY(dalloc(s, &s->d_wpsi, gif * N * (size_t)s->D));
   else
@@ -454,7 +448,7 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
     const char * wt = std::getenv("DOMA_SWEEP_WAIT_TEST");
     if (wt && std::string(wt) == "1") {
       a.spin_limit = 2000u;
-      a.wait_bias = 0x8000u;  // within the 16-bit epoch of the single-precision face tags
+      a.wait_bias = 0x40000000u;
     }
   };
   if (exact)
@@ -1501,13 +1495,8 @@ doma_status batch_sweep(doma_batch * b)
 
 doma_status batch_init_sources(doma_batch * b)
 {
-  for (auto * s : b->solvers) {
+  for (auto * s : b->solvers)
     DOMA_TRY(launch_mgi_init(s->it, DOMA_PREC_FP32, s->d_q, s->d_sigt, b->stream));
-    // A problem that finished early keeps its last face words while the batch
-    // epoch runs on; clearing them here means no stale tag can ever come round
-    // again once the 16-bit epoch of the face tags wraps.
-    DOMA_CUDA_TRY(cudaMemsetAsync(s->d_xf, 0, s->face_bytes, b->stream));
-  }
   std::vector<BatchLoop> loops(b->solvers.size(), BatchLoop{1u, 0u, 0u, 0u, 0.0});
   DOMA_CUDA_TRY(cudaMemcpyAsync(b->d_loops, loops.data(), loops.size() * sizeof(BatchLoop),
                                 cudaMemcpyHostToDevice, b->stream));

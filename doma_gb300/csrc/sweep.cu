@@ -41,7 +41,6 @@
 #include <type_traits>
 
 #include "common.cuh"
-#include "sweep_device.cuh"
 
 #ifndef DOMA_SWEEP_MIN_CTAS
 #define DOMA_SWEEP_MIN_CTAS 3
@@ -49,8 +48,6 @@
 
 namespace doma {
 namespace {
-
-using namespace sweep_dev;
 
 __device__ __forceinline__ double dA(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dS(double a, double b) { return __dsub_rn(a, b); }
@@ -162,6 +159,149 @@ __device__ __forceinline__ double twdd2_exact(double q, double st, double amu, d
   x = dS(dD(c, a), dM(dD(dS(1.0, a), a), xu));
   y = dS(dD(c, b), dM(dD(dS(1.0, b), b), yu));
   return c;
+}
+
+// ---- single-precision cell solves ------------------------------------------
+// Every operation is an explicit intrinsic (separately rounded add/mul, fused
+// multiply-add where written), so the compiler has no contraction choices and
+// the bits do not depend on which kernel the solve is inlined into.
+//
+// The cell balance is written divided by the cell volume, with the per-axis
+// streaming coefficients hx = |mu|/dx, hy = |eta|/dy, hz = |xi|/dz (DD uses
+// their doubles 2|mu|/dx, ...).  This is the same equation as DOMA's
+// (include/DiamondDifference3D.h:28-48, include/TWDiamondDifference3D.h:32-91),
+// rearranged so that the volume and face areas cancel.
+
+__device__ __forceinline__ float fA(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fS(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fM(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fF(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// One MUFU reciprocal (approximate, flush-to-zero; every argument here is a
+// normal number).
+__device__ __forceinline__ float rcp_approx(float a)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+
+// DD: psi = (q + cx x + cy y + cz z) / (cx + cy + cz + st), cyz = cy + cz.
+__device__ __forceinline__ float dd3_fast(float q, float st, float cx, float cy, float cz,
+                                          float cyz, float & x, float & y, float & z)
+{
+  const float num = fF(cz, z, fF(cy, y, fF(cx, x, q)));
+  const float c = fM(num, rcp_approx(fA(fA(cx, cyz), st)));
+  x = fF(2.0f, c, -x);
+  y = fF(2.0f, c, -y);
+  z = fF(2.0f, c, -z);
+  return c;
+}
+
+__device__ __forceinline__ float dd2_fast(float q, float st, float cx, float cy, float & x,
+                                          float & y)
+{
+  const float c = fM(fF(cy, y, fF(cx, x, q)), rcp_approx(fA(fA(cx, cy), st)));
+  x = fF(2.0f, c, -x);
+  y = fF(2.0f, c, -y);
+  return c;
+}
+
+// Reciprocal r = 1/a of one TW-DD axis weight.  DOMA's weight is
+// a = 1 - n / (D flux) when the upwind flux exceeds 1e-8 (else 0.5), clamped
+// to [0.5, 1] (include/TWDiamondDifference3D.h:43-75).  With Dx = D flux > 0,
+// 1/a = Dx / (Dx - n): a >= 1 <-> r <= 1, a in [0.5, 1] <-> r in [1, 2],
+// a < 0.5 (including a <= 0, Dx - n <= 0) <-> r = 2 after the clamp; the
+// floor 1e-30 on Dx - n sends a <= 0 to the r = 2 side.  r is clamped to
+// [1, 2] as 1 + sat(r - 1).
+__device__ __forceinline__ float tw_rweight(float n, float D, float flux)
+{
+  const float dx = fM(D, flux);
+  const float den = fmaxf(fS(dx, n), 1e-30f);
+  const float r = fA(1.0f, __saturatef(fF(dx, rcp_approx(den), -1.0f)));
+  return flux > 1e-8f ? r : 2.0f;
+}
+
+// TW-DD, volume-normalized.  With X = hx x, Y = hy y, Z = hz z and
+// B = theta (q + X + Y + Z), the weight numerators are B + (1 - theta) X etc.
+// and the denominators (st + 2 hy + 2 hz) x etc. (DOMA's, divided by V).
+// psi = (q + rx X + ry Y + rz Z) / (st + hx rx + hy ry + hz rz) and the
+// outgoing faces x' = (psi - (1 - a) x) / a = x + rx (psi - x).
+// sz = st + 2 hz and sy = st + 2 hy, syz = st + 2 hy + 2 hz.
+__device__ __forceinline__ float twdd3_fast(float q, float st, float hx, float hy, float hz,
+                                            float th, float om, float & x, float & y, float & z)
+{
+  const float X = fM(hx, x), Y = fM(hy, y), Z = fM(hz, z);
+  const float B = fF(th, fA(fA(X, Y), Z), fM(th, q));
+  const float h2x = fA(hx, hx), h2y = fA(hy, hy), h2z = fA(hz, hz);
+  const float ra = tw_rweight(fF(om, X, B), fA(fA(st, h2y), h2z), x);
+  const float rb = tw_rweight(fF(om, Y, B), fA(fA(st, h2z), h2x), y);
+  const float rc = tw_rweight(fF(om, Z, B), fA(fA(st, h2y), h2x), z);
+  const float num = fF(rc, Z, fF(rb, Y, fF(ra, X, q)));
+  const float den = fF(hz, rc, fF(hy, rb, fF(hx, ra, st)));
+  const float c = fM(num, rcp_approx(den));
+  x = fF(ra, fS(c, x), x);
+  y = fF(rb, fS(c, y), y);
+  z = fF(rc, fS(c, z), z);
+  return c;
+}
+
+// 2D TW-DD keeps DOMA's bare |xi| term in the y weight
+// (include/TWDiamondDifference2D.h:51), volume-normalized: theta |xi| / V,
+// passed in as txv.
+__device__ __forceinline__ float twdd2_fast(float q, float st, float hx, float hy, float txv,
+                                            float th, float om, float & x, float & y)
+{
+  const float X = fM(hx, x), Y = fM(hy, y);
+  const float B = fF(th, fA(X, Y), fM(th, q));
+  const float ra = tw_rweight(fF(om, X, B), fA(st, fA(hy, hy)), x);
+  const float rb = tw_rweight(fA(fF(om, Y, B), txv), fA(st, fA(hx, hx)), y);
+  const float num = fF(rb, Y, fF(ra, X, q));
+  const float den = fF(hy, rb, fF(hx, ra, st));
+  const float c = fM(num, rcp_approx(den));
+  x = fF(ra, fS(c, x), x);
+  y = fF(rb, fS(c, y), y);
+  return c;
+}
+
+// ---- scheduling primitives -------------------------------------------------
+
+__device__ __forceinline__ void st_release(unsigned * p, unsigned v)
+{
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned * p)
+{
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_relaxed(const int * p)
+{
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Wait until *flag == epoch.  Bounded: the first 32 polls are back to back,
+// then back-off of 32..128 ns; after `limit` polls it records
+// DOMA_DEVICE_WAIT_TIMEOUT in *error and returns false.  It also gives up at
+// once when another CTA has already failed.
+__device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, int * error)
+{
+  unsigned ns = 32;
+  for (unsigned it = 0; it < limit; ++it) {
+    if (ld_acquire(flag) == epoch) return true;
+    if (ld_relaxed(error) != 0) return false;
+    if (it >= 32) {
+      __nanosleep(ns);
+      if (ns < 128) ns *= 2;
+    }
+  }
+  atomicCAS(error, 0, (int)DOMA_DEVICE_WAIT_TIMEOUT);
+  return false;
 }
 
 // ---- one task: (octant, ordinate group, block) --------------------------------
@@ -416,6 +556,28 @@ struct TaskSmemF32 {
   static constexpr size_t bytes = floats * sizeof(float);
 };
 
+// Coalesced, all-loads-first copy of `count` float4s: in each round every
+// load of a thread is issued before its first shared-memory store, so the
+// round trips overlap.  A full-size CTA (kMaxSweepThreads) needs one round.
+template <int COUNT, typename L>
+__device__ __forceinline__ void stage_f4(float4 * dst, L load)
+{
+  constexpr int IT = (COUNT + kMaxSweepThreads - 1) / kMaxSweepThreads;
+  for (int base = 0; base < COUNT; base += IT * (int)blockDim.x) {
+    float4 v[IT];
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      const int e = base + (int)threadIdx.x + u * (int)blockDim.x;
+      v[u] = e < COUNT ? load(e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < IT; ++u) {
+      const int e = base + (int)threadIdx.x + u * (int)blockDim.x;
+      if (e < COUNT) dst[e] = v[u];
+    }
+  }
+}
+
 template <int DIMS, int SCHEME, int TX>
 __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const Task task,
                                              unsigned char * smem_raw, bool dataflow, unsigned epoch)
@@ -499,98 +661,29 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   // 2D TW-DD: theta |xi| / (dx dy) = txy / dx
   const float txy = DIMS == 2 && TW ? fM(fM(th, A.axi_f[ord]), __frcp_rn(A.wy[phys_j(min(jl, vy - 1))])) : 0.f;
 
-  unsigned long long * XW = reinterpret_cast<unsigned long long *>(A.xf);
-  unsigned long long * YW = reinterpret_cast<unsigned long long *>(A.yf);
-  unsigned long long * ZW = reinterpret_cast<unsigned long long *>(A.zf);
-  const unsigned want = epoch + A.wait_bias;
+  if (dataflow) wait_upstream<float, DIMS>(A, task, slot, epoch);
 
-  // -- wait: threads 0..DIMS-1 poll the done flags of the upstream blocks.  The
-  // flags are set without a fence, so they only say "about ready": every face
-  // word is then checked for its tag below.
-  if (dataflow) {
-    if (t < DIMS) {
-      const unsigned * f = nullptr;
-      if (t == 0 && task.bi > 0) f = done_flag(A, slot, task.bk, task.bj, task.bi - 1);
-      if (t == 1 && task.bj > 0) f = done_flag(A, slot, task.bk, task.bj - 1, task.bi);
-      if (t == 2 && task.bk > 0) f = done_flag(A, slot, task.bk - 1, task.bj, task.bi);
-      if (f) wait_flag_relaxed(f, want, A.spin_limit, A.error);
-    }
-    __syncthreads();
-  }
-
-  // -- incoming faces: all of a thread's words are loaded at once, and the ones
-  // whose tag is not yet the expected one are re-read together, round by round
-  // (bounded) ------------------------------------------------------------------------
+  // -- incoming faces: every load issued before the first store ----------------------
   {
-    constexpr int R2 = TX * kGroup / 2;   // 16-byte word pairs per face row
-    constexpr int IT = (SM::YF / 2 + kMaxSweepThreads - 1) / kMaxSweepThreads;
-    constexpr int NF = DIMS == 3 ? 2 : 1;  // y (and z) face blocks
+    constexpr int Y4 = SM::YF / 4, R4 = TX * kGroup / 4;   // float4s per block / per row
+    float xin_v = 0.f;
     const size_t xslot = F.x(k0 + kl, j0 + jl) + nl;
-    const bool xneed = active && task.bi > 0;
-    const unsigned xtag = face_tag(want, task.bi - 1);
-    const unsigned ftag[2] = {face_tag(want, task.bj - 1), face_tag(want, task.bk - 1)};
-    const bool present[2] = {task.bj > 0, task.bk > 0};
-    const int live[2] = {vz, vy};
-    unsigned long long xw = 0ull;
-    bool xfirst = true;
-    for (int base = 0; base < PZ * R2; base += IT * (int)blockDim.x) {
-      unsigned long long w[NF][IT][2];
-      bool in[NF][IT], need[NF][IT][2];
-      // word pair e of face block f (row rr = e / R2 of the block)
-      auto src = [&](int f, int e) {
-        const int rr = e / R2, r = e % R2;
-        return (f == 0 ? YW + F.y(k0 + rr, i0) : ZW + F.z(j0 + rr, i0)) + 2 * r;
-      };
-#pragma unroll
-      for (int f = 0; f < NF; ++f)
-#pragma unroll
-        for (int u = 0; u < IT; ++u) {
-          const int e = base + t + u * (int)blockDim.x;
-          const int rr = e / R2, r = e % R2, il = r / (kGroup / 2), nn = 2 * (r % (kGroup / 2));
-          in[f][u] = present[f] && e < PZ * R2 && rr < live[f] && il < vx;
-          need[f][u][0] = dataflow && in[f][u] && nn < gs;
-          need[f][u][1] = dataflow && in[f][u] && nn + 1 < gs;
-          w[f][u][0] = w[f][u][1] = 0ull;
-        }
-      bool pending = true;
-      for (unsigned it = 0; pending; ++it) {
-#pragma unroll
-        for (int f = 0; f < NF; ++f)
-#pragma unroll
-          for (int u = 0; u < IT; ++u)
-            if (in[f][u] && (it == 0 || need[f][u][0] || need[f][u][1]))
-              ld_tagged2(src(f, base + t + u * (int)blockDim.x), w[f][u][0], w[f][u][1]);
-        if (xneed && xfirst) xw = ld_tagged(XW + xslot);
-        pending = false;
-#pragma unroll
-        for (int f = 0; f < NF; ++f)
-#pragma unroll
-          for (int u = 0; u < IT; ++u)
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              need[f][u][h] = need[f][u][h] && tag_of(w[f][u][h]) != ftag[f];
-              pending |= need[f][u][h];
-            }
-        xfirst = xneed && dataflow && tag_of(xw) != xtag;
-        pending |= xfirst;
-        if (!pending) break;
-        if (it + 1 >= A.spin_limit) {
-          atomicCAS(A.error, 0, (int)DOMA_DEVICE_WAIT_TIMEOUT);
-          break;
-        }
-        if ((it & 15) == 15 && ld_relaxed(A.error) != 0) break;
-        if (it >= 2) __nanosleep(64);
-      }
-#pragma unroll
-      for (int f = 0; f < NF; ++f)
-#pragma unroll
-        for (int u = 0; u < IT; ++u) {
-          const int e = base + t + u * (int)blockDim.x;
-          if (e < PZ * R2)
-            reinterpret_cast<float2 *>(f == 0 ? yin : zin)[e] =
-                make_float2(value_of(w[f][u][0]), value_of(w[f][u][1]));
-        }
-    }
+    if (active && task.bi > 0) xin_v = __ldcg(A.xf + xslot);
+    stage_f4<Y4>(reinterpret_cast<float4 *>(yin), [&](int e) {
+      const int kk = e / R4, r = e % R4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (task.bj > 0 && kk < vz && r / (kGroup / 4) < vx)
+        v = __ldcg(reinterpret_cast<const float4 *>(A.yf + F.y(k0 + kk, i0)) + r);
+      return v;
+    });
+    if constexpr (DIMS == 3)
+      stage_f4<SM::ZF / 4>(reinterpret_cast<float4 *>(zin), [&](int e) {
+        const int jj = e / R4, r = e % R4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (task.bk > 0 && jj < vy && r / (kGroup / 4) < vx)
+          v = __ldcg(reinterpret_cast<const float4 *>(A.zf + F.z(j0 + jj, i0)) + r);
+        return v;
+      });
     __syncthreads();
 
     // -- wavefront: step s solves the cells with il + jl + kl == s ---------------------
@@ -605,11 +698,10 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const int hbase = nl * TX;
     const bool ybound = active && jl == vy - 1;
     const bool zbound = DIMS == 3 && active && kl == vz - 1;
-    unsigned long long * yout_g = YW + F.y(k0 + kl, i0) + nl;
-    unsigned long long * zout_g = DIMS == 3 ? ZW + F.z(j0 + jl, i0) + nl : nullptr;
+    float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
+    float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl : nullptr;
     float * P_lane = P + (nl >> 1) * CELLS + ebase;
-    float x = value_of(xw), ysh = 0.f, zsh = 0.f;
-    const unsigned ytag = face_tag(epoch, task.bj), ztag = face_tag(epoch, task.bk);
+    float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
     // 3D: fully unrolled; 2D (long skew) partly, which keeps it out of local memory
 #pragma unroll (DIMS == 3 ? STEPS : 4)
@@ -631,19 +723,23 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
       }
       x = valid ? xo : x;
       const float wp = valid ? fM(wgt, psi) : 0.f;
-      if (valid && ybound) st_tagged(yout_g + il * kGroup, y, ytag);
-      if (DIMS == 3 && valid && zbound) st_tagged(zout_g + il * kGroup, z, ztag);
+      if (valid && ybound) yout_g[il * kGroup] = y;
+      if (DIMS == 3 && valid && zbound) zout_g[il * kGroup] = z;
       // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
       const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
       if (valid && lane < 16) P_lane[il] = pair;
       ysh = __shfl_up_sync(FULL, y, 1);
       if (DIMS == 3) zsh = __shfl_up_sync(FULL, z, PY);
     }
-    if (active) st_tagged(XW + xslot, x, face_tag(epoch, task.bi));
+    if (active) A.xf[xslot] = x;
   }
-  // the angular reduction below reads every lane's pair sums
   __syncthreads();
-  if (dataflow && t == 0) st_relaxed(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
+
+  // -- publish completion first: nothing downstream reads the scalar flux -------------
+  if (dataflow && t == 0) {
+    __threadfence();
+    st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
+  }
 
   // -- the slot's scalar-flux partial: Kahan over ordinate pairs, fixed order ----------
   for (int e = t; e < CELLS; e += blockDim.x) {
@@ -675,11 +771,13 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 
 // Resident CTAs per SM the kernels are compiled for (caps the registers of
 // the single-precision body, whose unrolled wavefront would otherwise take
-// every register it can).
-template <typename T>
+// every register it can).  Measured on GB300 (64^3, 16 ordinates per
+// octant): DD is fastest with 4 CTAs per SM (64 registers), TW-DD, with more
+// live values per cell, with 3 (80 registers).
+template <typename T, int SCHEME>
 constexpr int sweep_min_ctas()
 {
-  return std::is_same<T, double>::value ? 1 : DOMA_SWEEP_MIN_CTAS;
+  return std::is_same<T, double>::value ? 1 : SCHEME == DOMA_SCHEME_DD ? 4 : DOMA_SWEEP_MIN_CTAS;
 }
 
 template <typename T, int DIMS, int TX>
@@ -693,7 +791,7 @@ constexpr size_t task_smem_bytes()
 // ticket counter; a claimed task waits only on tasks with smaller tickets,
 // which running CTAs already hold, so progress never depends on residency.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>()) sweep_persistent_kernel(const SweepArgs<T> A)
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>()) sweep_persistent_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_next;
@@ -726,7 +824,7 @@ __global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>()) sweep_p
 // every problem of a batch.  Tasks of problems that have converged publish
 // their done flag and return, so a batch keeps one static task list.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>())
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
     sweep_batch_kernel(const SweepArgs<T> * args, const BatchTask * tasks, int num_tasks,
                        unsigned * ticket, unsigned * exit_count, unsigned * epoch_ctr,
                        const BatchLoop * loops)
@@ -745,9 +843,12 @@ __global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>())
     const BatchTask bt = tasks[tk];
     const SweepArgs<T> & A = args[bt.prob];
     if (!loops[bt.prob].active) {  // uniform across the CTA: the flag changes between launches
-      // nothing waits on a finished problem's tasks (its downstream tasks
-      // skip too).  The claimer's write of s_next must be ordered before
-      // everyone's next read of it (run_task's barriers do this on the other path).
+      if (threadIdx.x == 0) {
+        const size_t slot = (size_t)(bt.t.grp * 8 + bt.t.oct) * A.ngroups + bt.t.og;
+        st_release(A.done + ((slot * A.nbz + bt.t.bk) * A.nby + bt.t.bj) * A.nbx + bt.t.bi, epoch);
+      }
+      // the claimer's write of s_next must be ordered before everyone's next
+      // read of it (run_task's barriers do this on the other path)
       __syncthreads();
       continue;
     }
@@ -766,7 +867,7 @@ __global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>())
 
 // One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T>()) sweep_level_kernel(const SweepArgs<T> A)
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>()) sweep_level_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   run_task<T, DIMS, SCHEME, TX>(A, A.tasks[A.task_offset + blockIdx.x], smem_raw, false, 0u);
