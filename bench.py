@@ -134,6 +134,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM traffic of one sweep launch on this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture of sweep_persistent_kernel, FP32
+# TW-DD, 64^3, 128 directions).  Far below the algorithmic bytes: the sweep's
+# working set stays in L2.
+SWEEP_DRAM_BYTES_PER_LAUNCH = 2_495_488 + 276_480
+
+
 def measured_peak_hbm():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -207,7 +214,7 @@ def learned_leg(args):
     for i in range(args.learned_problems):
         p = P.learned_problem(1_000_001 + i, n=args.learned_n, groups=8)
         t0 = time.perf_counter()
-        ref, info = E.reference_flux(p, tol=1e-10)
+        ref, info = E.reference_flux(p, tol=1e-9)
         ref_s = time.perf_counter() - t0
         plain = E.time_to_error(p, ref, args.learned_target, max_it=20000)
         lrn = E.time_to_error(p, ref, args.learned_target, net=net, first=args.accel_first,
@@ -349,9 +356,9 @@ def run_ours(args):
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, dt, upd = cpu_sample(p, options("fp64", args.tol), threads, args.ref_iters)
+        rate, dt, upd = cpu_sample(p, options("fp64", args.tol), threads, args.cpu_iters)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.ref_iters} source iterations of group 0 ({upd / 1e6:.1f} M updates, "
+               "sample": f"{args.cpu_iters} source iterations of group 0 ({upd / 1e6:.1f} M updates, "
                          f"{dt:.1f} s), {threads} OpenMP threads over ordinates"}
 
     learned = learned_leg(args) if args.learned_problems > 0 else None
@@ -371,7 +378,9 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": SWEEP_DRAM_BYTES_PER_LAUNCH if args.precision == "fp32" else None,
+                     "traffic_source": "ncu capture of one launch (dram__bytes_read + dram__bytes_write)",
                      "peak_source": peak_kind,
                      "bytes_per_update": b_upd, "sweep_ms": sweep_ms,
                      "sweep_launches": desc["launches_per_sweep"]},
@@ -397,14 +406,17 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--roofline-sweeps", type=int, default=50)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--ref-iters", type=int, default=3)
+    ap.add_argument("--ref-iters", type=int, default=30,
+                    help="source iterations of group 0 per --impl reference step")
+    ap.add_argument("--cpu-iters", type=int, default=300,
+                    help="source iterations of group 0 in the cpu_baseline sample (about 10 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-check", type=int, default=1)
     ap.add_argument("--learned-problems", type=int, default=1)
     ap.add_argument("--learned-n", type=int, default=64)
     ap.add_argument("--learned-target", type=float, default=1e-5)
-    ap.add_argument("--accel-first", type=int, default=3)
-    ap.add_argument("--accel-interval", type=int, default=3)
+    ap.add_argument("--accel-first", type=int, default=10)
+    ap.add_argument("--accel-interval", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

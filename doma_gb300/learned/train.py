@@ -48,9 +48,13 @@ def make_batch(ps: D.PairSet, gen: torch.Generator, batch: int):
 
 
 def train(ps: D.PairSet, steps: int = 4000, batch: int = 16, lr: float = 1e-3,
-          seed: int = 0, log_every: int = 200, log=print) -> tuple[UNet, list]:
+          seed: int = 0, log_every: int = 200, log=print, init=None) -> tuple[UNet, list]:
+    """Adam with a short warm-up and cosine decay; `init` (a weights file)
+    starts from trained weights instead of the seeded initialisation."""
     torch.cuda.synchronize()
     net = UNet(seed=seed)
+    if init is not None:
+        net.load(init)
     gen = torch.Generator().manual_seed(seed)
     history = []
     t0 = time.perf_counter()
@@ -80,6 +84,7 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--random-rounds", type=int, default=16)
+    ap.add_argument("--init", default=None, help="weights file to start from")
     ap.add_argument("--out", default="accel_weights.npz")
     a = ap.parse_args()
     torch.cuda.set_device(0)
@@ -92,7 +97,7 @@ def main():
         R, Z = D.generate_random([probs[i] for i in ps.kept], rounds=a.random_rounds, seed=a.seed)
         ps = D.PairSet(torch.cat([ps.R, R], dim=1), torch.cat([ps.Z, Z], dim=1), ps.F, ps.n,
                        ps.iterations, ps.seconds, ps.kept)
-    net, _ = train(ps, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed)
+    net, _ = train(ps, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed, init=a.init)
     net.save(a.out)
     print(f"weights written to {a.out}")
 
