@@ -102,3 +102,28 @@ def test_training_pairs_have_the_documented_structure():
     z0 = pairs.Z[:, :, 0].norm(dim=-1)
     assert torch.all(z0[:, 1:] < z0[:, :-1])
     assert torch.all(torch.isfinite(pairs.R)) and torch.all(torch.isfinite(pairs.Z))
+
+
+@pytest.mark.gpu
+def test_trained_network_cuts_the_iterations_to_tolerance():
+    """What the trained network gains: on a held-out problem (a seed outside
+    the training sets), plain FP32 multigroup iteration and the same
+    iteration with guarded corrections from the committed weights both stop at
+    1e-5 relative L2 error against an FP64 solution; the corrected one needs
+    far fewer iterations."""
+    from pathlib import Path
+
+    from doma_gb300.learned import evaluate as E
+    from doma_gb300.learned.net import UNet
+    weights = Path(__file__).resolve().parents[1] / "doma_gb300" / "learned" / "weights" / "unet_c32.npz"
+    p = P.learned_problem(900002, n=32, groups=4)
+    ref, _ = E.reference_flux(p, tol=1e-9)
+    plain = E.time_to_error(p, ref, 1e-5, max_it=20000, warm=False)
+    with UNet(seed=0) as net:
+        net.load(weights)
+        lrn = E.time_to_error(p, ref, 1e-5, net=net, first=2, interval=2, max_corrections=64,
+                              max_it=20000, warm=False)
+    assert plain["converged"] and lrn["converged"]
+    assert plain["error"] <= 1e-5 and lrn["error"] <= 1e-5
+    assert lrn["accepted"] > 0
+    assert lrn["iterations"] <= 0.5 * plain["iterations"], (plain["iterations"], lrn["iterations"])
