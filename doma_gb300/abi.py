@@ -132,6 +132,8 @@ SIGNATURES = {
     ),
     "doma_solver_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "doma_solver_solve_fixed_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport)]),
+    "doma_solver_solve_eigenvalue": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
+                                                    ctypes.POINTER(DomaReport), _dp]),
     "doma_solver_get_scalar_flux": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_size_t]),
     "doma_solver_source_iterations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
     "doma_solver_sweeps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),

@@ -132,6 +132,49 @@ __global__ void __launch_bounds__(kBlock) mg_source_kernel(const IterArgs A, int
   }
 }
 
+// k-eigenvalue mode, updateMultigroupSourceEigen (src/TransportSolver3D.cpp:404-430):
+// the in-scatter and fission / k terms are *added* to the current source,
+// which still holds the previous group's last increment source (DOMA does not
+// reset it there); the external source does not enter.  Same association as
+// DOMA: ((s S) phi) / pi and ((((s chi) nu_sigma_f) phi) / pi) / k.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) mg_source_eigen_kernel(const IterArgs A, int g, double k,
+                                                                 T * q, T * sigt_out)
+{
+  const size_t N = A.N;
+  const int G = A.G;
+  const double s = A.src_scale;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const unsigned m = A.mat[c];
+    double acc = (double)q[c];
+    const bool fis = A.fis && A.fis[m];
+    for (int gp = 0; gp < G; ++gp) {
+      const double pg = A.phi[(size_t)gp * N + c];
+      if (gp != g) acc = dA(acc, dD(dM(dM(s, A.scatter[((size_t)m * G + g) * G + gp]), pg), kPi));
+      if (fis)
+        acc = dA(acc, dD(dD(dM(dM(dM(s, A.chi[(size_t)m * G + g]), A.nsf[(size_t)m * G + gp]), pg),
+                            kPi), k));
+    }
+    q[c] = (T)acc;
+    sigt_out[c] = (T)A.total[(size_t)m * G + g];
+    A.prev[(size_t)g * N + c] = A.phi[(size_t)g * N + c];
+    A.phi[(size_t)g * N + c] = 0.0;
+  }
+}
+
+// k-eigenvalue mode, initializeSolve (src/TransportSolver3D.cpp:512-518): the
+// flux starts at 1 in every group, the previous iterate at 0.
+__global__ void __launch_bounds__(kBlock) eigen_init_kernel(const IterArgs A)
+{
+  const size_t n = A.N * (size_t)A.G;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    A.phi[i] = 1.0;
+    A.prev[i] = 0.0;
+  }
+}
+
 // The source-iteration epilogue for group g:
 //   dphi = sum of the swept angular flux (exact: all ordinates in DOMA's
 //          single-thread order; fp32: the (octant, ordinate group) partials in order)
@@ -457,6 +500,24 @@ doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q,
     mg_source_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, (double *)sigt, L);
   else
     mg_source_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, (float *)sigt, L);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k, void * q,
+                                   void * sigt, cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    mg_source_eigen_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, k, (double *)q, (double *)sigt);
+  else
+    mg_source_eigen_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, k, (float *)q, (float *)sigt);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_eigen_init(const IterArgs & a, cudaStream_t st)
+{
+  eigen_init_kernel<<<a.grid, kBlock, 0, st>>>(a);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }

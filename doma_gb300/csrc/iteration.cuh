@@ -77,6 +77,11 @@ doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q,
                              const LoopParams & L, cudaStream_t st);
 doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * q,
                                double * norms, const LoopParams & L, cudaStream_t st);
+// k-eigenvalue mode: group g's source added to the current one (in-scatter +
+// fission / k), and the starting flux (1 everywhere).
+doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k, void * q,
+                                   void * sigt, cudaStream_t st);
+doma_status launch_eigen_init(const IterArgs & a, cudaStream_t st);
 doma_status launch_mg_residual(const IterArgs & a, double * norms, const LoopParams & L,
                                cudaStream_t st);
 // Batched multigroup solve: per-problem data of the batched epilogue.

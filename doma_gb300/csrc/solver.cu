@@ -120,6 +120,16 @@ struct doma_solver {
   double * d_ref = nullptr;                                           // [G][N]
   double ref_norm2 = 0.0, ref_target = 0.0;
   doma_accel_stats stats{};
+
+  // k-eigenvalue mode: host copies of the flux and the previous iterate for
+  // the k update, which sums in DOMA's order (pinned, allocated on first use),
+  // and of the per-cell data that update reads
+  double *h_phi = nullptr, *h_prev = nullptr;
+  bool fissile = false;
+  std::vector<uint32_t> h_mat;   // [N]
+  std::vector<double> h_vol;     // [N] cell volume (area in 2D)
+  std::vector<uint8_t> h_fis;    // [M]
+  std::vector<double> h_nsf;     // [M][G]
 };
 
 namespace {
@@ -306,6 +316,15 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
     DOMA_TRY(upload(s, &s->d_chi, p->chi_p, M * G));
     DOMA_TRY(upload(s, &s->d_nsf, p->nu_sigma_f, M * G));
   }
+  s->h_mat.assign(p->cell_material, p->cell_material + N);
+  s->h_vol = vol;
+  s->h_fis.assign(M, 0u);
+  s->h_nsf.assign(M * G, 0.0);
+  if (p->has_fission) {
+    s->h_fis.assign(p->has_fission, p->has_fission + M);
+    s->h_nsf.assign(p->nu_sigma_f, p->nu_sigma_f + M * G);
+    for (size_t m = 0; m < M; ++m) s->fissile = s->fissile || s->h_fis[m] != 0u;
+  }
   DOMA_TRY(upload(s, &s->d_amu, amu.data(), (size_t)s->D));
   DOMA_TRY(upload(s, &s->d_aeta, aeta.data(), (size_t)s->D));
   DOMA_TRY(upload(s, &s->d_axi, axi.data(), (size_t)s->D));
@@ -481,6 +500,8 @@ void release(doma_solver * s)
   if (s->graph) cudaGraphDestroy(s->graph);
   for (void * p : s->allocations) cudaFree(p);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
+  if (s->h_phi) cudaFreeHost(s->h_phi);
+  if (s->h_prev) cudaFreeHost(s->h_prev);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
 }
@@ -1137,6 +1158,155 @@ doma_status solve_impl(doma_solver * s, doma_report * r)
   return status;
 }
 
+// ---- k-eigenvalue power iteration ------------------------------------------
+
+// updateEigenvalue (src/TransportSolver3D.cpp:432-456): num and den summed on
+// the host over cells in order, groups inner, cells without production
+// skipped -- DOMA's single-thread order, so k carries DOMA's bits.
+doma_status k_update(doma_solver * s, double k, double * k_new)
+{
+  const size_t G = s->G, N = s->N, bytes = G * N * sizeof(double);
+  if (!s->h_phi) {
+    DOMA_CUDA_TRY(cudaMallocHost(&s->h_phi, bytes));
+    DOMA_CUDA_TRY(cudaMallocHost(&s->h_prev, bytes));
+  }
+  DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_phi, s->d_phi, bytes, cudaMemcpyDeviceToHost, s->stream));
+  DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_prev, s->d_prev, bytes, cudaMemcpyDeviceToHost, s->stream));
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  double num = 0.0, den = 0.0;
+  for (size_t c = 0; c < N; ++c) {
+    const uint32_t m = s->h_mat[c];
+    if (!s->h_fis[m]) continue;
+    const double V = s->h_vol[c];
+    for (size_t g = 0; g < G; ++g) {
+      const double nsf = s->h_nsf[(size_t)m * G + g];
+      num = num + V * nsf * s->h_phi[g * N + c];
+      den = den + V * nsf * s->h_prev[g * N + c] / k;
+    }
+  }
+  *k_new = num / den;
+  return DOMA_OK;
+}
+
+// solveEigenvalue (src/TransportSolver3D.cpp:29-86; 2D :31-88), host-driven:
+// the group loop and source iterations are the fixed-source ones.
+doma_status solve_eigen_impl(doma_solver * s, double k_tol, doma_report * r, double * k_out)
+{
+  if (s->mgi) return bad("eigenvalue solves use Gauss-Seidel iteration");
+  if (!s->fissile) return bad("an eigenvalue solve needs a fissile material");
+  const doma_options & o = s->opts;
+  const int verbose = (int)o.verbose;
+  const size_t N = s->N;
+  const auto t0 = std::chrono::steady_clock::now();
+  const uint64_t launches0 = s->launches;
+  if (verbose) std::printf("Solving...\nInitializing the solver...\n");
+  DOMA_TRY(launch_eigen_init(s->it, s->stream));
+  ++s->launches;
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_q, 0, N * (o.precision == DOMA_PREC_FP64 ? 8 : 4), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
+
+  uint64_t sweeps = 0;
+  size_t si_len = 0;
+  unsigned mg = 0;
+  double k = 1.0, k_prev = 0.0, shape = 0.0, kdiff = 0.0, si_res = 0.0;
+  doma_status status = DOMA_OK;
+  do {
+    if (verbose) {
+      if (mg != 0u)
+        std::printf("Performing PI %u, shape residual = %g, k residual = %g\nk = %g\n", mg, shape,
+                    kdiff, k);
+      else
+        std::printf("Performing PI %u\n", mg);
+      std::printf("----------------------------------------------------------------------------------\n");
+    }
+    for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
+      DOMA_TRY(launch_mg_source_eigen(s->it, g, o.precision, k, s->d_q, s->d_sigt, s->stream));
+      ++s->launches;
+      unsigned it = 0;
+      si_res = 0.0;
+      do {
+        if (verbose >= 2) {
+          if (it != 0u)
+            std::printf("Performing SI %u for G%d, residual = %g\n", it, g, si_res);
+          else
+            std::printf("Performing SI %u for G%d\n", it, g);
+        }
+        DOMA_TRY(source_iteration(s, g));
+        ++sweeps;
+        double diff, tot;
+        DOMA_TRY(read_norms(s, 0, &diff, &tot));
+        if (!std::isfinite(diff) || !std::isfinite(tot)) {
+          set_error("source iteration norm is not finite (group " + std::to_string(g) + ")");
+          status = DOMA_NUMERIC_ERROR;
+          break;
+        }
+        si_res = ratio(diff, tot);
+        ++it;
+      } while (it < o.fs_max_it && o.fs_tol < si_res);
+      if (r && r->si_counts && si_len < r->si_counts_capacity) r->si_counts[si_len] = it;
+      ++si_len;
+      if (status != DOMA_OK) break;
+      if (it < o.fs_max_it) {
+        if (verbose)
+          std::printf("SI converged after %u iterations with a residual of %g for G%d\n", it,
+                      si_res, g);
+      } else {
+        if (verbose)
+          std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n",
+                      it, si_res, g);
+        status = DOMA_NOT_CONVERGED;  // solveEigenvalue returns false at once
+      }
+    }
+    if (status != DOMA_OK) break;
+    k_prev = k;
+    DOMA_TRY(k_update(s, k, &k));
+    DOMA_TRY(launch_mg_residual(s->it, s->d_ctl->norms + 2, LoopParams{}, s->stream));
+    ++s->launches;
+    double diff, tot;
+    DOMA_TRY(read_norms(s, 2, &diff, &tot));
+    if (!std::isfinite(diff) || !std::isfinite(tot) || !std::isfinite(k)) {
+      set_error("power iteration norm or k is not finite");
+      status = DOMA_NUMERIC_ERROR;
+      break;
+    }
+    shape = ratio(diff, tot);
+    kdiff = std::abs(k - k_prev);
+    ++mg;
+  } while (mg < o.mg_max_it && (o.mg_tol < shape || k_tol < kdiff));
+
+  if (status == DOMA_OK) {
+    if (mg < o.mg_max_it) {
+      if (verbose)
+        std::printf("PI converged after %u iterations with a flux shape residual of %g and a k "
+                    "residual of %g.\nConverged value of k = %g\n", mg, shape, kdiff, k);
+    } else {
+      if (verbose)
+        std::printf("PI failed to converge after %u iterations with a flux shape residual of %g "
+                    "and a k residual of %g.\n", mg, shape, kdiff);
+      status = DOMA_NOT_CONVERGED;
+      set_error("power iteration reached mg_max_it");
+    }
+  } else if (status == DOMA_NOT_CONVERGED) {
+    set_error("source iteration reached fs_max_it");
+  }
+  if (verbose) std::fflush(stdout);
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  const auto t1 = std::chrono::steady_clock::now();
+  if (k_out) *k_out = k;
+  if (r) {
+    r->status = status;
+    r->mg_iterations = mg;
+    r->si_iterations = sweeps;
+    r->updates = sweeps * (uint64_t)s->N * (uint64_t)s->D;
+    r->kernel_launches = s->launches - launches0;
+    r->mg_residual = shape;
+    r->si_residual = si_res;
+    r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    r->si_counts_len = si_len;
+  }
+  return status;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1198,6 +1368,14 @@ doma_status doma_solver_solve_fixed_source(doma_solver * s, doma_report * report
 {
   if (!s) return bad("null solver");
   return solve_impl(s, report);
+}
+
+doma_status doma_solver_solve_eigenvalue(doma_solver * s, double k_tol, doma_report * report,
+                                         double * k)
+{
+  if (!s) return bad("null solver");
+  if (!(k_tol >= 0.0)) return bad("k_tol must be >= 0");
+  return solve_eigen_impl(s, k_tol, report, k);
 }
 
 doma_status doma_solver_get_scalar_flux(doma_solver * s, double * out, size_t count)

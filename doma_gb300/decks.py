@@ -25,15 +25,18 @@ def _fmt_u(v) -> str:
 
 def deck_text(p: Problem, scheme: str = "dd", fs_tol: float = 1e-8, fs_max_it: int = 1000,
               mg_tol: float = 1e-8, mg_max_it: int = 100, theta: float | None = None,
-              precision: str | None = None) -> str:
+              precision: str | None = None, solve_type: str = "steady",
+              k_tol: float | None = None) -> str:
     G = p.num_groups
     extra = ""
+    if k_tol is not None:
+        extra += f' k_tol="{k_tol!r}"'
     if theta is not None:
         extra += f' theta="{theta!r}"'
     if precision is not None:
         extra += f' precision="{precision}"'
     lines = ["<doma_inp>",
-             f'  <solver solve_type="steady" scheme="{scheme}" num_groups="{G}" fs_tol="{fs_tol!r}"'
+             f'  <solver solve_type="{solve_type}" scheme="{scheme}" num_groups="{G}" fs_tol="{fs_tol!r}"'
              f' mg_tol="{mg_tol!r}" fs_max_it="{fs_max_it}" mg_max_it="{mg_max_it}"{extra}/>',
              f'  <angular_quad type="gc" np="{p.num_polar}" na="{p.num_azimuthal}"/>',
              f'  <mesh dims="{p.num_dims}" refinement="0">',

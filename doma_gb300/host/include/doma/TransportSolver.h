@@ -1,8 +1,8 @@
 // TransportSolver.h -- drop-in TransportSolver3D<T> / TransportSolver2D<T>
 // running DOMA's fixed-source path on the GPU.
 //
-// Same constructor, solveFixedSource signature, return convention and typedef
-// names as DOMA (DOMA include/TransportSolver3D.h:12-34,
+// Same constructor, solveFixedSource / solveEigenvalue signatures, return
+// convention and typedef names as DOMA (DOMA include/TransportSolver3D.h:12-34,
 // include/TransportSolver2D.h), so `DDTransportSolver3D s(mesh, params,
 // verbose, threads); s.solveFixedSource(base);` works unchanged.  T selects
 // the cell balance: DiamondDifference3D/2D or TWDiamondDifference3D/2D (the
@@ -11,13 +11,14 @@
 // in the GPU library).  Underneath, every call goes through the C ABI of
 // include/doma_gb300.h.
 //
-// Behaviour as in DOMA: solveFixedSource returns false when an iteration cap
-// is reached (the flux of the last iterate is kept in the mesh), prints
-// DOMA's progress lines (each SI residual too when verbose), writes the text
-// output when output_file_base is not empty and the solve converged.
+// Behaviour as in DOMA: the solves return false when an iteration cap is
+// reached (the flux of the last iterate is kept in the mesh), print DOMA's
+// progress lines (each SI residual too when verbose), write the text output
+// when output_file_base is not empty and the solve converged.  eigenvalue()
+// gives k after solveEigenvalue (DOMA keeps it private).
 // Differences: invalid input and CUDA failures throw std::runtime_error
 // instead of exiting; num_threads is accepted and unused (the device does
-// the work); the eigenvalue and transient drivers are not provided.
+// the work); the transient driver is not provided.
 #pragma once
 
 #include <cstdint>
@@ -63,15 +64,20 @@ public:
   TransportSolver3D & operator=(const TransportSolver3D &) = delete;
 
   bool solveFixedSource(const std::string & output_file_base = "", const double & t = 0.0);
+  bool solveEigenvalue(const std::string & output_file_base = "");
 
   const SolveStats & stats() const { return _stats; }
+  double eigenvalue() const { return _k; }
 
 private:
+  doma_solver * solver();
+
   BrickMesh3D & _mesh;
   const InputParameters & _params;
   const bool _verbose;
   doma_solver * _solver = nullptr;
   SolveStats _stats;
+  double _k = 1.0;
 };
 
 template <typename T>
@@ -90,15 +96,20 @@ public:
   TransportSolver2D & operator=(const TransportSolver2D &) = delete;
 
   bool solveFixedSource(const std::string & output_file_base = "", const double & t = 0.0);
+  bool solveEigenvalue(const std::string & output_file_base = "");
 
   const SolveStats & stats() const { return _stats; }
+  double eigenvalue() const { return _k; }
 
 private:
+  doma_solver * solver();
+
   BrickMesh2D & _mesh;
   const InputParameters & _params;
   const bool _verbose;
   doma_solver * _solver = nullptr;
   SolveStats _stats;
+  double _k = 1.0;
 };
 
 extern template class TransportSolver3D<DiamondDifference3D>;

@@ -23,8 +23,8 @@ struct ProblemData
 
 ProblemData gather(const InputParameters & params, const std::vector<unsigned int> & blocks)
 {
-  if (params._mode != RunMode::FixedSrc)
-    throw std::runtime_error("only fixed-source solves (solve_type=\"steady\") run on the GPU library");
+  if (params._mode == RunMode::Transient)
+    throw std::runtime_error("transient solves do not run on the GPU library (steady and eigen do)");
   const unsigned int G = params._num_e_groups;
   std::map<unsigned int, unsigned int> index;
   for (const auto & kv : params._block_mat_info) index.emplace(kv.first, 0u);
@@ -95,6 +95,9 @@ doma_solver * create(const doma_problem & p, const doma_options & o)
   return s;
 }
 
+void fill_stats(const doma_report & r, bool converged, std::vector<uint32_t> & counts,
+                SolveStats & stats);
+
 bool run(doma_solver * s, size_t flux_values, std::vector<double> & flux, SolveStats & stats)
 {
   std::vector<uint32_t> counts(1u << 16);
@@ -107,7 +110,14 @@ bool run(doma_solver * s, size_t flux_values, std::vector<double> & flux, SolveS
   flux.resize(flux_values);
   if (doma_solver_get_scalar_flux(s, flux.data(), flux.size()) != DOMA_OK)
     throw std::runtime_error(std::string("reading the scalar flux failed: ") + doma_last_error());
-  stats.converged = st == DOMA_OK;
+  fill_stats(r, st == DOMA_OK, counts, stats);
+  return stats.converged;
+}
+
+void fill_stats(const doma_report & r, bool converged, std::vector<uint32_t> & counts,
+                SolveStats & stats)
+{
+  stats.converged = converged;
   stats.mg_iterations = r.mg_iterations;
   stats.source_iterations = r.si_iterations;
   stats.updates = r.updates;
@@ -116,6 +126,24 @@ bool run(doma_solver * s, size_t flux_values, std::vector<double> & flux, SolveS
   stats.solve_ms = r.solve_ms;
   counts.resize(std::min(r.si_counts_len, counts.size()));
   stats.si_counts = counts;
+}
+
+// DOMA's solveEigenvalue through the C ABI; k_tol from the deck
+// (InputParameters::_k_tol).
+bool run_eigen(doma_solver * s, double k_tol, size_t flux_values, std::vector<double> & flux,
+               SolveStats & stats, double & k)
+{
+  std::vector<uint32_t> counts(1u << 16);
+  doma_report r{};
+  r.si_counts = counts.data();
+  r.si_counts_capacity = counts.size();
+  const doma_status st = doma_solver_solve_eigenvalue(s, k_tol, &r, &k);
+  if (st != DOMA_OK && st != DOMA_NOT_CONVERGED)
+    throw std::runtime_error(std::string("eigenvalue solve failed: ") + doma_last_error());
+  flux.resize(flux_values);
+  if (doma_solver_get_scalar_flux(s, flux.data(), flux.size()) != DOMA_OK)
+    throw std::runtime_error(std::string("reading the scalar flux failed: ") + doma_last_error());
+  fill_stats(r, st == DOMA_OK, counts, stats);
   return stats.converged;
 }
 
@@ -138,7 +166,7 @@ TransportSolver3D<T>::~TransportSolver3D()
 }
 
 template <typename T>
-bool TransportSolver3D<T>::solveFixedSource(const std::string & output_file_base, const double & /*t*/)
+doma_solver * TransportSolver3D<T>::solver()
 {
   if (!_solver) {
     const ProblemData d = gather(_params, _mesh.cellBlocks());
@@ -164,7 +192,22 @@ bool TransportSolver3D<T>::solveFixedSource(const std::string & output_file_base
     const doma_options o = make_options(_params, T::scheme, _verbose);
     _solver = create(p, o);
   }
-  const bool ok = run(_solver, _mesh._flux.size(), _mesh._flux, _stats);
+  return _solver;
+}
+
+template <typename T>
+bool TransportSolver3D<T>::solveFixedSource(const std::string & output_file_base, const double & /*t*/)
+{
+  const bool ok = run(solver(), _mesh._flux.size(), _mesh._flux, _stats);
+  if (ok && output_file_base != "") _mesh.dumpToTextFile(output_file_base);
+  return ok;
+}
+
+// DOMA's TransportSolver3D::solveEigenvalue (src/TransportSolver3D.cpp:29-86).
+template <typename T>
+bool TransportSolver3D<T>::solveEigenvalue(const std::string & output_file_base)
+{
+  const bool ok = run_eigen(solver(), _params._k_tol, _mesh._flux.size(), _mesh._flux, _stats, _k);
   if (ok && output_file_base != "") _mesh.dumpToTextFile(output_file_base);
   return ok;
 }
@@ -186,7 +229,7 @@ TransportSolver2D<T>::~TransportSolver2D()
 }
 
 template <typename T>
-bool TransportSolver2D<T>::solveFixedSource(const std::string & output_file_base, const double & /*t*/)
+doma_solver * TransportSolver2D<T>::solver()
 {
   if (!_solver) {
     const ProblemData d = gather(_params, _mesh.cellBlocks());
@@ -213,7 +256,22 @@ bool TransportSolver2D<T>::solveFixedSource(const std::string & output_file_base
     const doma_options o = make_options(_params, T::scheme, _verbose);
     _solver = create(p, o);
   }
-  const bool ok = run(_solver, _mesh._flux.size(), _mesh._flux, _stats);
+  return _solver;
+}
+
+template <typename T>
+bool TransportSolver2D<T>::solveFixedSource(const std::string & output_file_base, const double & /*t*/)
+{
+  const bool ok = run(solver(), _mesh._flux.size(), _mesh._flux, _stats);
+  if (ok && output_file_base != "") _mesh.dumpToTextFile(output_file_base);
+  return ok;
+}
+
+// DOMA's TransportSolver2D::solveEigenvalue (src/TransportSolver2D.cpp:31-88).
+template <typename T>
+bool TransportSolver2D<T>::solveEigenvalue(const std::string & output_file_base)
+{
+  const bool ok = run_eigen(solver(), _params._k_tol, _mesh._flux.size(), _mesh._flux, _stats, _k);
   if (ok && output_file_base != "") _mesh.dumpToTextFile(output_file_base);
   return ok;
 }

@@ -369,11 +369,13 @@ def streaming_duct(seed: int = 0, n: int = 100, np_: int = 6, na: int = 6, width
 
 def random_problem(seed: int = 0, dims: int = 3, nx: int = 5, ny: int = 4, nz: int = 3,
                    groups: int = 3, np_: int = 1, na: int = 1, materials: int = 3,
-                   fission: bool = False, upscatter: bool = True) -> Problem:
+                   fission: bool = False, upscatter: bool = True,
+                   fission_scale: float = 1.0) -> Problem:
     """Small irregular problem for unit tests: non-uniform widths in
     U[0.3, 1.5] cm, random materials, dense scattering (upscatter included
     when asked) with c ~ U[0.1, 0.9], a source in every other material and,
-    optionally, prompt fission in material 0."""
+    optionally, prompt fission in material 0 (nu sigma_f ~ U[0.01, 0.1] times
+    fission_scale)."""
     r = Rng(seed, f"random_problem_{dims}")
     G, M = groups, materials
     if dims == 2:
@@ -404,7 +406,7 @@ def random_problem(seed: int = 0, dims: int = 3, nx: int = 5, ny: int = 4, nz: i
         chi[0] = r.uniform(G, 0.0, 1.0)
         chi[0] /= chi[0].sum()
         nsf = np.zeros((M, G))
-        nsf[0] = r.uniform(G, 0.01, 0.1)
+        nsf[0] = r.uniform(G, 0.01, 0.1) * fission_scale
     return Problem(dims, dx, dy, dz, mat, sig, S, src, np_, na, has_fission=hf, chi_p=chi,
                    nu_sigma_f=nsf, name=f"random{dims}d_{nx}x{ny}x{nz}_g{G}_s{seed}")
 

@@ -84,6 +84,24 @@ class Solver:
                       si_residual=rep.si_residual, solve_ms=rep.solve_ms,
                       si_counts=counts[:n].copy())
 
+    def solve_eigenvalue(self, k_tol: float = 1e-5, si_capacity: int = 1 << 16) -> tuple[Report, float]:
+        """k-eigenvalue power iteration (DOMA's solveEigenvalue) -> (report, k).
+        report.mg_iterations counts power iterations."""
+        counts = np.zeros(si_capacity, dtype=np.uint32)
+        rep = abi.DomaReport()
+        rep.si_counts = counts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        rep.si_counts_capacity = si_capacity
+        k = ctypes.c_double(0.0)
+        st = self.lib.doma_solver_solve_eigenvalue(self._h, k_tol, ctypes.byref(rep), ctypes.byref(k))
+        abi.check(st, "doma_solver_solve_eigenvalue", self.lib,
+                  allow=(abi.DOMA_OK, abi.DOMA_NOT_CONVERGED))
+        n = min(rep.si_counts_len, si_capacity)
+        return (Report(converged=st == abi.DOMA_OK, status=st, mg_iterations=rep.mg_iterations,
+                       si_iterations=rep.si_iterations, updates=rep.updates,
+                       kernel_launches=rep.kernel_launches, mg_residual=rep.mg_residual,
+                       si_residual=rep.si_residual, solve_ms=rep.solve_ms,
+                       si_counts=counts[:n].copy()), float(k.value))
+
     def scalar_flux(self) -> np.ndarray:
         p = self.problem
         out = np.empty((p.num_groups, p.num_cells), dtype=np.float64)

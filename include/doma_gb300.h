@@ -19,6 +19,11 @@
  *   doma_solver_solve_fixed_source     TransportSolver3D<T>::solveFixedSource
  *                                      (src/TransportSolver3D.cpp:262-316) and the
  *                                      2D twin (src/TransportSolver2D.cpp:264-316)
+ *   doma_solver_solve_eigenvalue       TransportSolver3D<T>::solveEigenvalue
+ *                                      (src/TransportSolver3D.cpp:29-86, with
+ *                                      updateMultigroupSourceEigen / updateEigenvalue
+ *                                      :404-456) and the 2D twin
+ *                                      (src/TransportSolver2D.cpp:31-88, :406-456)
  *   doma_solver_get_scalar_flux        read-back of CartesianCell3D::_total_scalar_flux
  *                                      (include/CartesianCell3D.h:99), as used by
  *                                      BrickMesh3D::dumpToTextFile / fluxAtPoint
@@ -168,6 +173,19 @@ doma_status doma_solver_set_stream(doma_solver *solver, void *stream);
  * Returns DOMA_OK, or DOMA_NOT_CONVERGED when an iteration cap was hit (the
  * flux of the last iterate is kept, as in the reference). */
 doma_status doma_solver_solve_fixed_source(doma_solver *solver, doma_report *report);
+
+/* k-eigenvalue power iteration.  Gauss-Seidel over groups with a source
+ * iteration per group, as in the fixed-source solve, but the group source is
+ * in-scatter plus fission divided by k (no external source), the flux starts
+ * at 1 everywhere, and after each pass k is updated from the ratio of
+ * volume-weighted production sums.  Stops when opts.mg_max_it passes are done,
+ * or when both the flux-shape residual <= opts.mg_tol and |k - k_prev| <= k_tol.
+ * report->mg_iterations counts the passes (power iterations) and
+ * report->mg_residual is the last shape residual; *k gets the last k.
+ * Returns DOMA_OK, or DOMA_NOT_CONVERGED when a cap was reached (DOMA's
+ * false).  Gauss-Seidel iteration mode only. */
+doma_status doma_solver_solve_eigenvalue(doma_solver *solver, double k_tol, doma_report *report,
+                                         double *k);
 
 /* Copy the scalar flux to host memory: out[g*N + cell], N = nx*ny*nz. */
 doma_status doma_solver_get_scalar_flux(doma_solver *solver, double *out, size_t count);

@@ -530,6 +530,103 @@ int oracle_solve(const doma_problem *p, const doma_options *o, uint32_t num_thre
   return ok;
 }
 
+/* ------------------------------------------------------------------------ */
+/* k-eigenvalue power iteration: TransportSolver3D::solveEigenvalue
+ * (src/TransportSolver3D.cpp:29-86; 2D: src/TransportSolver2D.cpp:31-88).
+ * The flux starts at 1 in every group (initializeSolve, :512-515).  The
+ * group source (updateMultigroupSourceEigen, :404-430) is *added* to the
+ * current iteration source, which still holds the previous group's last
+ * scattering-increment source -- the reference never resets it there. */
+static void mg_source_eigen(oracle_state *s, unsigned g, double k)
+{
+  const doma_problem *p = s->p;
+  const unsigned G = s->G;
+  const double a = s->src_scale;
+  #pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < s->N; ++c) {
+    const unsigned m = p->cell_material[c];
+    s->cur[c] = 0.0;
+    double q = s->q[c];
+    const int fis = p->has_fission && p->has_fission[m];
+    for (unsigned gp = 0; gp < G; ++gp) {
+      if (gp != g)
+        q += a * p->scatter[((size_t)m * G + g) * G + gp] * s->phi[(size_t)gp * s->N + c] / M_PI;
+      if (fis)
+        q += a * p->chi_p[(size_t)m * G + g] * p->nu_sigma_f[(size_t)m * G + gp] *
+             s->phi[(size_t)gp * s->N + c] / M_PI / k;
+    }
+    s->q[c] = q;
+    s->prev[(size_t)g * s->N + c] = s->phi[(size_t)g * s->N + c];
+    s->phi[(size_t)g * s->N + c] = 0.0;
+    s->sigt[c] = p->total[(size_t)m * G + g];
+  }
+}
+
+/* updateEigenvalue (src/TransportSolver3D.cpp:432-456): cells in order,
+ * groups inner, cells without a production cross section skipped. */
+static double k_update(oracle_state *s, double k)
+{
+  const doma_problem *p = s->p;
+  const unsigned G = s->G;
+  double num = 0.0, den = 0.0;
+  for (size_t c = 0; c < s->N; ++c) {
+    const unsigned m = p->cell_material[c];
+    if (!(p->has_fission && p->has_fission[m])) continue;
+    for (unsigned g = 0; g < G; ++g) {
+      num = num + s->vol[c] * p->nu_sigma_f[(size_t)m * G + g] * s->phi[(size_t)g * s->N + c];
+      den = den + s->vol[c] * p->nu_sigma_f[(size_t)m * G + g] * s->prev[(size_t)g * s->N + c] / k;
+    }
+  }
+  return num / den;
+}
+
+int oracle_solve_eigen(const doma_problem *p, const doma_options *o, double k_tol,
+                       uint32_t num_threads, double *phi_out, double *k_out,
+                       uint32_t *si_counts, size_t si_cap, size_t *si_len,
+                       uint32_t *pi_iterations, double *shape_res_out, double *k_res_out)
+{
+  oracle_state s;
+  const unsigned T = num_threads ? num_threads : 1;
+  omp_set_num_threads((int)T);
+  if (state_init(&s, p, o, T)) { state_free(&s); return -1; }
+  for (size_t i = 0; i < s.N * s.G; ++i) s.phi[i] = 1.0;
+  size_t nsi = 0;
+  int ok = 1;
+  unsigned mg = 0;
+  double k = 1.0, k_prev = 0.0, shape = 0.0, kdiff = 0.0;
+  do {
+    for (unsigned g = 0; g < s.G && ok; ++g) {
+      mg_source_eigen(&s, g, k);
+      unsigned it = 0;
+      double res = 0.0;
+      do {
+        sweep(&s);
+        res = si_residual(&s, g);
+        si_update(&s, g);
+        ++it;
+      } while (it < o->fs_max_it && o->fs_tol < res);
+      if (si_counts && nsi < si_cap) si_counts[nsi] = it;
+      ++nsi;
+      if (!(it < o->fs_max_it)) ok = 0;
+    }
+    if (!ok) break;   /* solveEigenvalue returns false at once */
+    k_prev = k;
+    k = k_update(&s, k);
+    shape = mg_residual(&s);
+    kdiff = fabs(k - k_prev);
+    ++mg;
+  } while (mg < o->mg_max_it && (o->mg_tol < shape || k_tol < kdiff));
+  if (ok && !(mg < o->mg_max_it)) ok = 0;
+  memcpy(phi_out, s.phi, sizeof(double) * s.N * s.G);
+  if (k_out) *k_out = k;
+  if (si_len) *si_len = nsi;
+  if (pi_iterations) *pi_iterations = mg;
+  if (shape_res_out) *shape_res_out = shape;
+  if (k_res_out) *k_res_out = kdiff;
+  state_free(&s);
+  return ok;
+}
+
 int oracle_source_iterations(const doma_problem *p, const doma_options *o,
                              uint32_t num_threads, uint32_t group, uint32_t count,
                              double *phi_out, double *residuals)

@@ -32,6 +32,16 @@ int oracle_solve(const doma_problem *p, const doma_options *o, uint32_t num_thre
                  double *phi_out, uint32_t *si_counts, size_t si_cap, size_t *si_len,
                  uint32_t *mg_iterations, double *mg_residual);
 
+/* k-eigenvalue power iteration (DOMA's solveEigenvalue): Gauss-Seidel over
+ * groups with source iteration, fission source / k, k from the production
+ * ratio; stops when mg_max_it is reached or both the flux-shape residual
+ * (<= mg_tol) and |k - k_prev| (<= k_tol) have converged.  phi_out: [G][N];
+ * *k_out the last k.  Returns 1 converged, 0 a cap reached, -1 bad input. */
+int oracle_solve_eigen(const doma_problem *p, const doma_options *o, double k_tol,
+                       uint32_t num_threads, double *phi_out, double *k_out,
+                       uint32_t *si_counts, size_t si_cap, size_t *si_len,
+                       uint32_t *pi_iterations, double *shape_res_out, double *k_res_out);
+
 /* From a zero flux: set up group g's source, then run `count` source
  * iterations (sweep, residual, update) with no convergence test.  phi_out
  * ([G][N]) gets the flux afterwards; residuals ([count]) the SI residuals.

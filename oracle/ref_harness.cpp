@@ -1,6 +1,6 @@
 // ref_harness.cpp -- test infrastructure only.
 //
-// Drives DOMA's own fixed-source solver (the reference, compiled from its
+// Drives DOMA's own fixed-source and eigenvalue solvers (the reference, compiled from its
 // unmodified sources by oracle/Makefile into oracle/_ref/libdoma_ref.so) from
 // a doma_problem description, so that the CPU restatement in oracle/ and the
 // GPU library can be pinned against the reference itself.  The product never
@@ -181,6 +181,71 @@ ref_solve(const doma_problem * p, const doma_options * o, unsigned int num_threa
     }
     TransportSolver2D<OracleTap>::readFlux(mesh, p->num_groups, phi_out);
   }
+  std::cout.rdbuf(old);
+  copyLog(captured.str(), log, log_cap);
+  return ok ? 1 : 0;
+}
+
+// Eigenvalue solve with the reference (solveEigenvalue,
+// src/TransportSolver3D.cpp:29-86).  precision > 0 sets std::cout's precision
+// for the captured log first, so that the k and residuals it prints can be
+// read back exactly; 0 keeps the stream default (the reference's own log).
+int
+ref_solve_eigen(const doma_problem * p, const doma_options * o, double k_tol,
+                unsigned int num_threads, int precision, double * phi_out, char * log,
+                std::size_t log_cap)
+{
+  omp_set_num_threads(static_cast<int>(num_threads));
+  InputParameters params = makeParams(p, o);
+  params._mode = RunMode::Eigen;
+  params._k_tol = k_tol;
+  const bool verbose = o->verbose >= 2;
+
+  std::ostringstream captured;
+  if (precision > 0)
+    captured.precision(precision);
+  std::streambuf * old = std::cout.rdbuf(captured.rdbuf());
+  const std::streamsize old_precision = std::cout.precision();
+  if (precision > 0)
+    std::cout.precision(precision);
+  bool ok = false;
+  if (p->num_dims == 3)
+  {
+    std::array<BoundaryCondition, 6u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh3D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver3D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveEigenvalue("");
+    }
+    else
+    {
+      TWDDTransportSolver3D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveEigenvalue("");
+    }
+    TransportSolver3D<OracleTap>::readFlux(mesh, p->num_groups, phi_out);
+  }
+  else
+  {
+    std::array<BoundaryCondition, 4u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh2D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver2D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveEigenvalue("");
+    }
+    else
+    {
+      TWDDTransportSolver2D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveEigenvalue("");
+    }
+    TransportSolver2D<OracleTap>::readFlux(mesh, p->num_groups, phi_out);
+  }
+  std::cout.precision(old_precision);
   std::cout.rdbuf(old);
   copyLog(captured.str(), log, log_cap);
   return ok ? 1 : 0;

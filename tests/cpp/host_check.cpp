@@ -104,18 +104,24 @@ int main(int argc, char ** argv)
         const bool verbose = argc > 4 && std::string(argv[4]) == "verbose";
         bool ok;
         SolveStats st;
+        const bool eigen = p._mode == RunMode::Eigen;
+        double k = 0.0;
         if (p._eq_type == EquationType::DD) {
           DDTransportSolver3D s(mesh, p, verbose, 1);
-          ok = s.solveFixedSource();
+          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
+          k = s.eigenvalue();
         } else {
           TWDDTransportSolver3D s(mesh, p, verbose, 1);
-          ok = s.solveFixedSource();
+          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
+          k = s.eigenvalue();
         }
         write_bin(argv[3], mesh.scalarFlux());
+        char kbuf[64];
+        std::snprintf(kbuf, sizeof kbuf, "%.17g", k);
         std::cout << "{\"converged\": " << (ok ? "true" : "false") << ", \"mg\": " << st.mg_iterations
-                  << ", \"si_counts\": ";
+                  << ", \"k\": " << kbuf << ", \"si_counts\": ";
         json_list(st.si_counts);
         std::cout << "}" << std::endl;
         return 0;
@@ -141,18 +147,24 @@ int main(int argc, char ** argv)
         const bool verbose = argc > 4 && std::string(argv[4]) == "verbose";
         bool ok;
         SolveStats st;
+        const bool eigen = p._mode == RunMode::Eigen;
+        double k = 0.0;
         if (p._eq_type == EquationType::DD) {
           DDTransportSolver2D s(mesh, p, verbose, 1);
-          ok = s.solveFixedSource();
+          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
+          k = s.eigenvalue();
         } else {
           TWDDTransportSolver2D s(mesh, p, verbose, 1);
-          ok = s.solveFixedSource();
+          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
+          k = s.eigenvalue();
         }
         write_bin(argv[3], mesh.scalarFlux());
+        char kbuf[64];
+        std::snprintf(kbuf, sizeof kbuf, "%.17g", k);
         std::cout << "{\"converged\": " << (ok ? "true" : "false") << ", \"mg\": " << st.mg_iterations
-                  << ", \"si_counts\": ";
+                  << ", \"k\": " << kbuf << ", \"si_counts\": ";
         json_list(st.si_counts);
         std::cout << "}" << std::endl;
         return 0;

@@ -3,7 +3,8 @@
 Run from the repository root where the DOMA source tree is present:
 
     make -C oracle ref        # builds oracle/_ref/libdoma_ref.so from DOMA's sources
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py --eigen    # the k-eigenvalue fixtures only
 
 Each case is a seeded synthetic problem (doma_gb300.problems) solved by DOMA
 (single thread, the bit-reproducible order).  A fixture stores the generator
@@ -71,8 +72,30 @@ CASES = {
                      {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-12, "mg_max_it": 2}),
 }
 
+# k-eigenvalue cases: name -> (generator, kwargs, options kwargs, k_tol).  DOMA's
+# solveEigenvalue is run twice: with the stream's default precision (the log a
+# user sees) and with 17 digits (the exact k it prints).
+_FIS3 = {"seed": 11, "dims": 3, "nx": 7, "ny": 6, "nz": 5, "groups": 3, "np_": 2, "na": 2,
+         "materials": 4, "fission": True, "fission_scale": 10.0}
+_FIS2 = {"seed": 12, "dims": 2, "nx": 9, "ny": 7, "groups": 3, "np_": 2, "na": 3,
+         "materials": 3, "fission": True, "fission_scale": 10.0}
+EIGEN_CASES = {
+    "eigen3d_dd": ("random_problem", _FIS3,
+                   {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-7, "mg_max_it": 400}, 1e-8),
+    "eigen3d_twdd": ("random_problem", _FIS3,
+                     {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-9, "mg_tol": 1e-7,
+                      "mg_max_it": 400}, 1e-8),
+    "eigen2d_dd": ("random_problem", _FIS2,
+                   {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-7, "mg_max_it": 400}, 1e-8),
+    "eigen2d_twdd": ("random_problem", _FIS2,
+                     {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-9, "mg_tol": 1e-7,
+                      "mg_max_it": 400}, 1e-8),
+    "eigen_capped_dd": ("random_problem", _FIS3,
+                        {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-7, "mg_max_it": 4}, 1e-8),
+}
+
 # cases whose --verbose output (every SI residual) is also recorded
-VERBOSE_LOGS = {"capped_mg_dd", "capped_si_twdd", "random2d_dd"}
+VERBOSE_LOGS = {"capped_mg_dd", "capped_si_twdd", "random2d_dd", "eigen_capped_dd"}
 
 QUAD_SETS = [(dims, np_, na) for dims in (2, 3)
              for (np_, na) in [(1, 1), (2, 2), (3, 3), (4, 4), (6, 6), (2, 5), (5, 2)]]
@@ -82,9 +105,34 @@ def make_problem(gen: str, kwargs: dict) -> P.Problem:
     return getattr(P, gen)(**kwargs)
 
 
+def make_eigen() -> None:
+    for name, (gen, kw, okw, k_tol) in EIGEN_CASES.items():
+        p = make_problem(gen, kw)
+        opts = P.make_options(**okw)
+        t0 = time.time()
+        phi, ok, si, pi, _, log = ol.ref_solve_eigen(p, opts, k_tol, threads=1)
+        dt = time.time() - t0
+        phi17, _, _, _, k17, log17 = ol.ref_solve_eigen(p, opts, k_tol, threads=1, precision=17)
+        assert np.array_equal(phi, phi17)
+        if k17 is None:  # not converged: the last k printed is the one before the last pass
+            k17 = float(log17.rsplit("k = ", 1)[-1].split()[0]) if "k = " in log17 else None
+        meta = {"generator": gen, "kwargs": kw, "options": okw, "k_tol": k_tol,
+                "digest": p.digest(), "converged": ok, "pi_iterations": pi, "k": k17,
+                "k_is_final": bool(ok), "reference_seconds": round(dt, 3), "log": log}
+        if name in VERBOSE_LOGS:
+            vopts = P.make_options(**okw, verbose=2)
+            meta["log_verbose"] = ol.ref_solve_eigen(p, vopts, k_tol, threads=1)[5]
+        np.savez_compressed(HERE / f"{name}.npz", phi=phi, si_counts=si,
+                            meta=np.array(json.dumps(meta)))
+        print(f"{name:28s} converged={ok} pi={pi} k={k17} {dt:.2f}s")
+
+
 def main() -> None:
     if not ol.ref_available():
         raise SystemExit("oracle/_ref/libdoma_ref.so is missing: run `make -C oracle ref` first")
+    if "--eigen" in sys.argv:
+        make_eigen()
+        return
     quad = {}
     for dims, np_, na in QUAD_SETS:
         mu, eta, xi, w, counts = ol.ref_quadrature(np_, na, dims)
@@ -110,6 +158,7 @@ def main() -> None:
                             meta=np.array(json.dumps(meta)))
         print(f"{name:28s} converged={ok} mg={mg} si={list(map(int, si))[:8]}... "
               f"{dt:.2f}s")
+    make_eigen()
 
 
 if __name__ == "__main__":

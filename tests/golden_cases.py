@@ -12,7 +12,29 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def case_names():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "quadrature")
+    """The fixed-source fixtures."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz")
+                  if p.stem != "quadrature" and not p.stem.startswith("eigen"))
+
+
+def eigen_case_names():
+    """The k-eigenvalue fixtures."""
+    return sorted(p.stem for p in GOLDEN.glob("eigen*.npz"))
+
+
+def load_eigen_case(name: str):
+    """-> (problem, options, k_tol, expected dict)"""
+    z = np.load(GOLDEN / f"{name}.npz")
+    meta = json.loads(str(z["meta"]))
+    p = getattr(P, meta["generator"])(**meta["kwargs"])
+    if p.digest() != meta["digest"]:
+        raise AssertionError(f"{name}: regenerated inputs differ from the fixture's")
+    opts = P.make_options(**meta["options"])
+    exp = {"phi": z["phi"], "si_counts": z["si_counts"], "converged": meta["converged"],
+           "pi_iterations": meta["pi_iterations"], "k": meta["k"],
+           "k_is_final": meta["k_is_final"], "log": meta["log"],
+           "log_verbose": meta.get("log_verbose")}
+    return p, opts, meta["k_tol"], exp
 
 
 def load_case(name: str):

@@ -53,6 +53,12 @@ def oracle() -> ctypes.CDLL:
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
             ctypes.c_uint32, ctypes.c_uint32, _dp, _dp,
         ]
+        lib.oracle_solve_eigen.restype = ctypes.c_int
+        lib.oracle_solve_eigen.argtypes = [
+            ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_double,
+            ctypes.c_uint32, _dp, _dp, _u32p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+            _u32p, _dp, _dp,
+        ]
         lib.oracle_multigroup_solve.restype = ctypes.c_int
         lib.oracle_multigroup_solve.argtypes = [
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
@@ -74,6 +80,11 @@ def ref() -> ctypes.CDLL:
         lib.ref_solve.argtypes = [
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
             _dp, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p,
+        ]
+        lib.ref_solve_eigen.restype = ctypes.c_int
+        lib.ref_solve_eigen.argtypes = [
+            ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_double,
+            ctypes.c_uint32, ctypes.c_int, _dp, ctypes.c_char_p, ctypes.c_size_t,
         ]
         lib.ref_quadrature.restype = ctypes.c_int
         lib.ref_quadrature.argtypes = [ctypes.c_uint32] * 3 + [_dp] * 4 + [_u32p]
@@ -159,3 +170,45 @@ def ref_solve(p: Problem, opts: abi.DomaOptions, threads: int = 1, out_base: str
     si = np.array([int(m) for m in _SI_RE.findall(log)], dtype=np.uint32)
     mg = _MG_RE.findall(log)
     return phi, bool(rc), si, (int(mg[-1]) if mg else None), log
+
+
+def oracle_solve_eigen(p: Problem, opts: abi.DomaOptions, k_tol: float, threads: int = 1):
+    """-> (phi[G][N], k, converged, si_counts, pi_iterations, shape_residual, k_residual)"""
+    phi = np.zeros((p.num_groups, p.num_cells))
+    k = ctypes.c_double(0)
+    cap = 1 << 16
+    si = np.zeros(cap, dtype=np.uint32)
+    n_si = ctypes.c_size_t(0)
+    pi = ctypes.c_uint32(0)
+    shape = ctypes.c_double(0)
+    kres = ctypes.c_double(0)
+    cp = p.to_c()
+    rc = oracle().oracle_solve_eigen(ctypes.byref(cp), ctypes.byref(opts), k_tol, threads,
+                                     phi.ctypes.data_as(_dp), ctypes.byref(k),
+                                     si.ctypes.data_as(_u32p), cap, ctypes.byref(n_si),
+                                     ctypes.byref(pi), ctypes.byref(shape), ctypes.byref(kres))
+    if rc < 0:
+        raise ValueError("oracle rejected the problem")
+    return (phi, float(k.value), bool(rc), si[: min(n_si.value, cap)].copy(), int(pi.value),
+            float(shape.value), float(kres.value))
+
+
+_PI_RE = re.compile(r"PI (?:converged|failed to converge) after (\d+) iterations")
+_K_RE = re.compile(r"Converged value of k = (\S+)")
+
+
+def ref_solve_eigen(p: Problem, opts: abi.DomaOptions, k_tol: float, threads: int = 1,
+                    precision: int = 0):
+    """Run DOMA's solveEigenvalue.  -> (phi[G][N], converged, si_counts, pi_iterations or
+    None, k or None, log).  With precision=17 the printed k is exact."""
+    phi = np.zeros((p.num_groups, p.num_cells))
+    cap = 1 << 22
+    buf = ctypes.create_string_buffer(cap)
+    cp = p.to_c()
+    rc = ref().ref_solve_eigen(ctypes.byref(cp), ctypes.byref(opts), k_tol, threads, precision,
+                               phi.ctypes.data_as(_dp), buf, cap)
+    log = buf.value.decode()
+    si = np.array([int(m) for m in _SI_RE.findall(log)], dtype=np.uint32)
+    pi = _PI_RE.findall(log)
+    k = _K_RE.findall(log)
+    return (phi, bool(rc), si, (int(pi[-1]) if pi else None), (float(k[-1]) if k else None), log)

@@ -13,7 +13,7 @@ import pytest
 import oracle_lib as ol
 from doma_gb300 import problems as P
 from doma_gb300.solver import Solver, quadrature
-from golden_cases import case_names, load_case, quadrature_sets
+from golden_cases import case_names, load_case, quadrature_sets, eigen_case_names, load_eigen_case
 
 pytestmark = pytest.mark.gpu
 
@@ -283,3 +283,62 @@ def test_multigroup_cap_is_reported():
     opts = P.make_options(fs_tol=1e-14, fs_max_it=4, iteration="multigroup")
     phi, rep = run(p, opts)
     assert not rep.converged and rep.status == 1 and rep.mg_iterations == 4
+
+
+# ---- k-eigenvalue power iteration ------------------------------------------------
+
+def run_eigen(p, opts, k_tol):
+    with Solver(p, opts) as s:
+        rep, k = s.solve_eigenvalue(k_tol)
+        return s.scalar_flux(), rep, k
+
+
+@pytest.mark.parametrize("name", eigen_case_names())
+def test_fp64_eigenvalue_matches_reference_golden(name):
+    """DOMA's solveEigenvalue: same return value, power-iteration and SI
+    counts, k and flux (the contract is 1e-12 relative; the host-side k update
+    sums in DOMA's order, so both come out bit-equal)."""
+    p, opts, k_tol, exp = load_eigen_case(name)
+    phi, rep, k = run_eigen(p, opts, k_tol)
+    assert rep.converged == exp["converged"]
+    assert rep.mg_iterations == exp["pi_iterations"]
+    assert list(rep.si_counts) == list(exp["si_counts"])
+    if exp["k_is_final"]:
+        assert abs(k - exp["k"]) <= 1e-12 * abs(exp["k"])
+    assert rel_linf(phi, exp["phi"]) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("name", eigen_case_names())
+def test_eigenvalue_progress_lines_match_reference(capfd, name):
+    """The PI / SI progress lines of solveEigenvalue, line for line."""
+    p, opts, k_tol, exp = load_eigen_case(name)
+    opts.verbose = 1
+    capfd.readouterr()
+    run_eigen(p, opts, k_tol)
+    assert capfd.readouterr().out == exp["log"]
+    if exp["log_verbose"] is not None:
+        opts.verbose = 2
+        run_eigen(p, opts, k_tol)
+        assert capfd.readouterr().out == exp["log_verbose"]
+
+
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+def test_fp32_eigenvalue_against_fp64(scheme):
+    """The FP32 sweep in the power iteration: k within 1e-5 and the flux within
+    1e-4 (relative L2) of the FP64 mode's."""
+    p, _, k_tol, _ = load_eigen_case("eigen3d_dd")
+    kw = dict(scheme=scheme, theta=0.9, fs_tol=1e-7, mg_tol=1e-6, mg_max_it=400)
+    phi64, rep64, k64 = run_eigen(p, P.make_options(precision="fp64", **kw), 1e-7)
+    phi32, rep32, k32 = run_eigen(p, P.make_options(precision="fp32", **kw), 1e-7)
+    assert rep64.converged and rep32.converged
+    assert abs(k32 - k64) <= 1e-5 * k64
+    assert np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64) <= 1e-4
+
+
+def test_eigenvalue_needs_fission_and_gauss_seidel():
+    """Input errors come back as DOMA_BAD_INPUT (checked before any GPU work)."""
+    from doma_gb300 import abi
+    p = P.random_problem(3, 3, 4, 4, 4, groups=2)  # no fissile material
+    with Solver(p, P.make_options()) as s:
+        with pytest.raises(abi.DomaError, match="fissile"):
+            s.solve_eigenvalue(1e-6)

@@ -142,3 +142,40 @@ def test_cli_writes_reference_layout(tmp_path):
     for g in range(2):
         vals = np.array([float(x) for x in (tmp_path / f"cube_g{g}_flux.txt").read_text().split()])
         assert np.allclose(vals, o_phi[g], rtol=6e-6, atol=0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,scheme", [(3, "dd"), (2, "tw_dd")])
+def test_dropin_eigenvalue_matches_oracle(host_check, tmp_path, dims, scheme):
+    """TransportSolver3D/2D::solveEigenvalue on an eigenvalue deck (k_tol read
+    from the deck) against the CPU restatement of DOMA's power iteration."""
+    p = P.random_problem(13, dims, 7, 6, 5, groups=2, np_=2, na=2, materials=3, fission=True,
+                         fission_scale=8.0)
+    deck = write_deck(p, tmp_path / "e.xml", scheme=scheme, fs_tol=1e-10, mg_tol=1e-6,
+                      mg_max_it=400, solve_type="eigen", k_tol=1e-7)
+    d = json.loads(run(host_check, "solve", deck, tmp_path / "phi.bin").stdout.splitlines()[-1])
+    phi = np.fromfile(tmp_path / "phi.bin").reshape(p.num_groups, p.num_cells)
+    opts = P.make_options(scheme=scheme, fs_tol=1e-10, mg_tol=1e-6, mg_max_it=400)
+    o_phi, k, ok, si, pi, _, _ = ol.oracle_solve_eigen(p, opts, 1e-7)
+    assert d["converged"] == ok and d["mg"] == pi and d["si_counts"] == list(map(int, si))
+    assert abs(d["k"] - k) <= 1e-12 * k
+    assert np.abs(phi - o_phi).max() <= 1e-12 * np.abs(o_phi).max()
+
+
+@pytest.mark.gpu
+def test_cli_runs_eigenvalue_decks(tmp_path):
+    if not nb.CLI.exists():
+        nb.build()
+    p = P.random_problem(14, 3, 6, 6, 6, groups=2, np_=1, na=2, materials=3, fission=True,
+                         fission_scale=8.0)
+    deck = write_deck(p, tmp_path / "core.xml", scheme="dd", mg_tol=1e-5, mg_max_it=400,
+                      solve_type="eigen", k_tol=1e-6)
+    r = subprocess.run([str(nb.CLI), "-i", str(deck)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "Eigenvalue solver finished executing." in r.stdout
+    assert "Converged value of k = " in r.stdout and "Time elapsed:" in r.stdout
+    _, k, ok, *_ = ol.oracle_solve_eigen(p, P.make_options(scheme="dd", mg_tol=1e-5, mg_max_it=400),
+                                         1e-6)
+    assert ok
+    assert f"Converged value of k = {k:g}" in r.stdout
+    assert (tmp_path / "core_g1_flux.txt").exists()

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as ol
-from golden_cases import case_names, load_case, quadrature_sets
+from golden_cases import case_names, eigen_case_names, load_case, load_eigen_case, quadrature_sets
 
 
 @pytest.mark.parametrize("dims,np_,na,mu,eta,xi,w,counts", quadrature_sets())
@@ -47,3 +47,17 @@ def test_oracle_rejects_bad_input():
     p.cell_material[0] = 99
     with pytest.raises(ValueError):
         ol.oracle_solve(p, P.make_options())
+
+
+@pytest.mark.parametrize("name", eigen_case_names())
+def test_oracle_eigenvalue_bitwise_equals_reference(name):
+    """k-eigenvalue power iteration: flux, k, power-iteration and SI counts
+    exactly as DOMA's solveEigenvalue produced them."""
+    p, opts, k_tol, exp = load_eigen_case(name)
+    phi, k, ok, si, pi, _, _ = ol.oracle_solve_eigen(p, opts, k_tol, threads=1)
+    assert ok == exp["converged"]
+    assert pi == exp["pi_iterations"]
+    assert list(si) == list(exp["si_counts"])
+    if exp["k_is_final"]:
+        assert k == exp["k"]
+    assert np.array_equal(phi, exp["phi"]), np.abs(phi - exp["phi"]).max()
