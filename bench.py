@@ -22,6 +22,8 @@ fluxes and every norm in FP64.
   roofline  the sweep kernels alone (bare sweeps of group 0), achieved
             algorithmic bytes (6 s + 3 s / D_oct per update, s = 4) per second
             against the measured HBM copy bandwidth.
+  roofline_all_groups  the same kernel with all 8 groups in flight in one
+            launch (the multigroup iteration's sweep), same byte count.
   cpu_baseline  the CPU restatement of DOMA's OpenMP sweep (oracle/) on the
             host cores, a bounded sample of source iterations of group 0.
 
@@ -242,6 +244,7 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
+    from doma_gb300 import problems as P
     from doma_gb300.solver import Solver
 
     rank, world, local = dist_env()
@@ -316,6 +319,29 @@ def run_ours(args):
     peak, peak_kind = measured_peak_hbm()
     solver.close()
 
+    # -- the same sweep kernel with every group of the problem in flight (the
+    # multigroup iteration's sweep: one persistent launch over G groups) ----------
+    roof_all = None
+    if args.all_groups_roofline:
+        mg_opts = P.make_options(scheme="tw_dd", theta=0.7, precision=args.precision, fs_tol=args.tol,
+                                 fs_max_it=5000, iteration="multigroup")
+        with Solver(p, mg_opts) as smg:
+            smg.set_stream(stream.cuda_stream)
+            smg.source_iterations(0, 1)
+            smg.sweeps(0, 3)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            smg.sweeps(0, nsw)
+            e1.record(stream)
+            e1.synchronize()
+            mg_ms = e0.elapsed_time(e1) / nsw
+        mg_achieved = b_upd * upd_sweep * p.num_groups / (mg_ms / 1e3) / 1e9
+        roof_all = {"bound": "hbm", "achieved": mg_achieved, "peak": peak, "unit": "GB/s",
+                    "frac": mg_achieved / peak, "sweep_ms": mg_ms, "groups_in_flight": p.num_groups,
+                    "gupdates": upd_sweep * p.num_groups / (mg_ms / 1e3) / 1e9}
+
     # -- FP64 drop-in reference solution and its rate ----------------------------
     err = None
     fp64_rate = None
@@ -384,6 +410,7 @@ def run_ours(args):
                      "peak_source": peak_kind,
                      "bytes_per_update": b_upd, "sweep_ms": sweep_ms,
                      "sweep_launches": desc["launches_per_sweep"]},
+        "roofline_all_groups": roof_all,
         "cpu_baseline": cpu,
         "learned": learned,
         "gpu_launches": launches,
@@ -412,6 +439,8 @@ def main():
                     help="source iterations of group 0 in the cpu_baseline sample (about 10 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-check", type=int, default=1)
+    ap.add_argument("--all-groups-roofline", type=int, default=1,
+                    help="also time the sweep with every group in flight (multigroup mode)")
     ap.add_argument("--learned-problems", type=int, default=1)
     ap.add_argument("--learned-n", type=int, default=64)
     ap.add_argument("--learned-target", type=float, default=1e-5)
