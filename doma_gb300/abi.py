@@ -73,6 +73,34 @@ class DomaProblem(ctypes.Structure):
     ]
 
 
+class DomaTransient(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_double),
+        ("num_steps", ctypes.c_uint32),
+        ("num_d_groups", ctypes.c_uint32),
+        ("inv_v", ctypes.POINTER(ctypes.c_double)),
+        ("d_groups", ctypes.POINTER(ctypes.c_uint32)),
+        ("chi_d", ctypes.POINTER(ctypes.c_double)),
+        ("beta", ctypes.POINTER(ctypes.c_double)),
+        ("lambda_", ctypes.POINTER(ctypes.c_double)),
+        ("step_type", ctypes.POINTER(ctypes.c_uint32)),
+        ("step_insert", ctypes.POINTER(ctypes.c_double)),
+        ("step_remove", ctypes.POINTER(ctypes.c_double)),
+        ("step_source", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+DOMA_STEP_NONE = 0
+DOMA_STEP_BOTH = 1
+DOMA_STEP_INSERT = 2
+DOMA_STEP_REMOVE = 3
+
+# int (*doma_step_callback)(void *user, uint32_t step, double t, const double *phi,
+#                           const double *dnps)
+StepCallback = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_double,
+                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double))
+
+
 class DomaOptions(ctypes.Structure):
     _fields_ = [
         ("scheme", ctypes.c_uint32),
@@ -134,6 +162,9 @@ SIGNATURES = {
     "doma_solver_solve_fixed_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport)]),
     "doma_solver_solve_eigenvalue": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double,
                                                     ctypes.POINTER(DomaReport), _dp]),
+    "doma_solver_solve_transient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaTransient),
+                                                   StepCallback, ctypes.c_void_p,
+                                                   ctypes.POINTER(DomaReport)]),
     "doma_solver_get_scalar_flux": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_size_t]),
     "doma_solver_source_iterations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
     "doma_solver_sweeps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),

@@ -175,6 +175,106 @@ __global__ void __launch_bounds__(kBlock) eigen_init_kernel(const IterArgs A)
   }
 }
 
+// Transient mode, updateMultigroupSource with RunMode::Transient
+// (src/TransportSolver3D.cpp:339-402; 2D: src/TransportSolver2D.cpp): the
+// external source plus a source step that is on at t, then per source group
+// g': in-scatter, prompt fission (scaled by 1 - sum_d beta when the material
+// has delayed groups), the delayed-neutron source and the previous step's
+// flux term.  The last two sit inside the g' loop in DOMA, so each is added G
+// times; that is kept.  DOMA's association: (((s chi_d) C_d) lambda_d) / pi
+// and ((((s phi_last) inv_v) / dt) / pi).  In 2D the cell solves use
+// sigma_t + inv_v / dt (DiamondDifference2D.h:22-25); the 3D ones do not.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) mg_source_transient_kernel(const IterArgs A,
+                                                                     const TransientArgs X, int g,
+                                                                     T * q_out, T * sigt_out,
+                                                                     const LoopParams L)
+{
+  if (L.graph) {
+    const bool stop = L.ctl->failed != 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (!stop) L.ctl->si_it = 0u;
+      cudaGraphSetConditional(L.si_handle, stop ? 0u : 1u);
+    }
+    if (stop) return;
+  }
+  const size_t N = A.N;
+  const int G = A.G, D = X.D;
+  const double s = A.src_scale;
+  const double t = X.clock[0], dt = X.clock[1];
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const unsigned m = A.mat[c];
+    const size_t mg = (size_t)m * G + g;
+    double q = A.source ? dD(dM(s, A.source[mg]), kPi) : 0.0;
+    const unsigned st = X.step_type ? X.step_type[m] : 0u;
+    if (st != 0u) {
+      const double ins = X.step_insert[m], rem = X.step_remove[m];
+      const bool on = st == 1u ? (ins <= t && t <= rem) : (st == 2u ? ins <= t : t <= rem);
+      q = dA(q, on ? dD(dM(s, X.step_source[mg]), kPi) : 0.0);
+    }
+    const bool fis = A.fis && A.fis[m];
+    const unsigned Dm = X.dg ? X.dg[m] : 0u;
+    const double inv_v = X.inv_v[mg];
+    const double last = X.last[(size_t)g * N + c];
+    for (int gp = 0; gp < G; ++gp) {
+      const double pg = A.phi[(size_t)gp * N + c];
+      const size_t mgp = (size_t)m * G + gp;
+      if (gp != g) q = dA(q, dD(dM(dM(s, A.scatter[mg * G + gp]), pg), kPi));
+      if (fis && Dm == 0u) {
+        q = dA(q, dD(dM(dM(dM(s, A.chi[mg]), A.nsf[mgp]), pg), kPi));
+      } else if (fis) {
+        double gb = 0.0;
+        for (unsigned d = 0; d < Dm; ++d) gb = dA(gb, X.beta[mgp * D + d]);
+        q = dA(q, dD(dM(dM(dM(dM(s, dS(1.0, gb)), A.chi[mg]), A.nsf[mgp]), pg), kPi));
+      }
+      for (unsigned d = 0; d < Dm; ++d)
+        q = dA(q, dD(dM(dM(dM(s, X.chi_d[mg * D + d]), X.dnps[(size_t)d * N + c]),
+                        X.lambda[(size_t)m * D + d]), kPi));
+      q = dA(q, dD(dD(dM(dM(s, last), inv_v), dt), kPi));
+    }
+    q_out[c] = (T)q;
+    sigt_out[c] = (T)(X.dims2 ? dA(A.total[mg], dD(inv_v, dt)) : A.total[mg]);
+    A.prev[(size_t)g * N + c] = A.phi[(size_t)g * N + c];
+    A.phi[(size_t)g * N + c] = 0.0;
+  }
+}
+
+// stepDNPs (src/TransportSolver3D.cpp:236-260): production summed over groups
+// in order, ((nu_sigma_f phi) beta); then (P / lambda) (1 - decay) + C decay.
+__global__ void __launch_bounds__(kBlock) step_dnps_kernel(const IterArgs A, const TransientArgs X)
+{
+  const size_t N = A.N;
+  const int G = A.G, D = X.D;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const unsigned m = A.mat[c];
+    const unsigned Dm = X.dg ? X.dg[m] : 0u;
+    for (unsigned d = 0; d < Dm; ++d) {
+      double p = 0.0;
+      for (int g = 0; g < G; ++g) {
+        const size_t mg = (size_t)m * G + g;
+        p = dA(p, dM(dM(A.nsf[mg], A.phi[(size_t)g * N + c]), X.beta[mg * D + d]));
+      }
+      const double lam = X.lambda[(size_t)m * D + d], dec = X.decay[(size_t)m * D + d];
+      double & C = X.dnps[(size_t)d * N + c];
+      C = dA(dM(dD(p, lam), dS(1.0, dec)), dM(C, dec));
+    }
+  }
+}
+
+// updateStepFluxes (src/TransportSolver3D.cpp:199-222) and t += dt.
+__global__ void __launch_bounds__(kBlock) step_rollover_kernel(const IterArgs A, const TransientArgs X)
+{
+  const size_t n = A.N * (size_t)A.G;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    X.last[i] = A.phi[i];
+    A.phi[i] = 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) X.clock[0] = dA(X.clock[0], X.clock[1]);
+}
+
 // The source-iteration epilogue for group g:
 //   dphi = sum of the swept angular flux (exact: all ordinates in DOMA's
 //          single-thread order; fp32: the (octant, ordinate group) partials in order)
@@ -518,6 +618,34 @@ doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, dou
 doma_status launch_eigen_init(const IterArgs & a, cudaStream_t st)
 {
   eigen_init_kernel<<<a.grid, kBlock, 0, st>>>(a);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_mg_source_transient(const IterArgs & a, const TransientArgs & x, int g,
+                                       int precision, void * q, void * sigt,
+                                       const LoopParams & L, cudaStream_t st)
+{
+  if (precision == DOMA_PREC_FP64)
+    mg_source_transient_kernel<double><<<a.grid, kBlock, 0, st>>>(a, x, g, (double *)q,
+                                                                  (double *)sigt, L);
+  else
+    mg_source_transient_kernel<float><<<a.grid, kBlock, 0, st>>>(a, x, g, (float *)q,
+                                                                 (float *)sigt, L);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_step_dnps(const IterArgs & a, const TransientArgs & x, cudaStream_t st)
+{
+  step_dnps_kernel<<<a.grid, kBlock, 0, st>>>(a, x);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+doma_status launch_step_rollover(const IterArgs & a, const TransientArgs & x, cudaStream_t st)
+{
+  step_rollover_kernel<<<a.grid, kBlock, 0, st>>>(a, x);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }

@@ -35,6 +35,27 @@ struct IterArgs {
   const float * corr = nullptr;
 };
 
+// Transient mode (doma_transient on the device).  clock[0] is the step's
+// time t, clock[1] the step length dt: device memory, so that one captured
+// graph serves every step.  Delayed-group arrays are padded to D.
+struct TransientArgs {
+  int D = 0;                          // delayed groups (padded)
+  bool dims2 = false;                 // 2D: the cell solves see sigma_t + inv_v / dt
+  double * clock = nullptr;           // [2] t, dt
+  const double * inv_v = nullptr;     // [M][G]
+  const uint32_t * dg = nullptr;      // [M] delayed groups per material, or null
+  const double * chi_d = nullptr;     // [M][G][D]
+  const double * beta = nullptr;      // [M][G][D]
+  const double * lambda = nullptr;    // [M][D]
+  const double * decay = nullptr;     // [M][D] exp(-lambda dt), formed on the host
+  const uint32_t * step_type = nullptr;   // [M] or null
+  const double * step_insert = nullptr;   // [M]
+  const double * step_remove = nullptr;   // [M]
+  const double * step_source = nullptr;   // [M][G]
+  double * last = nullptr;            // [G][N] previous step's flux
+  double * dnps = nullptr;            // [D][N] precursor concentrations
+};
+
 // Device-side solve state (one per solver, in device memory; mirrored in
 // pinned host memory for read-back).
 struct LoopCtl {
@@ -82,6 +103,16 @@ doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * 
 doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k, void * q,
                                    void * sigt, cudaStream_t st);
 doma_status launch_eigen_init(const IterArgs & a, cudaStream_t st);
+// Transient mode: group g's source at the clock's t (external, source steps,
+// in-scatter, prompt fission (1 - beta), delayed neutrons, previous-step
+// flux inv_v / dt); graph-aware like launch_mg_source.
+doma_status launch_mg_source_transient(const IterArgs & a, const TransientArgs & x, int g,
+                                       int precision, void * q, void * sigt,
+                                       const LoopParams & L, cudaStream_t st);
+// Precursor step: C_d = (production / lambda_d) (1 - decay) + C_d decay.
+doma_status launch_step_dnps(const IterArgs & a, const TransientArgs & x, cudaStream_t st);
+// Next step: last := phi, phi := 0, t := t + dt.
+doma_status launch_step_rollover(const IterArgs & a, const TransientArgs & x, cudaStream_t st);
 doma_status launch_mg_residual(const IterArgs & a, double * norms, const LoopParams & L,
                                cudaStream_t st);
 // Batched multigroup solve: per-problem data of the batched epilogue.

@@ -130,6 +130,16 @@ struct doma_solver {
   std::vector<double> h_vol;     // [N] cell volume (area in 2D)
   std::vector<uint8_t> h_fis;    // [M]
   std::vector<double> h_nsf;     // [M][G]
+
+  // transient mode: device tables and state, allocated on first use for
+  // tr_D delayed groups (grown, with the graph rebuilt, when a call needs
+  // more); the captured Gauss-Seidel graph of a transient step
+  TransientArgs tr{};
+  int tr_D = 0;
+  std::vector<void *> tr_allocs;
+  double * h_dnps = nullptr;     // pinned [tr_D][N], for the step callback
+  cudaGraph_t tr_graph = nullptr;
+  cudaGraphExec_t tr_exec = nullptr;
 };
 
 namespace {
@@ -502,6 +512,10 @@ void release(doma_solver * s)
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->h_phi) cudaFreeHost(s->h_phi);
   if (s->h_prev) cudaFreeHost(s->h_prev);
+  if (s->tr_exec) cudaGraphExecDestroy(s->tr_exec);
+  if (s->tr_graph) cudaGraphDestroy(s->tr_graph);
+  for (void * p : s->tr_allocs) cudaFree(p);
+  if (s->h_dnps) cudaFreeHost(s->h_dnps);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
 }
@@ -539,6 +553,139 @@ doma_status read_norms(doma_solver * s, int first, double * diff, double * tot)
 double ratio(double diff, double tot)
 {
   return tot > 1e-8 ? std::sqrt(diff) / std::sqrt(tot) : 0.0;
+}
+
+// Tallies of a host-driven solve.
+struct Tally {
+  uint64_t sweeps = 0;
+  size_t si_len = 0;
+  unsigned mg = 0;
+  double mg_res = 0.0, si_res = 0.0;
+};
+
+// True for the statuses after which a solve still reports (the iteration
+// stopped); false for errors that end the call at once.
+bool reportable(doma_status st)
+{
+  return st == DOMA_OK || st == DOMA_NOT_CONVERGED || st == DOMA_NUMERIC_ERROR;
+}
+
+// sourceIteration (src/TransportSolver3D.cpp:458-497) for group g, its source
+// already staged: sweep + epilogue until the SI residual is at most fs_tol or
+// fs_max_it is reached, with DOMA's progress lines.  The count goes to
+// r->si_counts.  Returns DOMA_OK, DOMA_NOT_CONVERGED (fs_max_it reached),
+// DOMA_NUMERIC_ERROR or the error that stopped it.
+doma_status group_source_iteration(doma_solver * s, int g, doma_report * r, Tally & t)
+{
+  const doma_options & o = s->opts;
+  const int verbose = (int)o.verbose;
+  unsigned it = 0;
+  t.si_res = 0.0;
+  doma_status status = DOMA_OK;
+  do {
+    if (verbose >= 2) {
+      if (it != 0u)
+        std::printf("Performing SI %u for G%d, residual = %g\n", it, g, t.si_res);
+      else
+        std::printf("Performing SI %u for G%d\n", it, g);
+    }
+    DOMA_TRY(source_iteration(s, g));
+    ++t.sweeps;
+    double diff, tot;
+    DOMA_TRY(read_norms(s, 0, &diff, &tot));
+    if (!std::isfinite(diff) || !std::isfinite(tot)) {
+      set_error("source iteration norm is not finite (group " + std::to_string(g) + ")");
+      status = DOMA_NUMERIC_ERROR;
+      break;
+    }
+    t.si_res = ratio(diff, tot);
+    ++it;
+  } while (it < o.fs_max_it && o.fs_tol < t.si_res);
+  if (r && r->si_counts && t.si_len < r->si_counts_capacity) r->si_counts[t.si_len] = it;
+  ++t.si_len;
+  if (status != DOMA_OK) return status;
+  if (it < o.fs_max_it) {
+    if (verbose)
+      std::printf("SI converged after %u iterations with a residual of %g for G%d\n", it,
+                  t.si_res, g);
+    return DOMA_OK;
+  }
+  if (verbose)
+    std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n", it,
+                t.si_res, g);
+  return DOMA_NOT_CONVERGED;
+}
+
+// The Gauss-Seidel loop of solveFixedSource (src/TransportSolver3D.cpp:271-315),
+// host-driven: stage(g) sets up group g's source, then its source iteration;
+// the MG residual after each pass over the groups; DOMA's progress lines.
+template <typename Stage>
+doma_status gs_host_loop(doma_solver * s, Stage && stage, doma_report * r, Tally & t)
+{
+  const doma_options & o = s->opts;
+  const int verbose = (int)o.verbose;
+  doma_status status = DOMA_OK;
+  t.mg = 0;
+  t.mg_res = 0.0;
+  do {
+    if (verbose) {
+      if (t.mg != 0u)
+        std::printf("Performing MGI %u, residual = %g\n", t.mg, t.mg_res);
+      else
+        std::printf("Performing MGI %u\n", t.mg);
+      std::printf("----------------------------------------------------------------------------------\n");
+    }
+    for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
+      DOMA_TRY(stage(g));
+      ++s->launches;
+      status = group_source_iteration(s, g, r, t);
+      if (!reportable(status)) return status;
+    }
+    if (status != DOMA_OK) break;
+    DOMA_TRY(launch_mg_residual(s->it, s->d_ctl->norms + 2, LoopParams{}, s->stream));
+    ++s->launches;
+    double diff, tot;
+    DOMA_TRY(read_norms(s, 2, &diff, &tot));
+    if (!std::isfinite(diff) || !std::isfinite(tot)) {
+      set_error("Gauss-Seidel norm is not finite");
+      status = DOMA_NUMERIC_ERROR;
+      break;
+    }
+    t.mg_res = ratio(diff, tot);
+    ++t.mg;
+  } while (t.mg < o.mg_max_it && o.mg_tol < t.mg_res && s->G > 1);
+
+  if (status == DOMA_OK) {
+    if (t.mg < o.mg_max_it) {
+      if (verbose && s->G > 1)
+        std::printf("MGI converged after %u iterations with a residual of %g\n", t.mg, t.mg_res);
+    } else {
+      if (verbose)
+        std::printf("MGI failed to converge after %u iterations with a residual of %g\n", t.mg,
+                    t.mg_res);
+      status = DOMA_NOT_CONVERGED;
+      set_error("Gauss-Seidel iteration reached mg_max_it");
+    }
+  } else if (status == DOMA_NOT_CONVERGED) {
+    set_error("source iteration reached fs_max_it");
+  }
+  return status;
+}
+
+void fill_report(const doma_solver * s, doma_report * r, doma_status status, const Tally & t,
+                 std::chrono::steady_clock::time_point t0, uint64_t launches0)
+{
+  if (!r) return;
+  const auto t1 = std::chrono::steady_clock::now();
+  r->status = status;
+  r->mg_iterations = t.mg;
+  r->si_iterations = t.sweeps;
+  r->updates = t.sweeps * (uint64_t)s->N * (uint64_t)s->D;
+  r->kernel_launches = s->launches - launches0;
+  r->mg_residual = t.mg_res;
+  r->si_residual = t.si_res;
+  r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  r->si_counts_len = t.si_len;
 }
 
 LoopParams loop_params(doma_solver * s, int G)
@@ -592,7 +739,10 @@ doma_status add_while(cudaStream_t cap, cudaGraphConditionalHandle h, cudaGraph_
 //               mg_residual }
 // mg_source arms its group's SI loop, the epilogue decides whether the SI
 // loop goes on, the Gauss-Seidel residual kernel decides the outer loop.
-doma_status build_graph(doma_solver * s)
+// Capture the Gauss-Seidel / source-iteration loop as one graph with WHILE
+// nodes: the fixed-source solve, or (transient) one time step, whose source
+// kernel reads t and dt from the device clock.
+doma_status build_graph(doma_solver * s, bool transient)
 {
   cudaStream_t c0 = nullptr, c1 = nullptr, c2 = nullptr;
   DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
@@ -606,7 +756,7 @@ doma_status build_graph(doma_solver * s)
   auto run = [&]() -> doma_status {
     cudaGraph_t root = nullptr;
     if (cudaGraphCreate(&root, 0) != cudaSuccess) return fail(DOMA_CUDA_ERROR);
-    s->graph = root;
+    (transient ? s->tr_graph : s->graph) = root;
     cudaGraphConditionalHandle mg_h;
     DOMA_CUDA_TRY(cudaGraphConditionalHandleCreate(&mg_h, root, 1u, cudaGraphCondAssignDefault));
     std::vector<cudaGraphConditionalHandle> si_h(s->G);
@@ -624,7 +774,9 @@ doma_status build_graph(doma_solver * s)
         LoopParams L = loop_params(s, s->G);
         L.si_handle = si_h[g];
         L.mg_handle = mg_h;
-        st = launch_mg_source(s->it, g, s->opts.precision, s->d_q, s->d_sigt, L, c1);
+        st = transient ? launch_mg_source_transient(s->it, s->tr, g, s->opts.precision, s->d_q,
+                                                    s->d_sigt, L, c1)
+                       : launch_mg_source(s->it, g, s->opts.precision, s->d_q, s->d_sigt, L, c1);
         cudaGraph_t si_body = nullptr;
         if (st == DOMA_OK) st = add_while(c1, si_h[g], &si_body);
         if (st == DOMA_OK) {
@@ -649,7 +801,7 @@ doma_status build_graph(doma_solver * s)
     cudaGraph_t out = nullptr;
     DOMA_CUDA_TRY(cudaStreamEndCapture(c0, &out));
     if (st != DOMA_OK) return fail(st);
-    DOMA_CUDA_TRY(cudaGraphInstantiate(&s->graph_exec, root, 0));
+    DOMA_CUDA_TRY(cudaGraphInstantiate(transient ? &s->tr_exec : &s->graph_exec, root, 0));
     return DOMA_OK;
   };
   doma_status st = run();
@@ -662,13 +814,22 @@ doma_status build_graph(doma_solver * s)
 
 // Print DOMA's progress lines (src/TransportSolver3D.cpp:268-315,466-494)
 // from the histories the graph recorded.
-void print_history(doma_solver * s, const DevCtl & c, const std::vector<unsigned> & counts,
-                   const std::vector<double> & pres, const std::vector<double> & mgh,
-                   const std::vector<double> & sih)
+// One launch of a captured Gauss-Seidel graph, read back: the loop state and
+// the per-(MG iteration, group) SI counts and residual histories.
+struct GraphRun {
+  DevCtl c{};
+  std::vector<unsigned> counts;
+  std::vector<double> pres, mgh, sih;
+};
+
+void print_history(doma_solver * s, const GraphRun & run, bool banner)
 {
+  const DevCtl & c = run.c;
+  const std::vector<unsigned> & counts = run.counts;
+  const std::vector<double> &pres = run.pres, &mgh = run.mgh, &sih = run.sih;
   const int G = s->G;
   const int verbose = (int)s->opts.verbose;
-  std::printf("Solving...\nInitializing the solver...\n");
+  if (banner) std::printf("Solving...\nInitializing the solver...\n");
   size_t pair = 0, hist = 0;
   for (unsigned m = 0;; ++m) {
     if (pair >= c.pairs) break;
@@ -709,62 +870,86 @@ void print_history(doma_solver * s, const DevCtl & c, const std::vector<unsigned
   std::fflush(stdout);
 }
 
-doma_status solve_graph(doma_solver * s, doma_report * r)
+doma_status graph_run(doma_solver * s, cudaGraphExec_t exec, GraphRun & out)
 {
-  const size_t G = s->G, N = s->N;
-  const auto t0 = std::chrono::steady_clock::now();
-  if (!s->graph_exec) DOMA_TRY(build_graph(s));
-  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
-  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
   // clear error and loop state; keep the persistent-sweep counters
   DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
   DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->si_it, 0, sizeof(DevCtl) - offsetof(DevCtl, si_it),
                                 s->stream));
-  DOMA_CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+  DOMA_CUDA_TRY(cudaGraphLaunch(exec, s->stream));
   DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s->stream));
   DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
-  const DevCtl c = *s->h_ctl;
+  out.c = *s->h_ctl;
+  const DevCtl & c = out.c;
   const size_t npairs = std::min<size_t>(c.pairs, s->pair_cap);
-  std::vector<unsigned> counts(npairs);
-  std::vector<double> pres(npairs), mgh(std::min<size_t>(c.mg_it, s->mg_cap)), sih;
+  out.counts.assign(npairs, 0u);
+  out.pres.assign(npairs, 0.0);
+  out.mgh.assign(std::min<size_t>(c.mg_it, s->mg_cap), 0.0);
+  out.sih.clear();
   if (npairs) {
-    DOMA_CUDA_TRY(cudaMemcpy(counts.data(), s->d_pair_counts, npairs * sizeof(unsigned),
+    DOMA_CUDA_TRY(cudaMemcpy(out.counts.data(), s->d_pair_counts, npairs * sizeof(unsigned),
                              cudaMemcpyDeviceToHost));
-    DOMA_CUDA_TRY(cudaMemcpy(pres.data(), s->d_pair_res, npairs * sizeof(double),
+    DOMA_CUDA_TRY(cudaMemcpy(out.pres.data(), s->d_pair_res, npairs * sizeof(double),
                              cudaMemcpyDeviceToHost));
   }
-  if (!mgh.empty())
-    DOMA_CUDA_TRY(cudaMemcpy(mgh.data(), s->d_mg_hist, mgh.size() * sizeof(double),
+  if (!out.mgh.empty())
+    DOMA_CUDA_TRY(cudaMemcpy(out.mgh.data(), s->d_mg_hist, out.mgh.size() * sizeof(double),
                              cudaMemcpyDeviceToHost));
   if (s->d_si_hist && c.hist_len) {
-    sih.resize(std::min<unsigned long long>(c.hist_len, s->hist_cap));
-    DOMA_CUDA_TRY(cudaMemcpy(sih.data(), s->d_si_hist, sih.size() * sizeof(double),
+    out.sih.resize(std::min<unsigned long long>(c.hist_len, s->hist_cap));
+    DOMA_CUDA_TRY(cudaMemcpy(out.sih.data(), s->d_si_hist, out.sih.size() * sizeof(double),
                              cudaMemcpyDeviceToHost));
   }
-  if (s->opts.verbose) print_history(s, c, counts, pres, mgh, sih);
+  return DOMA_OK;
+}
 
-  doma_status status = DOMA_OK;
+// The status a graph run ended with (and its error message).
+doma_status graph_status(const doma_solver * s, const DevCtl & c)
+{
   if (c.failed == DOMA_DEVICE_WAIT_TIMEOUT) {
     set_error("a sweep wait for an upstream block timed out");
-    status = DOMA_DEVICE_WAIT_TIMEOUT;
-  } else if (c.failed == DOMA_NUMERIC_ERROR) {
-    set_error("a residual norm is not finite");
-    status = DOMA_NUMERIC_ERROR;
-  } else if (c.failed == DOMA_NOT_CONVERGED) {
-    set_error("source iteration reached fs_max_it");
-    status = DOMA_NOT_CONVERGED;
-  } else if (!(c.mg_it < s->opts.mg_max_it)) {
-    set_error("Gauss-Seidel iteration reached mg_max_it");
-    status = DOMA_NOT_CONVERGED;
+    return DOMA_DEVICE_WAIT_TIMEOUT;
   }
-  // kernel launches: the graph launches G mg_source + one MG residual per MG
-  // iteration and (sweep launches + 1) per source iteration
+  if (c.failed == DOMA_NUMERIC_ERROR) {
+    set_error("a residual norm is not finite");
+    return DOMA_NUMERIC_ERROR;
+  }
+  if (c.failed == DOMA_NOT_CONVERGED) {
+    set_error("source iteration reached fs_max_it");
+    return DOMA_NOT_CONVERGED;
+  }
+  if (!(c.mg_it < s->opts.mg_max_it)) {
+    set_error("Gauss-Seidel iteration reached mg_max_it");
+    return DOMA_NOT_CONVERGED;
+  }
+  return DOMA_OK;
+}
+
+// Kernel launches of a graph run: G sources + one MG residual per MG
+// iteration and (sweep launches + 1) per source iteration.
+uint64_t graph_launches(const doma_solver * s, const DevCtl & c)
+{
   uint64_t per_sweep = s->sched.persistent ? 1 : 0;
   if (!s->sched.persistent)
     for (size_t L = 0; L + 1 < s->sched.level_begin.size(); ++L)
       per_sweep += s->sched.level_begin[L + 1] > s->sched.level_begin[L];
-  const uint64_t launches = c.sweeps * (per_sweep + 1) +
-                            (uint64_t)(c.mg_it + (c.failed ? 1 : 0)) * (uint64_t)(s->G + 1);
+  return c.sweeps * (per_sweep + 1) +
+         (uint64_t)(c.mg_it + (c.failed ? 1 : 0)) * (uint64_t)(s->G + 1);
+}
+
+doma_status solve_graph(doma_solver * s, doma_report * r)
+{
+  const size_t G = s->G, N = s->N;
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!s->graph_exec) DOMA_TRY(build_graph(s, false));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
+  GraphRun run;
+  DOMA_TRY(graph_run(s, s->graph_exec, run));
+  const DevCtl & c = run.c;
+  if (s->opts.verbose) print_history(s, run, true);
+  const doma_status status = graph_status(s, c);
+  const uint64_t launches = graph_launches(s, c);
   s->launches += launches;
   const auto t1 = std::chrono::steady_clock::now();
   if (r) {
@@ -778,7 +963,8 @@ doma_status solve_graph(doma_solver * s, doma_report * r)
     r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     r->si_counts_len = c.pairs;
     if (r->si_counts)
-      for (size_t k = 0; k < npairs && k < r->si_counts_capacity; ++k) r->si_counts[k] = counts[k];
+      for (size_t k = 0; k < run.counts.size() && k < r->si_counts_capacity; ++k)
+        r->si_counts[k] = run.counts[k];
   }
   return status;
 }
@@ -1050,112 +1236,33 @@ doma_status solve_impl(doma_solver * s, doma_report * r)
   if (s->mgi && (s->accel || s->d_ref)) return solve_multigroup_guided(s, r);
   if (s->mgi) return solve_multigroup(s, r);
   if (s->use_graph) return solve_graph(s, r);
-  const doma_options & o = s->opts;
-  const int verbose = (int)o.verbose;
   const size_t G = s->G, N = s->N;
   const auto t0 = std::chrono::steady_clock::now();
   const uint64_t launches0 = s->launches;
-  if (verbose) {
-    std::printf("Solving...\nInitializing the solver...\n");
-  }
+  if (s->opts.verbose) std::printf("Solving...\nInitializing the solver...\n");
   DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
   DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
   DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
-
-  uint64_t sweeps = 0;
-  size_t si_len = 0;
-  unsigned mg = 0;
-  double mg_res = 0.0, si_res = 0.0;
-  doma_status status = DOMA_OK;
-  do {
-    if (verbose) {
-      if (mg != 0u)
-        std::printf("Performing MGI %u, residual = %g\n", mg, mg_res);
-      else
-        std::printf("Performing MGI %u\n", mg);
-      std::printf("----------------------------------------------------------------------------------\n");
-    }
-    for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
-      DOMA_TRY(launch_mg_source(s->it, g, o.precision, s->d_q, s->d_sigt, LoopParams{}, s->stream));
-      ++s->launches;
-      unsigned it = 0;
-      si_res = 0.0;
-      do {
-        if (verbose >= 2) {
-          if (it != 0u)
-            std::printf("Performing SI %u for G%d, residual = %g\n", it, g, si_res);
-          else
-            std::printf("Performing SI %u for G%d\n", it, g);
-        }
-        DOMA_TRY(source_iteration(s, g));
-        ++sweeps;
-        double diff, tot;
-        DOMA_TRY(read_norms(s, 0, &diff, &tot));
-        if (!std::isfinite(diff) || !std::isfinite(tot)) {
-          set_error("source iteration norm is not finite (group " + std::to_string(g) + ")");
-          status = DOMA_NUMERIC_ERROR;
-          break;
-        }
-        si_res = ratio(diff, tot);
-        ++it;
-      } while (it < o.fs_max_it && o.fs_tol < si_res);
-      if (r && r->si_counts && si_len < r->si_counts_capacity) r->si_counts[si_len] = it;
-      ++si_len;
-      if (status != DOMA_OK) break;
-      if (it < o.fs_max_it) {
-        if (verbose)
-          std::printf("SI converged after %u iterations with a residual of %g for G%d\n", it,
-                      si_res, g);
-      } else {
-        if (verbose)
-          std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n",
-                      it, si_res, g);
-        status = DOMA_NOT_CONVERGED;
-      }
-    }
-    if (status != DOMA_OK) break;
-    DOMA_TRY(launch_mg_residual(s->it, s->d_ctl->norms + 2, LoopParams{}, s->stream));
-    ++s->launches;
-    double diff, tot;
-    DOMA_TRY(read_norms(s, 2, &diff, &tot));
-    if (!std::isfinite(diff) || !std::isfinite(tot)) {
-      set_error("Gauss-Seidel norm is not finite");
-      status = DOMA_NUMERIC_ERROR;
-      break;
-    }
-    mg_res = ratio(diff, tot);
-    ++mg;
-  } while (mg < o.mg_max_it && o.mg_tol < mg_res && s->G > 1);
-
-  if (status == DOMA_OK) {
-    if (mg < o.mg_max_it) {
-      if (verbose && s->G > 1)
-        std::printf("MGI converged after %u iterations with a residual of %g\n", mg, mg_res);
-    } else {
-      if (verbose)
-        std::printf("MGI failed to converge after %u iterations with a residual of %g\n", mg,
-                    mg_res);
-      status = DOMA_NOT_CONVERGED;
-      set_error("Gauss-Seidel iteration reached mg_max_it");
-    }
-  } else if (status == DOMA_NOT_CONVERGED) {
-    set_error("source iteration reached fs_max_it");
-  }
-  if (verbose) std::fflush(stdout);
+  Tally t;
+  auto stage = [&](int g) {
+    return launch_mg_source(s->it, g, s->opts.precision, s->d_q, s->d_sigt, LoopParams{},
+                            s->stream);
+  };
+  const doma_status status = gs_host_loop(s, stage, r, t);
+  if (!reportable(status)) return status;
+  if (s->opts.verbose) std::fflush(stdout);
   DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
-  const auto t1 = std::chrono::steady_clock::now();
-  if (r) {
-    r->status = status;
-    r->mg_iterations = mg;
-    r->si_iterations = sweeps;
-    r->updates = sweeps * (uint64_t)s->N * (uint64_t)s->D;
-    r->kernel_launches = s->launches - launches0;
-    r->mg_residual = mg_res;
-    r->si_residual = si_res;
-    r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-    r->si_counts_len = si_len;
-  }
+  fill_report(s, r, status, t, t0, launches0);
   return status;
+}
+
+// Pinned host copies of the flux and the previous iterate (first use).
+doma_status ensure_host_flux(doma_solver * s)
+{
+  const size_t bytes = (size_t)s->G * s->N * sizeof(double);
+  if (!s->h_phi) DOMA_CUDA_TRY(cudaMallocHost(&s->h_phi, bytes));
+  if (!s->h_prev) DOMA_CUDA_TRY(cudaMallocHost(&s->h_prev, bytes));
+  return DOMA_OK;
 }
 
 // ---- k-eigenvalue power iteration ------------------------------------------
@@ -1166,10 +1273,7 @@ doma_status solve_impl(doma_solver * s, doma_report * r)
 doma_status k_update(doma_solver * s, double k, double * k_new)
 {
   const size_t G = s->G, N = s->N, bytes = G * N * sizeof(double);
-  if (!s->h_phi) {
-    DOMA_CUDA_TRY(cudaMallocHost(&s->h_phi, bytes));
-    DOMA_CUDA_TRY(cudaMallocHost(&s->h_prev, bytes));
-  }
+  DOMA_TRY(ensure_host_flux(s));
   DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_phi, s->d_phi, bytes, cudaMemcpyDeviceToHost, s->stream));
   DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_prev, s->d_prev, bytes, cudaMemcpyDeviceToHost, s->stream));
   DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -1205,57 +1309,23 @@ doma_status solve_eigen_impl(doma_solver * s, double k_tol, doma_report * r, dou
   DOMA_CUDA_TRY(cudaMemsetAsync(s->d_q, 0, N * (o.precision == DOMA_PREC_FP64 ? 8 : 4), s->stream));
   DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
 
-  uint64_t sweeps = 0;
-  size_t si_len = 0;
-  unsigned mg = 0;
-  double k = 1.0, k_prev = 0.0, shape = 0.0, kdiff = 0.0, si_res = 0.0;
+  Tally t;
+  double k = 1.0, k_prev = 0.0, shape = 0.0, kdiff = 0.0;
   doma_status status = DOMA_OK;
   do {
     if (verbose) {
-      if (mg != 0u)
-        std::printf("Performing PI %u, shape residual = %g, k residual = %g\nk = %g\n", mg, shape,
-                    kdiff, k);
+      if (t.mg != 0u)
+        std::printf("Performing PI %u, shape residual = %g, k residual = %g\nk = %g\n", t.mg,
+                    shape, kdiff, k);
       else
-        std::printf("Performing PI %u\n", mg);
+        std::printf("Performing PI %u\n", t.mg);
       std::printf("----------------------------------------------------------------------------------\n");
     }
     for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
       DOMA_TRY(launch_mg_source_eigen(s->it, g, o.precision, k, s->d_q, s->d_sigt, s->stream));
       ++s->launches;
-      unsigned it = 0;
-      si_res = 0.0;
-      do {
-        if (verbose >= 2) {
-          if (it != 0u)
-            std::printf("Performing SI %u for G%d, residual = %g\n", it, g, si_res);
-          else
-            std::printf("Performing SI %u for G%d\n", it, g);
-        }
-        DOMA_TRY(source_iteration(s, g));
-        ++sweeps;
-        double diff, tot;
-        DOMA_TRY(read_norms(s, 0, &diff, &tot));
-        if (!std::isfinite(diff) || !std::isfinite(tot)) {
-          set_error("source iteration norm is not finite (group " + std::to_string(g) + ")");
-          status = DOMA_NUMERIC_ERROR;
-          break;
-        }
-        si_res = ratio(diff, tot);
-        ++it;
-      } while (it < o.fs_max_it && o.fs_tol < si_res);
-      if (r && r->si_counts && si_len < r->si_counts_capacity) r->si_counts[si_len] = it;
-      ++si_len;
-      if (status != DOMA_OK) break;
-      if (it < o.fs_max_it) {
-        if (verbose)
-          std::printf("SI converged after %u iterations with a residual of %g for G%d\n", it,
-                      si_res, g);
-      } else {
-        if (verbose)
-          std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n",
-                      it, si_res, g);
-        status = DOMA_NOT_CONVERGED;  // solveEigenvalue returns false at once
-      }
+      status = group_source_iteration(s, g, r, t);  // a failed group: solveEigenvalue returns false
+      if (!reportable(status)) return status;
     }
     if (status != DOMA_OK) break;
     k_prev = k;
@@ -1271,18 +1341,18 @@ doma_status solve_eigen_impl(doma_solver * s, double k_tol, doma_report * r, dou
     }
     shape = ratio(diff, tot);
     kdiff = std::abs(k - k_prev);
-    ++mg;
-  } while (mg < o.mg_max_it && (o.mg_tol < shape || k_tol < kdiff));
+    ++t.mg;
+  } while (t.mg < o.mg_max_it && (o.mg_tol < shape || k_tol < kdiff));
 
   if (status == DOMA_OK) {
-    if (mg < o.mg_max_it) {
+    if (t.mg < o.mg_max_it) {
       if (verbose)
         std::printf("PI converged after %u iterations with a flux shape residual of %g and a k "
-                    "residual of %g.\nConverged value of k = %g\n", mg, shape, kdiff, k);
+                    "residual of %g.\nConverged value of k = %g\n", t.mg, shape, kdiff, k);
     } else {
       if (verbose)
         std::printf("PI failed to converge after %u iterations with a flux shape residual of %g "
-                    "and a k residual of %g.\n", mg, shape, kdiff);
+                    "and a k residual of %g.\n", t.mg, shape, kdiff);
       status = DOMA_NOT_CONVERGED;
       set_error("power iteration reached mg_max_it");
     }
@@ -1291,19 +1361,225 @@ doma_status solve_eigen_impl(doma_solver * s, double k_tol, doma_report * r, dou
   }
   if (verbose) std::fflush(stdout);
   DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
-  const auto t1 = std::chrono::steady_clock::now();
   if (k_out) *k_out = k;
-  if (r) {
-    r->status = status;
-    r->mg_iterations = mg;
-    r->si_iterations = sweeps;
-    r->updates = sweeps * (uint64_t)s->N * (uint64_t)s->D;
-    r->kernel_launches = s->launches - launches0;
-    r->mg_residual = shape;
-    r->si_residual = si_res;
-    r->solve_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-    r->si_counts_len = si_len;
+  t.mg_res = shape;
+  fill_report(s, r, status, t, t0, launches0);
+  return status;
+}
+
+// ---- transient (zero initial condition) ------------------------------------
+
+// The checks DOMA's deck reader makes on transient data
+// (src/InputParameters.cpp:286-500), plus what its solver assumes: a material
+// with delayed groups has production cross sections (stepDNPs reads them) and
+// positive decay constants (it divides by them).
+doma_status transient_validate(const doma_solver * s, const doma_transient * tr)
+{
+  if (!tr) return bad("transient data is null");
+  if (!(tr->dt > 0.0) || !std::isfinite(tr->dt)) return bad("transient dt must be positive and finite");
+  if (!tr->inv_v) return bad("transient inv_v is required");
+  const size_t M = s->M, G = s->G, D = tr->num_d_groups;
+  for (size_t i = 0; i < M * G; ++i)
+    if (!std::isfinite(tr->inv_v[i])) return bad("transient inv_v must be finite");
+  if (D > 0 && (!tr->d_groups || !tr->chi_d || !tr->beta || !tr->lambda))
+    return bad("delayed groups need d_groups, chi_d, beta and lambda");
+  if (tr->d_groups)
+    for (size_t m = 0; m < M; ++m) {
+      const uint32_t Dm = tr->d_groups[m];
+      if (Dm > D)
+        return bad("material " + std::to_string(m) + " has more delayed groups than num_d_groups");
+      if (Dm > 0 && !s->h_fis[m])
+        return bad("material " + std::to_string(m) + " has delayed groups but no fission data");
+      for (uint32_t d = 0; d < Dm; ++d)
+        if (!(tr->lambda[m * D + d] > 0.0) || !std::isfinite(tr->lambda[m * D + d]))
+          return bad("material " + std::to_string(m) + ": decay constants must be positive");
+    }
+  if (tr->step_type) {
+    if (!tr->step_insert || !tr->step_remove || !tr->step_source)
+      return bad("source steps need step_insert, step_remove and step_source");
+    for (size_t m = 0; m < M; ++m) {
+      const uint32_t st = tr->step_type[m];
+      if (st > DOMA_STEP_REMOVE)
+        return bad("material " + std::to_string(m) + ": unknown source step type");
+      if (st == DOMA_STEP_BOTH && tr->step_remove[m] < tr->step_insert[m])
+        return bad("The step source for block " + std::to_string(m) + " is being removed at " +
+                   std::to_string(tr->step_remove[m]) +
+                   ", which is less than the insertion time of " +
+                   std::to_string(tr->step_insert[m]) + "!");
+    }
   }
+  return DOMA_OK;
+}
+
+template <typename T>
+doma_status talloc(doma_solver * s, T ** p, size_t count)
+{
+  void * v = nullptr;
+  cudaError_t e = cudaMalloc(&v, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return DOMA_CUDA_ERROR;
+  }
+  s->tr_allocs.push_back(v);
+  *p = static_cast<T *>(v);
+  return DOMA_OK;
+}
+
+// Device tables of a transient call, padded to the allocated delayed-group
+// count (absent arrays upload as zeros, so the captured graph's arguments
+// never change), the clock (t = 0, dt) and the zero initial condition
+// (initZeroIC, src/TransportSolver3D.cpp:142-157).
+doma_status transient_upload(doma_solver * s, const doma_transient * tr)
+{
+  const size_t M = s->M, G = s->G, N = s->N, D = tr->num_d_groups;
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (s->tr_allocs.empty() || D > (size_t)s->tr_D) {
+    if (s->tr_exec) cudaGraphExecDestroy(s->tr_exec);
+    if (s->tr_graph) cudaGraphDestroy(s->tr_graph);
+    s->tr_exec = nullptr;
+    s->tr_graph = nullptr;
+    for (void * p : s->tr_allocs) cudaFree(p);
+    s->tr_allocs.clear();
+    if (s->h_dnps) cudaFreeHost(s->h_dnps);
+    s->h_dnps = nullptr;
+    const size_t Dc = std::max<size_t>(D, 1);
+    TransientArgs & x = s->tr;
+    x = TransientArgs{};
+    x.D = (int)Dc;
+    x.dims2 = s->dims == 2;
+    double *clock, *inv_v, *chi_d, *beta, *lambda, *decay, *ins, *rem, *ssrc, *last, *dnps;
+    uint32_t *dg, *stype;
+    DOMA_TRY(talloc(s, &clock, 2));
+    DOMA_TRY(talloc(s, &inv_v, M * G));
+    DOMA_TRY(talloc(s, &dg, M));
+    DOMA_TRY(talloc(s, &chi_d, M * G * Dc));
+    DOMA_TRY(talloc(s, &beta, M * G * Dc));
+    DOMA_TRY(talloc(s, &lambda, M * Dc));
+    DOMA_TRY(talloc(s, &decay, M * Dc));
+    DOMA_TRY(talloc(s, &stype, M));
+    DOMA_TRY(talloc(s, &ins, M));
+    DOMA_TRY(talloc(s, &rem, M));
+    DOMA_TRY(talloc(s, &ssrc, M * G));
+    DOMA_TRY(talloc(s, &last, G * N));
+    DOMA_TRY(talloc(s, &dnps, Dc * N));
+    DOMA_CUDA_TRY(cudaMallocHost(&s->h_dnps, Dc * N * sizeof(double)));
+    x.clock = clock; x.inv_v = inv_v; x.dg = dg; x.chi_d = chi_d; x.beta = beta;
+    x.lambda = lambda; x.decay = decay; x.step_type = stype; x.step_insert = ins;
+    x.step_remove = rem; x.step_source = ssrc; x.last = last; x.dnps = dnps;
+    s->tr_D = (int)Dc;
+  }
+  const size_t Dc = (size_t)s->tr_D;
+  std::vector<uint32_t> dg(M, 0u), stype(M, 0u);
+  std::vector<double> chi_d(M * G * Dc, 0.0), beta(M * G * Dc, 0.0), lambda(M * Dc, 0.0),
+      decay(M * Dc, 0.0), ins(M, 0.0), rem(M, 0.0), ssrc(M * G, 0.0);
+  if (tr->d_groups)
+    for (size_t m = 0; m < M; ++m) {
+      dg[m] = tr->d_groups[m];
+      for (size_t d = 0; d < dg[m]; ++d) {
+        for (size_t g = 0; g < G; ++g) {
+          chi_d[(m * G + g) * Dc + d] = tr->chi_d[(m * G + g) * D + d];
+          beta[(m * G + g) * Dc + d] = tr->beta[(m * G + g) * D + d];
+        }
+        const double lam = tr->lambda[m * D + d];
+        lambda[m * Dc + d] = lam;
+        decay[m * Dc + d] = std::exp(-lam * tr->dt);  // stepDNPs: std::exp(-lambda * dt)
+      }
+    }
+  if (tr->step_type) {
+    stype.assign(tr->step_type, tr->step_type + M);
+    ins.assign(tr->step_insert, tr->step_insert + M);
+    rem.assign(tr->step_remove, tr->step_remove + M);
+    ssrc.assign(tr->step_source, tr->step_source + M * G);
+  }
+  const double clock[2] = {0.0, tr->dt};
+  const TransientArgs & x = s->tr;
+  DOMA_CUDA_TRY(cudaMemcpy(x.clock, clock, sizeof(clock), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.inv_v, tr->inv_v, M * G * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.dg, dg.data(), M * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.chi_d, chi_d.data(), chi_d.size() * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.beta, beta.data(), beta.size() * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.lambda, lambda.data(), lambda.size() * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.decay, decay.data(), decay.size() * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.step_type, stype.data(), M * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.step_insert, ins.data(), M * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.step_remove, rem.data(), M * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemcpy((void *)x.step_source, ssrc.data(), M * G * sizeof(double), cudaMemcpyHostToDevice));
+  DOMA_CUDA_TRY(cudaMemsetAsync(x.last, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(x.dnps, 0, Dc * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_phi, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(s->d_prev, 0, G * N * sizeof(double), s->stream));
+  DOMA_CUDA_TRY(cudaMemsetAsync(&s->d_ctl->error, 0, sizeof(int), s->stream));
+  return DOMA_OK;
+}
+
+// solveTransient with TransientIC::Zero (src/TransportSolver3D.cpp:88-140):
+// per step the Gauss-Seidel solve with the transient source (one graph
+// launch, or the host loop), stepDNPs, the callback, updateStepFluxes.
+doma_status solve_transient_impl(doma_solver * s, const doma_transient * tr,
+                                 doma_step_callback callback, void * user, doma_report * r)
+{
+  if (s->mgi) return bad("transient solves use Gauss-Seidel iteration");
+  DOMA_TRY(transient_validate(s, tr));
+  const int verbose = (int)s->opts.verbose;
+  const size_t G = s->G, N = s->N, D = tr->num_d_groups;
+  const auto t0 = std::chrono::steady_clock::now();
+  const uint64_t launches0 = s->launches;
+  DOMA_TRY(transient_upload(s, tr));
+  if (s->use_graph && !s->tr_exec) DOMA_TRY(build_graph(s, true));
+  if (callback) DOMA_TRY(ensure_host_flux(s));
+  if (verbose) std::printf("Setting up initial conditions...\n");
+  Tally t;
+  doma_status status = DOMA_OK;
+  double time = 0.0;
+  for (uint32_t step = 0; step < tr->num_steps; ++step) {
+    if (verbose) std::printf("Solving timestep %u...\n", step);
+    if (s->use_graph) {
+      GraphRun run;
+      DOMA_TRY(graph_run(s, s->tr_exec, run));
+      if (verbose) print_history(s, run, false);
+      status = graph_status(s, run.c);
+      s->launches += graph_launches(s, run.c);
+      t.sweeps += run.c.sweeps;
+      t.mg = run.c.mg_it;
+      t.mg_res = run.c.mg_res;
+      t.si_res = run.c.si_res;
+      if (r && r->si_counts)
+        for (size_t k = 0; k < run.counts.size(); ++k)
+          if (t.si_len + k < r->si_counts_capacity) r->si_counts[t.si_len + k] = run.counts[k];
+      t.si_len += run.c.pairs;
+    } else {
+      auto stage = [&](int g) {
+        return launch_mg_source_transient(s->it, s->tr, g, s->opts.precision, s->d_q, s->d_sigt,
+                                          LoopParams{}, s->stream);
+      };
+      status = gs_host_loop(s, stage, r, t);
+      if (!reportable(status)) return status;
+    }
+    if (status != DOMA_OK) break;  // solveTransient returns false at once
+    DOMA_TRY(launch_step_dnps(s->it, s->tr, s->stream));
+    ++s->launches;
+    if (callback) {
+      DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_phi, s->d_phi, G * N * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s->stream));
+      if (D)
+        DOMA_CUDA_TRY(cudaMemcpyAsync(s->h_dnps, s->tr.dnps, D * N * sizeof(double),
+                                      cudaMemcpyDeviceToHost, s->stream));
+      DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+      if (verbose) std::fflush(stdout);
+      if (callback(user, step, time, s->h_phi, D ? s->h_dnps : nullptr) != 0) {
+        status = bad("the step callback stopped the transient after step " + std::to_string(step));
+        break;
+      }
+    }
+    if (step + 1 != tr->num_steps) {
+      DOMA_TRY(launch_step_rollover(s->it, s->tr, s->stream));
+      ++s->launches;
+    }
+    time += tr->dt;
+  }
+  if (verbose) std::fflush(stdout);
+  DOMA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  fill_report(s, r, status, t, t0, launches0);
   return status;
 }
 
@@ -1376,6 +1652,14 @@ doma_status doma_solver_solve_eigenvalue(doma_solver * s, double k_tol, doma_rep
   if (!s) return bad("null solver");
   if (!(k_tol >= 0.0)) return bad("k_tol must be >= 0");
   return solve_eigen_impl(s, k_tol, report, k);
+}
+
+doma_status doma_solver_solve_transient(doma_solver * s, const doma_transient * tr,
+                                        doma_step_callback callback, void * user,
+                                        doma_report * report)
+{
+  if (!s) return bad("null solver");
+  return solve_transient_impl(s, tr, callback, user, report);
 }
 
 doma_status doma_solver_get_scalar_flux(doma_solver * s, double * out, size_t count)

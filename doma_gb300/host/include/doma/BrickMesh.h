@@ -36,6 +36,10 @@ public:
 
   // <base>_dims.txt, _blocks.txt, _meshx/y/z.txt and _g<g>_flux.txt.
   void dumpToTextFile(const std::string & file_name, bool only_flux = false);
+  // <base>_d<d>_dnps.txt for each delayed group d below the most that any
+  // cell's material has; a cell whose material has fewer prints 0
+  // (DOMA src/BrickMesh3D.cpp:273-295).
+  void dumpDNPsToTextFile(const std::string & file_name);
 
   unsigned int numX() const { return _tot_num_x; }
   unsigned int numY() const { return _tot_num_y; }
@@ -48,6 +52,8 @@ public:
   const std::vector<unsigned int> & cellBlocks() const { return _block_of_cell; }
   // [g * numCells() + cell]
   const std::vector<double> & scalarFlux() const { return _flux; }
+  // [d * numCells() + cell] precursors after the last transient step
+  const std::vector<double> & precursors() const { return _dnps; }
   // Replace the scalar flux ([G][N]; throws on a size mismatch).
   void setScalarFlux(const std::vector<double> & flux);
 
@@ -64,6 +70,8 @@ private:
   const InputParameters & _params;
   unsigned int _num_threads;
   std::vector<double> _flux;
+  std::vector<double> _dnps;             // [D][N] precursor concentrations (transients)
+  std::vector<unsigned int> _cell_d;     // [N] delayed groups of each cell's material
 };
 
 class BrickMesh2D
@@ -75,6 +83,7 @@ public:
   void validateProps();
   bool fluxAtPoint(const double & x, const double & y, unsigned int g, double & returned_flux) const;
   void dumpToTextFile(const std::string & file_name, bool only_flux = false);
+  void dumpDNPsToTextFile(const std::string & file_name);
 
   unsigned int numX() const { return _tot_num_x; }
   unsigned int numY() const { return _tot_num_y; }
@@ -84,6 +93,7 @@ public:
   const std::vector<double> & widthsY() const { return _wy; }
   const std::vector<unsigned int> & cellBlocks() const { return _block_of_cell; }
   const std::vector<double> & scalarFlux() const { return _flux; }
+  const std::vector<double> & precursors() const { return _dnps; }
   void setScalarFlux(const std::vector<double> & flux);
 
 private:
@@ -99,4 +109,6 @@ private:
   const InputParameters & _params;
   unsigned int _num_threads;
   std::vector<double> _flux;
+  std::vector<double> _dnps;             // [D][N] precursor concentrations (transients)
+  std::vector<unsigned int> _cell_d;     // [N] delayed groups of each cell's material
 };

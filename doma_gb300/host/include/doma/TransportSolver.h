@@ -15,10 +15,16 @@
 // reached (the flux of the last iterate is kept in the mesh), print DOMA's
 // progress lines (each SI residual too when verbose), write the text output
 // when output_file_base is not empty and the solve converged.  eigenvalue()
-// gives k after solveEigenvalue (DOMA keeps it private).
+// gives k after solveEigenvalue (DOMA keeps it private).  solveTransient
+// (DOMA src/TransportSolver3D.cpp:88-140) writes the zero initial condition
+// as <base>_* files, then after each step <base>_t<step>_g<g>_flux.txt and
+// <base>_t<step>_d<d>_dnps.txt, and returns false as soon as a step's solve
+// reaches a cap; the mesh keeps the last step's flux and precursors.
 // Differences: invalid input and CUDA failures throw std::runtime_error
 // instead of exiting; num_threads is accepted and unused (the device does
-// the work); the transient driver is not provided.
+// the work); transients start from zero only (DOMA's steady-state start
+// reads its previous-step and precursor arrays before sizing them) and
+// write no files when output_file_base is empty.
 #pragma once
 
 #include <cstdint>
@@ -65,14 +71,18 @@ public:
 
   bool solveFixedSource(const std::string & output_file_base = "", const double & t = 0.0);
   bool solveEigenvalue(const std::string & output_file_base = "");
+  bool solveTransient(const std::string & output_file_base);
 
   const SolveStats & stats() const { return _stats; }
   double eigenvalue() const { return _k; }
 
 private:
   doma_solver * solver();
+  static int stepDone(void * user, uint32_t step, double t, const double * phi,
+                      const double * dnps);
 
   BrickMesh3D & _mesh;
+  std::string _step_base;
   const InputParameters & _params;
   const bool _verbose;
   doma_solver * _solver = nullptr;
@@ -97,14 +107,18 @@ public:
 
   bool solveFixedSource(const std::string & output_file_base = "", const double & t = 0.0);
   bool solveEigenvalue(const std::string & output_file_base = "");
+  bool solveTransient(const std::string & output_file_base);
 
   const SolveStats & stats() const { return _stats; }
   double eigenvalue() const { return _k; }
 
 private:
   doma_solver * solver();
+  static int stepDone(void * user, uint32_t step, double t, const double * phi,
+                      const double * dnps);
 
   BrickMesh2D & _mesh;
+  std::string _step_base;
   const InputParameters & _params;
   const bool _verbose;
   doma_solver * _solver = nullptr;

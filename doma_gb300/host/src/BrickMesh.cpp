@@ -11,6 +11,7 @@
 // significant digits for coordinates and fluxes.
 #include "doma/BrickMesh.h"
 
+#include <algorithm>
 #include <fstream>
 #include <iomanip>
 #include <stdexcept>
@@ -48,6 +49,24 @@ void check_axis(const std::vector<unsigned int> & counts, const std::vector<doub
                              " interval counts and lengths differ in size!");
   for (auto c : counts)
     if (c == 0) throw std::runtime_error(std::string("Error: an ") + axis + " interval has no cells!");
+}
+
+// Shared by both meshes: DOMA's dumpDNPsToTextFile.
+void dump_dnps(const std::string & file_name, const std::vector<double> & dnps,
+               const std::vector<unsigned int> & cell_d, size_t N)
+{
+  unsigned int D = 0;
+  for (unsigned int d : cell_d) D = std::max(D, d);
+  for (unsigned int d = 0; d < D; ++d) {
+    std::ofstream out(file_name + "_d" + std::to_string(d) + "_dnps.txt", std::ofstream::out);
+    out << std::setprecision(6);
+    for (size_t c = 0; c < N; ++c) {
+      if (cell_d[c] == D && (size_t)d * N + c < dnps.size())
+        out << dnps[(size_t)d * N + c] << std::endl;
+      else
+        out << 0.0 << std::endl;
+    }
+  }
 }
 
 }  // namespace
@@ -229,4 +248,14 @@ void BrickMesh2D::setScalarFlux(const std::vector<double> & flux)
 {
   if (flux.size() != _flux.size()) throw std::runtime_error("scalar flux size mismatch");
   _flux = flux;
+}
+
+void BrickMesh3D::dumpDNPsToTextFile(const std::string & file_name)
+{
+  dump_dnps(file_name, _dnps, _cell_d, numCells());
+}
+
+void BrickMesh2D::dumpDNPsToTextFile(const std::string & file_name)
+{
+  dump_dnps(file_name, _dnps, _cell_d, numCells());
 }

@@ -2,12 +2,12 @@
 //
 // Same flags as DOMA's driver (src/main.cpp:20-30): -i/--input_file <deck>,
 // -n/--n-threads <T> (accepted; the device does the work) and --verbose.
-// 2D and 3D fixed-source and eigenvalue decks are solved through the drop-in
-// TransportSolver2D/3D; output goes next to the deck as <dir>/<stem>_* text
-// files, and the run ends with DOMA's "Time elapsed: <s> (s)." line.  Like
-// DOMA, a solve that hits an iteration cap still exits 0 (after DOMA's
-// failure message); --strict makes it exit 3 instead.  Decks the GPU library
-// does not run (1D, transient) exit 1 with a message.
+// 2D and 3D fixed-source, eigenvalue and transient decks are solved through
+// the drop-in TransportSolver2D/3D; output goes next to the deck as
+// <dir>/<stem>_* text files, and the run ends with DOMA's "Time elapsed: <s>
+// (s)." line.  Like DOMA, a solve that hits an iteration cap still exits 0
+// (after DOMA's failure message); --strict makes it exit 3 instead.  1D decks
+// and transients with a steady-state start exit 1 with a message.
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
@@ -24,7 +24,7 @@ namespace {
 void usage(const char * argv0)
 {
   std::cerr << "Usage: " << argv0 << " -i <input_file> [-n <threads>] [--verbose] [--strict]\n"
-            << "Discrete Ordinates Mini-App, fixed-source and eigenvalue paths on the GPU.\n";
+            << "Discrete Ordinates Mini-App, fixed-source, eigenvalue and transient paths on the GPU.\n";
 }
 
 template <typename Solver, typename Mesh>
@@ -33,10 +33,19 @@ int run(Mesh & mesh, const InputParameters & params, bool verbose, unsigned thre
         const std::chrono::high_resolution_clock::time_point & start)
 {
   Solver solver(mesh, params, verbose, threads);
-  const bool eigen = params._mode == RunMode::Eigen;
-  if (eigen ? solver.solveEigenvalue(base) : solver.solveFixedSource(base)) {
-    std::cout << (eigen ? "Eigenvalue solver finished executing." : "Fixed source solver finished executing.")
-              << std::endl;
+  bool ok = false;
+  const char * done = "Fixed source solver finished executing.";
+  if (params._mode == RunMode::Eigen) {
+    ok = solver.solveEigenvalue(base);
+    done = "Eigenvalue solver finished executing.";
+  } else if (params._mode == RunMode::Transient) {
+    ok = solver.solveTransient(base);
+    done = "Transient solver finished executing.";
+  } else {
+    ok = solver.solveFixedSource(base);
+  }
+  if (ok) {
+    std::cout << done << std::endl;
     const auto stop = std::chrono::high_resolution_clock::now();
     std::cout << "Time elapsed: " << std::chrono::duration_cast<std::chrono::seconds>(stop - start).count()
               << " (s)." << std::endl;
@@ -71,10 +80,6 @@ int main(int argc, char ** argv)
     const InputParameters params = parseInputParameters(path.string());
     const std::string base = (path.parent_path() / path.stem()).string();
     const auto start = std::chrono::high_resolution_clock::now();
-    if (params._mode == RunMode::Transient) {
-      std::cerr << "Transient decks do not run on the GPU library (steady and eigenvalue decks do)." << std::endl;
-      return 1;
-    }
     if (params._num_dims == 3) {
       std::array<BoundaryCondition, 6u> bcs;
       bcs.fill(BoundaryCondition::Vacuum);

@@ -219,6 +219,80 @@ class Problem:
         )
 
 
+@dataclass
+class Transient:
+    """Time-dependent data of a transient solve, per material (the layout of
+    doma_transient).  Delayed-group arrays are padded to D = num_d_groups;
+    material m uses the first d_groups[m].  t1 is the end time handed to a
+    DOMA deck (t0 = 0); dt = t1 / num_steps."""
+
+    t1: float
+    num_steps: int
+    inv_v: np.ndarray
+    d_groups: np.ndarray | None = None
+    chi_d: np.ndarray | None = None
+    beta: np.ndarray | None = None
+    lambda_: np.ndarray | None = None
+    step_type: np.ndarray | None = None
+    step_insert: np.ndarray | None = None
+    step_remove: np.ndarray | None = None
+    step_source: np.ndarray | None = None
+
+    def __post_init__(self):
+        self.inv_v = np.ascontiguousarray(self.inv_v, dtype=np.float64)
+        M, G = self.inv_v.shape
+        if self.d_groups is not None:
+            self.d_groups = np.ascontiguousarray(self.d_groups, dtype=np.uint32).reshape(M)
+            D = int(self.d_groups.max()) if M else 0
+            self.chi_d = np.ascontiguousarray(self.chi_d, dtype=np.float64).reshape(M, G, D)
+            self.beta = np.ascontiguousarray(self.beta, dtype=np.float64).reshape(M, G, D)
+            self.lambda_ = np.ascontiguousarray(self.lambda_, dtype=np.float64).reshape(M, D)
+        if self.step_type is not None:
+            self.step_type = np.ascontiguousarray(self.step_type, dtype=np.uint32).reshape(M)
+            self.step_insert = np.ascontiguousarray(self.step_insert, dtype=np.float64).reshape(M)
+            self.step_remove = np.ascontiguousarray(self.step_remove, dtype=np.float64).reshape(M)
+            self.step_source = np.ascontiguousarray(self.step_source, dtype=np.float64).reshape(M, G)
+
+    @property
+    def dt(self) -> float:
+        return (self.t1 - 0.0) / float(self.num_steps)
+
+    @property
+    def num_d_groups(self) -> int:
+        return 0 if self.d_groups is None else int(self.chi_d.shape[2])
+
+    def times(self) -> list[float]:
+        """The times of the steps, accumulated as t += dt."""
+        t, out = 0.0, []
+        for _ in range(self.num_steps):
+            out.append(t)
+            t += self.dt
+        return out
+
+    def digest(self) -> str:
+        h = hashlib.sha256()
+        h.update(np.array([self.t1, float(self.num_steps)]).tobytes())
+        for a in (self.inv_v, self.d_groups, self.chi_d, self.beta, self.lambda_, self.step_type,
+                  self.step_insert, self.step_remove, self.step_source):
+            h.update(b"|" if a is None else np.ascontiguousarray(a).tobytes())
+        return h.hexdigest()
+
+    def to_c(self) -> abi.DomaTransient:
+        """A doma_transient pointing at this object's arrays (keep self alive)."""
+        dp = ctypes.POINTER(ctypes.c_double)
+        up = ctypes.POINTER(ctypes.c_uint32)
+
+        def ptr(a, t=dp):
+            return None if a is None else a.ctypes.data_as(t)
+
+        return abi.DomaTransient(
+            dt=self.dt, num_steps=self.num_steps, num_d_groups=self.num_d_groups,
+            inv_v=ptr(self.inv_v), d_groups=ptr(self.d_groups, up), chi_d=ptr(self.chi_d),
+            beta=ptr(self.beta), lambda_=ptr(self.lambda_), step_type=ptr(self.step_type, up),
+            step_insert=ptr(self.step_insert), step_remove=ptr(self.step_remove),
+            step_source=ptr(self.step_source))
+
+
 def make_options(scheme: str = "dd", theta: float = 0.9, precision: str = "fp64",
                  fs_tol: float = 1e-8, fs_max_it: int = 1000, mg_tol: float = 1e-8,
                  mg_max_it: int = 200, verbose: int = 0, tile=(0, 0, 0),
@@ -409,6 +483,63 @@ def random_problem(seed: int = 0, dims: int = 3, nx: int = 5, ny: int = 4, nz: i
         nsf[0] = r.uniform(G, 0.01, 0.1) * fission_scale
     return Problem(dims, dx, dy, dz, mat, sig, S, src, np_, na, has_fission=hf, chi_p=chi,
                    nu_sigma_f=nsf, name=f"random{dims}d_{nx}x{ny}x{nz}_g{G}_s{seed}")
+
+
+def transient_problem(seed: int = 0, dims: int = 3, nx: int = 6, ny: int = 5, nz: int = 4,
+                      groups: int = 3, np_: int = 1, na: int = 2, materials: int = 4,
+                      num_steps: int = 4, t1: float = 1.0, delayed: int = 3,
+                      steps: bool = True) -> tuple[Problem, Transient]:
+    """A random_problem with fission in materials 0 and 1 and the data of a
+    transient: inverse velocities U[0.5, 5]; `delayed` precursor groups in
+    material 0 and one fewer in material 1 (materials without fission have
+    none), beta ~ U[0.001, 0.01], lambda ~ U[0.05, 2], normalised chi_d; and,
+    with `steps`, a source step of each kind: material 1 on between t1/4 and
+    t1/2 (both ends), material 2 inserted at 0.3 t1, material 3 removed at
+    t1/2 (a removal time equal to a step time is still on)."""
+    if materials < 4:
+        raise ValueError("transient_problem needs at least 4 materials")
+    p = random_problem(seed, dims, nx, ny, nz, groups, np_, na, materials, fission=True)
+    r = Rng(seed, f"transient_{dims}")
+    G, M = groups, materials
+    hf = p.has_fission.copy()
+    chi, nsf = p.chi_p.copy(), p.nu_sigma_f.copy()
+    hf[1] = 1
+    chi[1] = r.uniform(G, 0.0, 1.0)
+    chi[1] /= chi[1].sum()
+    nsf[1] = r.uniform(G, 0.01, 0.1)
+    p = p.with_(has_fission=hf, chi_p=chi, nu_sigma_f=nsf, name=p.name + "_transient")
+    inv_v = r.uniform(M * G, 0.5, 5.0).reshape(M, G)
+    tr = Transient(t1=t1, num_steps=num_steps, inv_v=inv_v)
+    if delayed > 0:
+        D = delayed
+        dg = np.zeros(M, dtype=np.uint32)
+        dg[0], dg[1] = D, max(D - 1, 0)
+        chi_d = np.zeros((M, G, D))
+        beta = np.zeros((M, G, D))
+        lam = np.zeros((M, D))
+        for m in (0, 1):
+            d = int(dg[m])
+            if d == 0:
+                continue
+            cd = r.uniform(G * d, 0.0, 1.0).reshape(G, d)
+            chi_d[m, :, :d] = cd / cd.sum(axis=0, keepdims=True)
+            beta[m, :, :d] = r.uniform(G * d, 0.001, 0.01).reshape(G, d)
+            lam[m, :d] = r.uniform(d, 0.05, 2.0)
+        tr.d_groups, tr.chi_d, tr.beta, tr.lambda_ = dg, chi_d, beta, lam
+    if steps:
+        st = np.zeros(M, dtype=np.uint32)
+        ins = np.zeros(M)
+        rem = np.zeros(M)
+        ssrc = np.zeros((M, G))
+        st[1], ins[1], rem[1] = abi.DOMA_STEP_BOTH, 0.25 * t1, 0.5 * t1
+        st[2], ins[2] = abi.DOMA_STEP_INSERT, 0.3 * t1
+        st[3], rem[3] = abi.DOMA_STEP_REMOVE, 0.5 * t1
+        for m in range(M):
+            if st[m]:
+                ssrc[m] = r.uniform(G, 0.5, 3.0)
+        tr.step_type, tr.step_insert, tr.step_remove, tr.step_source = st, ins, rem, ssrc
+    tr.__post_init__()
+    return p, tr
 
 
 def square_2d(seed: int = 0, n: int = 32, groups: int = 2, np_: int = 2, na: int = 2,

@@ -102,6 +102,47 @@ class Solver:
                        si_residual=rep.si_residual, solve_ms=rep.solve_ms,
                        si_counts=counts[:n].copy()), float(k.value))
 
+    def solve_transient(self, transient, on_step=None, si_capacity: int = 1 << 16) -> Report:
+        """Transient solve from a zero initial condition (DOMA's solveTransient).
+        transient: problems.Transient.  on_step(step, t, phi[G][N], dnps[D][N])
+        is called after each step with copies of that step's flux and
+        precursors; a truthy return stops the solve.  -> report (si_counts over
+        every step; mg_iterations of the last step)."""
+        p = self.problem
+        G, N, D = p.num_groups, p.num_cells, transient.num_d_groups
+        counts = np.zeros(si_capacity, dtype=np.uint32)
+        rep = abi.DomaReport()
+        rep.si_counts = counts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        rep.si_counts_capacity = si_capacity
+        ct = transient.to_c()
+        errors = []
+
+        def _cb(user, step, t, phi, dnps):
+            if on_step is None:
+                return 0
+            try:
+                f = np.ctypeslib.as_array(phi, shape=(G * N,)).reshape(G, N).copy()
+                d = (np.ctypeslib.as_array(dnps, shape=(D * N,)).reshape(D, N).copy()
+                     if D else np.zeros((0, N)))
+                return 1 if on_step(int(step), float(t), f, d) else 0
+            except Exception as e:  # surfaced after the call returns
+                errors.append(e)
+                return 1
+
+        cb = abi.StepCallback(_cb)
+        st = self.lib.doma_solver_solve_transient(self._h, ctypes.byref(ct), cb, None,
+                                                  ctypes.byref(rep))
+        if errors:
+            raise errors[0]
+        abi.check(st, "doma_solver_solve_transient", self.lib,
+                  allow=(abi.DOMA_OK, abi.DOMA_NOT_CONVERGED))
+        n = min(rep.si_counts_len, si_capacity)
+        return Report(converged=st == abi.DOMA_OK, status=st, mg_iterations=rep.mg_iterations,
+                      si_iterations=rep.si_iterations, updates=rep.updates,
+                      kernel_launches=rep.kernel_launches, mg_residual=rep.mg_residual,
+                      si_residual=rep.si_residual, solve_ms=rep.solve_ms,
+                      si_counts=counts[:n].copy())
+
     def scalar_flux(self) -> np.ndarray:
         p = self.problem
         out = np.empty((p.num_groups, p.num_cells), dtype=np.float64)

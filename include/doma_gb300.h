@@ -24,6 +24,11 @@
  *                                      updateMultigroupSourceEigen / updateEigenvalue
  *                                      :404-456) and the 2D twin
  *                                      (src/TransportSolver2D.cpp:31-88, :406-456)
+ *   doma_solver_solve_transient        TransportSolver3D<T>::solveTransient with a zero
+ *                                      initial condition (src/TransportSolver3D.cpp:88-140,
+ *                                      initZeroIC / updateStepFluxes / stepDNPs :142-260,
+ *                                      the transient terms of updateMultigroupSource
+ *                                      :339-402) and the 2D twin
  *   doma_solver_get_scalar_flux        read-back of CartesianCell3D::_total_scalar_flux
  *                                      (include/CartesianCell3D.h:99), as used by
  *                                      BrickMesh3D::dumpToTextFile / fluxAtPoint
@@ -107,6 +112,41 @@ typedef struct doma_problem {
   uint32_t num_azimuthal;         /* na of <angular_quad>: 2*na Chebyshev roots */
 } doma_problem;
 
+/* Time-dependent data of a transient solve (DOMA's RunMode::Transient):
+ * the per-block fields of MaterialProps that only transients read
+ * (include/InputParameters.h:24-48) and the <source_step> blocks
+ * (SourceStep, include/InputParameters.h:9-22), indexed by material.  The
+ * delayed-group arrays are padded to num_d_groups; material m uses the first
+ * d_groups[m] of them (DOMA's _num_d_groups, which may differ per block). */
+typedef enum doma_step_type {
+  DOMA_STEP_NONE = 0,    /* no source step in this material */
+  DOMA_STEP_BOTH = 1,    /* on for insert_time <= t <= remove_time */
+  DOMA_STEP_INSERT = 2,  /* on for insert_time <= t */
+  DOMA_STEP_REMOVE = 3   /* on for t <= remove_time */
+} doma_step_type;
+
+typedef struct doma_transient {
+  double dt;                   /* step length; DOMA: (t1 - t0) / num_steps */
+  uint32_t num_steps;          /* time steps; the steps run at t = 0, dt, 2 dt, ... */
+  uint32_t num_d_groups;       /* D: delayed-neutron groups (the most of any material) */
+  const double *inv_v;         /* [M][G] inverse velocities */
+  const uint32_t *d_groups;    /* [M] delayed groups of each material (<= D), or NULL: none */
+  const double *chi_d;         /* [M][G][D] delayed spectra (DOMA's _n_g_chi_d, g*D_m + d) */
+  const double *beta;          /* [M][G][D] delayed fractions (DOMA's _g_n_beta, g*D_m + d) */
+  const double *lambda;        /* [M][D] decay constants */
+  const uint32_t *step_type;   /* [M] doma_step_type, or NULL: no source steps */
+  const double *step_insert;   /* [M] insertion times */
+  const double *step_remove;   /* [M] removal times */
+  const double *step_source;   /* [M][G] the stepped source */
+} doma_transient;
+
+/* Called after each time step of doma_solver_solve_transient with the step's
+ * scalar flux phi[g*N + cell] and precursor concentrations dnps[d*N + cell]
+ * (NULL when D = 0), both host memory valid during the call.  A nonzero
+ * return stops the solve (DOMA_BAD_INPUT with that message). */
+typedef int (*doma_step_callback)(void *user, uint32_t step, double t, const double *phi,
+                                  const double *dnps);
+
 /* Solver options (the <solver> block of a DOMA deck plus GPU choices). */
 typedef struct doma_options {
   uint32_t scheme;      /* DOMA_SCHEME_DD or DOMA_SCHEME_TW_DD */
@@ -186,6 +226,20 @@ doma_status doma_solver_solve_fixed_source(doma_solver *solver, doma_report *rep
  * false).  Gauss-Seidel iteration mode only. */
 doma_status doma_solver_solve_eigenvalue(doma_solver *solver, double k_tol, doma_report *report,
                                          double *k);
+
+/* Time-dependent fixed-source solve from a zero initial condition: at each
+ * step the Gauss-Seidel / source-iteration solve of doma_solver_solve_fixed_source
+ * with the transient source terms (source steps, prompt fission scaled by
+ * 1 - beta, delayed neutrons, the previous step's flux times inv_v / dt), then
+ * the precursor update, then `callback` (may be NULL), then the previous-step
+ * flux := this step's.  Returns DOMA_OK, or DOMA_NOT_CONVERGED as soon as a
+ * step's solve reaches a cap (DOMA's false).  report covers the last step.
+ * Gauss-Seidel iteration mode only.  DOMA's steady-state initial condition is
+ * not offered: the reference's version reads the precursor and previous-step
+ * arrays before it sizes them. */
+doma_status doma_solver_solve_transient(doma_solver *solver, const doma_transient *tr,
+                                        doma_step_callback callback, void *user,
+                                        doma_report *report);
 
 /* Copy the scalar flux to host memory: out[g*N + cell], N = nx*ny*nz. */
 doma_status doma_solver_get_scalar_flux(doma_solver *solver, double *out, size_t count);

@@ -627,6 +627,166 @@ int oracle_solve_eigen(const doma_problem *p, const doma_options *o, double k_to
   return ok;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Transient fixed source from a zero initial condition:
+ * TransportSolver3D::solveTransient (src/TransportSolver3D.cpp:88-140) with
+ * initZeroIC, updateStepFluxes and stepDNPs (:142-260), and the transient
+ * terms of updateMultigroupSource (:339-402; 2D: TransportSolver2D.cpp).
+ * Kept as DOMA has them: the delayed-neutron and time terms sit inside the
+ * loop over source groups g', so each is added G times; the 3D cell solve
+ * does not see the 1/(v dt) term (the sweep is not handed the mode), the 2D
+ * one does (tot = sigma_t + inv_v / dt). */
+typedef struct {
+  const doma_transient *tr;
+  unsigned D;
+  double *phi_last;   /* [G][N] */
+  double *dnps;       /* [N][D]: DOMA's _current_t_dnps (== _last_t_dnps between steps) */
+} transient_state;
+
+static unsigned mat_d(const transient_state *ts, unsigned m)
+{
+  return ts->tr->d_groups ? ts->tr->d_groups[m] : 0u;
+}
+
+static void mg_source_transient(oracle_state *s, const transient_state *ts, unsigned g, double t)
+{
+  const doma_problem *p = s->p;
+  const doma_transient *tr = ts->tr;
+  const unsigned G = s->G, D = ts->D;
+  const double a = s->src_scale, dt = tr->dt;
+  #pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < s->N; ++c) {
+    const unsigned m = p->cell_material[c];
+    const unsigned Dm = mat_d(ts, m);
+    s->cur[c] = 0.0;
+    double q = p->source ? a * p->source[(size_t)m * G + g] / M_PI : 0.0;
+    const unsigned st = tr->step_type ? tr->step_type[m] : 0u;
+    if (st != 0u) {
+      const double ins = tr->step_insert[m], rem = tr->step_remove[m];
+      const double v = a * tr->step_source[(size_t)m * G + g] / M_PI;
+      if (st == 1u) q += ins <= t && t <= rem ? v : 0.0;
+      else if (st == 2u) q += ins <= t ? v : 0.0;
+      else q += t <= rem ? v : 0.0;
+    }
+    const int fis = p->has_fission && p->has_fission[m];
+    for (unsigned gp = 0; gp < G; ++gp) {
+      const double pg = s->phi[(size_t)gp * s->N + c];
+      if (gp != g)
+        q += a * p->scatter[((size_t)m * G + g) * G + gp] * pg / M_PI;
+      if (fis && Dm == 0u)
+        q += a * p->chi_p[(size_t)m * G + g] * p->nu_sigma_f[(size_t)m * G + gp] * pg / M_PI;
+      else if (fis && Dm > 0u) {
+        double g_beta = 0.0;
+        for (unsigned d = 0; d < Dm; ++d) g_beta += tr->beta[((size_t)m * G + gp) * D + d];
+        q += a * (1.0 - g_beta) * p->chi_p[(size_t)m * G + g] * p->nu_sigma_f[(size_t)m * G + gp] *
+             pg / M_PI;
+      }
+      for (unsigned d = 0; d < Dm; ++d)
+        q += a * tr->chi_d[((size_t)m * G + g) * D + d] * ts->dnps[c * D + d] *
+             tr->lambda[(size_t)m * D + d] / M_PI;
+      q += a * ts->phi_last[(size_t)g * s->N + c] * tr->inv_v[(size_t)m * G + g] / dt / M_PI;
+    }
+    s->q[c] = q;
+    s->prev[(size_t)g * s->N + c] = s->phi[(size_t)g * s->N + c];
+    s->phi[(size_t)g * s->N + c] = 0.0;
+    s->sigt[c] = p->total[(size_t)m * G + g];
+    if (s->dims == 2) s->sigt[c] += tr->inv_v[(size_t)m * G + g] / dt;
+  }
+}
+
+/* stepDNPs (src/TransportSolver3D.cpp:236-260) */
+static void step_dnps(oracle_state *s, transient_state *ts)
+{
+  const doma_problem *p = s->p;
+  const doma_transient *tr = ts->tr;
+  const unsigned G = s->G, D = ts->D;
+  for (size_t c = 0; c < s->N; ++c) {
+    const unsigned m = p->cell_material[c];
+    const unsigned Dm = mat_d(ts, m);
+    for (unsigned d = 0; d < Dm; ++d) {
+      double c_src = 0.0;
+      for (unsigned g = 0; g < G; ++g)
+        c_src += p->nu_sigma_f[(size_t)m * G + g] * s->phi[(size_t)g * s->N + c] *
+                 tr->beta[((size_t)m * G + g) * D + d];
+      const double lam = tr->lambda[(size_t)m * D + d];
+      const double decay = exp(-lam * tr->dt);
+      ts->dnps[c * D + d] = (c_src / lam) * (1.0 - decay) + ts->dnps[c * D + d] * decay;
+    }
+  }
+}
+
+int oracle_solve_transient(const doma_problem *p, const doma_options *o, const doma_transient *tr,
+                           uint32_t num_threads, double *phi_steps, double *dnps_out,
+                           uint32_t *steps_done, uint32_t *si_counts, size_t si_cap,
+                           size_t *si_len)
+{
+  oracle_state s;
+  const unsigned T = num_threads ? num_threads : 1;
+  omp_set_num_threads((int)T);
+  if (!tr || !(tr->dt > 0.0) || !tr->inv_v) return -1;
+  if (tr->num_d_groups && (!tr->d_groups || !tr->chi_d || !tr->beta || !tr->lambda)) return -1;
+  if (tr->step_type && (!tr->step_insert || !tr->step_remove || !tr->step_source)) return -1;
+  if (state_init(&s, p, o, T)) { state_free(&s); return -1; }
+  transient_state ts;
+  ts.tr = tr;
+  ts.D = tr->num_d_groups;
+  ts.phi_last = calloc(s.N * s.G, sizeof(double));
+  ts.dnps = calloc(s.N * (ts.D ? ts.D : 1), sizeof(double));
+  size_t nsi = 0;
+  int ok = 1;
+  unsigned step = 0;
+  double t = 0.0;
+  for (; step < tr->num_steps; ++step) {
+    /* solveFixedSource("", t) in transient mode: no re-initialisation */
+    unsigned mg = 0;
+    double mres = 0.0;
+    do {
+      for (unsigned g = 0; g < s.G && ok; ++g) {
+        mg_source_transient(&s, &ts, g, t);
+        unsigned it = 0;
+        double res = 0.0;
+        do {
+          sweep(&s);
+          res = si_residual(&s, g);
+          si_update(&s, g);
+          ++it;
+        } while (it < o->fs_max_it && o->fs_tol < res);
+        if (si_counts && nsi < si_cap) si_counts[nsi] = it;
+        ++nsi;
+        if (!(it < o->fs_max_it)) ok = 0;
+      }
+      if (!ok) break;
+      mres = mg_residual(&s);
+      ++mg;
+    } while (mg < o->mg_max_it && o->mg_tol < mres && s.G > 1u);
+    if (ok && !(mg < o->mg_max_it)) ok = 0;
+    if (!ok) {
+      /* the reference returns with the failing step's partial flux in place */
+      if (phi_steps)
+        memcpy(phi_steps + (size_t)step * s.N * s.G, s.phi, sizeof(double) * s.N * s.G);
+      break;
+    }
+    step_dnps(&s, &ts);
+    if (phi_steps) memcpy(phi_steps + (size_t)step * s.N * s.G, s.phi, sizeof(double) * s.N * s.G);
+    if (step != tr->num_steps - 1u) {
+      /* updateStepFluxes */
+      memcpy(ts.phi_last, s.phi, sizeof(double) * s.N * s.G);
+      memset(s.phi, 0, sizeof(double) * s.N * s.G);
+      memset(s.q, 0, sizeof(double) * s.N);
+    }
+    t += tr->dt;
+  }
+  if (dnps_out && ts.D)
+    for (size_t c = 0; c < s.N; ++c)
+      for (unsigned d = 0; d < ts.D; ++d) dnps_out[(size_t)d * s.N + c] = ts.dnps[c * ts.D + d];
+  if (steps_done) *steps_done = step;
+  if (si_len) *si_len = nsi;
+  free(ts.phi_last);
+  free(ts.dnps);
+  state_free(&s);
+  return ok;
+}
+
 int oracle_source_iterations(const doma_problem *p, const doma_options *o,
                              uint32_t num_threads, uint32_t group, uint32_t count,
                              double *phi_out, double *residuals)

@@ -42,6 +42,17 @@ int oracle_solve_eigen(const doma_problem *p, const doma_options *o, double k_to
                        uint32_t *si_counts, size_t si_cap, size_t *si_len,
                        uint32_t *pi_iterations, double *shape_res_out, double *k_res_out);
 
+/* Transient fixed source from a zero initial condition (DOMA's
+ * solveTransient with TransientIC::Zero).  phi_steps ([num_steps][G][N], may
+ * be NULL) receives each step's flux, and for a step whose solve failed the
+ * partial flux it stopped with; dnps_out ([D][N], may be NULL) the precursor
+ * concentrations after the last step done; *steps_done the steps completed.  Returns 1 when every step converged, 0 when a step's solve
+ * reached a cap (the reference then returns false at once), -1 on bad input. */
+int oracle_solve_transient(const doma_problem *p, const doma_options *o, const doma_transient *tr,
+                           uint32_t num_threads, double *phi_steps, double *dnps_out,
+                           uint32_t *steps_done, uint32_t *si_counts, size_t si_cap,
+                           size_t *si_len);
+
 /* From a zero flux: set up group g's source, then run `count` source
  * iterations (sweep, residual, update) with no convergence test.  phi_out
  * ([G][N]) gets the flux afterwards; residuals ([count]) the SI residuals.

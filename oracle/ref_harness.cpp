@@ -1,6 +1,6 @@
 // ref_harness.cpp -- test infrastructure only.
 //
-// Drives DOMA's own fixed-source and eigenvalue solvers (the reference, compiled from its
+// Drives DOMA's own fixed-source, eigenvalue and transient solvers (the reference, compiled from its
 // unmodified sources by oracle/Makefile into oracle/_ref/libdoma_ref.so) from
 // a doma_problem description, so that the CPU restatement in oracle/ and the
 // GPU library can be pinned against the reference itself.  The product never
@@ -46,6 +46,14 @@ public:
       for (unsigned int g = 0; g < G; ++g)
         out[g * N + c] = mesh._cells[c]._total_scalar_flux[g];
   }
+  // _current_t_dnps as [D][N], zero where a cell has fewer than D groups.
+  static void readDNPs(const BrickMesh3D & mesh, unsigned int D, double * out)
+  {
+    const std::size_t N = mesh._cells.size();
+    for (std::size_t c = 0; c < N; ++c)
+      for (unsigned int d = 0; d < D; ++d)
+        out[d * N + c] = d < mesh._cells[c]._current_t_dnps.size() ? mesh._cells[c]._current_t_dnps[d] : 0.0;
+  }
 };
 
 template <>
@@ -58,6 +66,14 @@ public:
     for (std::size_t c = 0; c < N; ++c)
       for (unsigned int g = 0; g < G; ++g)
         out[g * N + c] = mesh._cells[c]._total_scalar_flux[g];
+  }
+  // _current_t_dnps as [D][N], zero where a cell has fewer than D groups.
+  static void readDNPs(const BrickMesh2D & mesh, unsigned int D, double * out)
+  {
+    const std::size_t N = mesh._cells.size();
+    for (std::size_t c = 0; c < N; ++c)
+      for (unsigned int d = 0; d < D; ++d)
+        out[d * N + c] = d < mesh._cells[c]._current_t_dnps.size() ? mesh._cells[c]._current_t_dnps[d] : 0.0;
   }
 };
 
@@ -246,6 +262,102 @@ ref_solve_eigen(const doma_problem * p, const doma_options * o, double k_tol,
     TransportSolver2D<OracleTap>::readFlux(mesh, p->num_groups, phi_out);
   }
   std::cout.precision(old_precision);
+  std::cout.rdbuf(old);
+  copyLog(captured.str(), log, log_cap);
+  return ok ? 1 : 0;
+}
+
+// Transient solve with the reference (solveTransient with TransientIC::Zero,
+// src/TransportSolver3D.cpp:88-140).  The transient inputs become material
+// properties and block step sources as InputParameters.cpp:286-500 would fill
+// them; t0 = 0 and t1 = num_steps * dt, so that the reference's own
+// dt = (t1 - t0) / num_steps is formed by the same division the caller used.
+// phi_out receives the last step's flux [G][N], dnps_out ([D][N]) its
+// precursors.  The reference writes its per-step text files under out_base.
+int
+ref_solve_transient(const doma_problem * p, const doma_options * o, const doma_transient * tr,
+                    double t1, unsigned int num_threads, double * phi_out, double * dnps_out,
+                    char * log, std::size_t log_cap, const char * out_base)
+{
+  omp_set_num_threads(static_cast<int>(num_threads));
+  InputParameters params = makeParams(p, o);
+  params._mode = RunMode::Transient;
+  params._t0 = 0.0;
+  params._t1 = t1;
+  params._num_steps = tr->num_steps;
+  params._ic = TransientIC::Zero;
+  const unsigned int G = p->num_groups, D = tr->num_d_groups;
+  for (unsigned int m = 0; m < p->num_materials; ++m)
+  {
+    MaterialProps & mp = params._block_mat_info.at(m);
+    mp._g_inv_v.assign(tr->inv_v + m * G, tr->inv_v + (m + 1) * G);
+    const unsigned int Dm = tr->d_groups ? tr->d_groups[m] : 0u;
+    mp._num_d_groups = Dm;
+    for (unsigned int g = 0; g < G; ++g)
+      for (unsigned int d = 0; d < Dm; ++d)
+      {
+        mp._n_g_chi_d.push_back(tr->chi_d[(std::size_t(m) * G + g) * D + d]);
+        mp._g_n_beta.push_back(tr->beta[(std::size_t(m) * G + g) * D + d]);
+      }
+    for (unsigned int d = 0; d < Dm; ++d)
+      mp._n_lambda.push_back(tr->lambda[std::size_t(m) * D + d]);
+    const unsigned int st = tr->step_type ? tr->step_type[m] : 0u;
+    if (st != 0u)
+    {
+      SourceStep step;
+      step._type = st == 1u ? StepType::Both : (st == 2u ? StepType::Insert : StepType::Remove);
+      step._insert_time = tr->step_insert[m];
+      step._remove_time = tr->step_remove[m];
+      step._g_src.assign(tr->step_source + m * G, tr->step_source + (m + 1) * G);
+      params._block_step_src.emplace(m, step);
+    }
+  }
+  const bool verbose = o->verbose >= 2;
+  const std::string base = out_base ? std::string(out_base) : std::string();
+
+  std::ostringstream captured;
+  std::streambuf * old = std::cout.rdbuf(captured.rdbuf());
+  bool ok = false;
+  if (p->num_dims == 3)
+  {
+    std::array<BoundaryCondition, 6u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh3D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver3D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveTransient(base);
+    }
+    else
+    {
+      TWDDTransportSolver3D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveTransient(base);
+    }
+    TransportSolver3D<OracleTap>::readFlux(mesh, G, phi_out);
+    if (dnps_out)
+      TransportSolver3D<OracleTap>::readDNPs(mesh, D, dnps_out);
+  }
+  else
+  {
+    std::array<BoundaryCondition, 4u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh2D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver2D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveTransient(base);
+    }
+    else
+    {
+      TWDDTransportSolver2D solver(mesh, params, verbose, num_threads);
+      ok = solver.solveTransient(base);
+    }
+    TransportSolver2D<OracleTap>::readFlux(mesh, G, phi_out);
+    if (dnps_out)
+      TransportSolver2D<OracleTap>::readDNPs(mesh, D, dnps_out);
+  }
   std::cout.rdbuf(old);
   copyLog(captured.str(), log, log_cap);
   return ok ? 1 : 0;

@@ -4,8 +4,11 @@
 //   host_check dump  <deck> <flux.bin> <base>    mesh from the deck, flux [G][N] from a
 //                                                raw float64 file, DOMA-layout text output
 //   host_check point <deck> <flux.bin> x y [z] g fluxAtPoint
-//   host_check solve <deck> <flux.bin> [verbose] drop-in solver on the GPU; writes the
-//                                                flux and prints SI counts (JSON)
+//   host_check solve <deck> <flux.bin> [verbose|quiet] [base]
+//                                                drop-in solver on the GPU (the deck's
+//                                                mode; a transient writes its step files
+//                                                under base); writes the flux and prints
+//                                                SI counts (JSON)
 #include <array>
 #include <cstdio>
 #include <cstdlib>
@@ -77,6 +80,27 @@ int main(int argc, char ** argv)
         json_list(kv.second->_g_src);
         std::cout << ", \"chi_p\": ";
         json_list(kv.second->_g_chi_p);
+        std::cout << ", \"delayed_groups\": " << kv.second->_num_d_groups << ", \"inv_v\": ";
+        json_list(kv.second->_g_inv_v);
+        std::cout << ", \"chi_d\": ";
+        json_list(kv.second->_n_g_chi_d);
+        std::cout << ", \"beta\": ";
+        json_list(kv.second->_g_n_beta);
+        std::cout << ", \"lambda\": ";
+        json_list(kv.second->_n_lambda);
+        std::cout << "}";
+        first = false;
+      }
+      std::cout << "}, \"t0\": " << p._t0 << ", \"t1\": " << p._t1 << ", \"t_steps\": "
+                << p._num_steps << ", \"ic\": " << (int)p._ic << ", \"steps\": {";
+      std::map<unsigned, const SourceStep *> steps;
+      for (const auto & kv : p._block_step_src) steps[kv.first] = &kv.second;
+      first = true;
+      for (const auto & kv : steps) {
+        std::cout << (first ? "" : ", ") << "\"" << kv.first << "\": {\"type\": "
+                  << (int)kv.second->_type << ", \"insert\": " << kv.second->_insert_time
+                  << ", \"remove\": " << kv.second->_remove_time << ", \"source\": ";
+        json_list(kv.second->_g_src);
         std::cout << "}";
         first = false;
       }
@@ -105,15 +129,17 @@ int main(int argc, char ** argv)
         bool ok;
         SolveStats st;
         const bool eigen = p._mode == RunMode::Eigen;
+        const bool transient = p._mode == RunMode::Transient;
+        const std::string base = argc > 5 ? argv[5] : "";
         double k = 0.0;
         if (p._eq_type == EquationType::DD) {
           DDTransportSolver3D s(mesh, p, verbose, 1);
-          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
           k = s.eigenvalue();
         } else {
           TWDDTransportSolver3D s(mesh, p, verbose, 1);
-          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
           k = s.eigenvalue();
         }
@@ -148,15 +174,17 @@ int main(int argc, char ** argv)
         bool ok;
         SolveStats st;
         const bool eigen = p._mode == RunMode::Eigen;
+        const bool transient = p._mode == RunMode::Transient;
+        const std::string base = argc > 5 ? argv[5] : "";
         double k = 0.0;
         if (p._eq_type == EquationType::DD) {
           DDTransportSolver2D s(mesh, p, verbose, 1);
-          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
           k = s.eigenvalue();
         } else {
           TWDDTransportSolver2D s(mesh, p, verbose, 1);
-          ok = eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
           st = s.stats();
           k = s.eigenvalue();
         }

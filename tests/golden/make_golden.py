@@ -5,6 +5,7 @@ Run from the repository root where the DOMA source tree is present:
     make -C oracle ref        # builds oracle/_ref/libdoma_ref.so from DOMA's sources
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py --eigen    # the k-eigenvalue fixtures only
+    python tests/golden/make_golden.py --transient  # the transient fixtures only
 
 Each case is a seeded synthetic problem (doma_gb300.problems) solved by DOMA
 (single thread, the bit-reproducible order).  A fixture stores the generator
@@ -94,8 +95,35 @@ EIGEN_CASES = {
                         {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-7, "mg_max_it": 4}, 1e-8),
 }
 
+# transient cases (zero initial condition): name -> (transient_problem kwargs, options kwargs).
+# Every step's flux is DOMA's: step k comes from a run of k steps with t1 = k dt, which
+# reproduces the first k steps exactly because (k dt) / k == dt for these dt.
+TRANSIENT_CASES = {
+    "transient3d_dd": ({"seed": 1, "dims": 3, "num_steps": 4, "delayed": 3},
+                       {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-9}),
+    "transient3d_twdd": ({"seed": 1, "dims": 3, "num_steps": 4, "delayed": 3},
+                         {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-9, "mg_tol": 1e-9}),
+    "transient2d_dd": ({"seed": 1, "dims": 2, "num_steps": 4, "delayed": 3},
+                       {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-9}),
+    "transient2d_twdd": ({"seed": 1, "dims": 2, "num_steps": 4, "delayed": 3},
+                         {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-9, "mg_tol": 1e-9}),
+    "transient3d_g1_nodelay_twdd": ({"seed": 4, "dims": 3, "groups": 1, "num_steps": 3,
+                                     "delayed": 0},
+                                    {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-9,
+                                     "mg_tol": 1e-9}),
+    "transient2d_thirds_twdd": ({"seed": 7, "dims": 2, "num_steps": 3, "t1": 1.0},
+                                {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-9,
+                                 "mg_tol": 1e-9}),
+    "transient3d_capped_mid_dd": ({"seed": 9, "dims": 3, "num_steps": 4},
+                                  {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-10,
+                                   "mg_max_it": 11}),
+    "transient2d_capped_si_dd": ({"seed": 6, "dims": 2, "num_steps": 4, "t1": 3.0},
+                                 {"scheme": "dd", "fs_tol": 1e-12, "fs_max_it": 12}),
+}
+
 # cases whose --verbose output (every SI residual) is also recorded
-VERBOSE_LOGS = {"capped_mg_dd", "capped_si_twdd", "random2d_dd", "eigen_capped_dd"}
+VERBOSE_LOGS = {"capped_mg_dd", "capped_si_twdd", "random2d_dd", "eigen_capped_dd",
+                "transient2d_dd"}
 
 QUAD_SETS = [(dims, np_, na) for dims in (2, 3)
              for (np_, na) in [(1, 1), (2, 2), (3, 3), (4, 4), (6, 6), (2, 5), (5, 2)]]
@@ -127,11 +155,48 @@ def make_eigen() -> None:
         print(f"{name:28s} converged={ok} pi={pi} k={k17} {dt:.2f}s")
 
 
+def make_transient() -> None:
+    import dataclasses
+    for name, (kw, okw) in TRANSIENT_CASES.items():
+        p, tr = P.transient_problem(**kw)
+        opts = P.make_options(**okw)
+        t0 = time.time()
+        phi, dnps, ok, si, log = ol.ref_solve_transient(p, tr, opts, threads=1)
+        dt = time.time() - t0
+        done = log.count("Solving timestep") - (0 if ok else 1)
+        steps = []
+        for k in range(1, done + 1):
+            if k == tr.num_steps:
+                steps.append(phi)
+                continue
+            t1k = k * tr.dt
+            assert t1k / k == tr.dt, (name, k)
+            trk = dataclasses.replace(tr, t1=t1k, num_steps=k)
+            phik, _, okk, _, _ = ol.ref_solve_transient(p, trk, opts, threads=1)
+            assert okk
+            steps.append(phik)
+        if not ok:
+            steps.append(phi)  # the partial flux the failing step stopped with
+        meta = {"generator": "transient_problem", "kwargs": kw, "options": okw,
+                "digest": p.digest(), "transient_digest": tr.digest(), "converged": ok,
+                "steps_done": done, "times": tr.times()[: len(steps)],
+                "reference_seconds": round(dt, 3), "log": log}
+        if name in VERBOSE_LOGS:
+            vopts = P.make_options(**okw, verbose=2)
+            meta["log_verbose"] = ol.ref_solve_transient(p, tr, vopts, threads=1)[4]
+        np.savez_compressed(HERE / f"{name}.npz", phi_steps=np.array(steps), dnps=dnps,
+                            si_counts=si, meta=np.array(json.dumps(meta)))
+        print(f"{name:28s} converged={ok} steps={done} si={len(si)} {dt:.2f}s")
+
+
 def main() -> None:
     if not ol.ref_available():
         raise SystemExit("oracle/_ref/libdoma_ref.so is missing: run `make -C oracle ref` first")
     if "--eigen" in sys.argv:
         make_eigen()
+        return
+    if "--transient" in sys.argv:
+        make_transient()
         return
     quad = {}
     for dims, np_, na in QUAD_SETS:
@@ -159,6 +224,7 @@ def main() -> None:
         print(f"{name:28s} converged={ok} mg={mg} si={list(map(int, si))[:8]}... "
               f"{dt:.2f}s")
     make_eigen()
+    make_transient()
 
 
 if __name__ == "__main__":

@@ -14,7 +14,7 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 def case_names():
     """The fixed-source fixtures."""
     return sorted(p.stem for p in GOLDEN.glob("*.npz")
-                  if p.stem != "quadrature" and not p.stem.startswith("eigen"))
+                  if p.stem != "quadrature" and not p.stem.startswith(("eigen", "transient")))
 
 
 def eigen_case_names():
@@ -35,6 +35,27 @@ def load_eigen_case(name: str):
            "k_is_final": meta["k_is_final"], "log": meta["log"],
            "log_verbose": meta.get("log_verbose")}
     return p, opts, meta["k_tol"], exp
+
+
+def transient_case_names():
+    """The transient (zero initial condition) fixtures."""
+    return sorted(p.stem for p in GOLDEN.glob("transient*.npz"))
+
+
+def load_transient_case(name: str):
+    """-> (problem, transient, options, expected dict).  phi_steps holds DOMA's
+    flux after each completed step and, when a step failed, the partial flux it
+    stopped with; dnps the precursors after the last completed step."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    meta = json.loads(str(z["meta"]))
+    p, tr = P.transient_problem(**meta["kwargs"])
+    if p.digest() != meta["digest"] or tr.digest() != meta["transient_digest"]:
+        raise AssertionError(f"{name}: regenerated inputs differ from the fixture's")
+    opts = P.make_options(**meta["options"])
+    exp = {"phi_steps": z["phi_steps"], "dnps": z["dnps"], "si_counts": z["si_counts"],
+           "converged": meta["converged"], "steps_done": meta["steps_done"],
+           "times": meta["times"], "log": meta["log"], "log_verbose": meta.get("log_verbose")}
+    return p, tr, opts, exp
 
 
 def load_case(name: str):

@@ -59,6 +59,12 @@ def oracle() -> ctypes.CDLL:
             ctypes.c_uint32, _dp, _dp, _u32p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
             _u32p, _dp, _dp,
         ]
+        lib.oracle_solve_transient.restype = ctypes.c_int
+        lib.oracle_solve_transient.argtypes = [
+            ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions),
+            ctypes.POINTER(abi.DomaTransient), ctypes.c_uint32, _dp, _dp, _u32p, _u32p,
+            ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
+        ]
         lib.oracle_multigroup_solve.restype = ctypes.c_int
         lib.oracle_multigroup_solve.argtypes = [
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
@@ -85,6 +91,12 @@ def ref() -> ctypes.CDLL:
         lib.ref_solve_eigen.argtypes = [
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_double,
             ctypes.c_uint32, ctypes.c_int, _dp, ctypes.c_char_p, ctypes.c_size_t,
+        ]
+        lib.ref_solve_transient.restype = ctypes.c_int
+        lib.ref_solve_transient.argtypes = [
+            ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions),
+            ctypes.POINTER(abi.DomaTransient), ctypes.c_double, ctypes.c_uint32, _dp, _dp,
+            ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p,
         ]
         lib.ref_quadrature.restype = ctypes.c_int
         lib.ref_quadrature.argtypes = [ctypes.c_uint32] * 3 + [_dp] * 4 + [_u32p]
@@ -212,3 +224,44 @@ def ref_solve_eigen(p: Problem, opts: abi.DomaOptions, k_tol: float, threads: in
     pi = _PI_RE.findall(log)
     k = _K_RE.findall(log)
     return (phi, bool(rc), si, (int(pi[-1]) if pi else None), (float(k[-1]) if k else None), log)
+
+
+def oracle_solve_transient(p: Problem, tr, opts: abi.DomaOptions, threads: int = 1):
+    """-> (phi_steps[S][G][N], dnps[D][N], converged, steps_done, si_counts)"""
+    S, G, N, D = tr.num_steps, p.num_groups, p.num_cells, tr.num_d_groups
+    phis = np.zeros((S, G, N))
+    dnps = np.zeros((max(D, 1), N))
+    done = ctypes.c_uint32(0)
+    cap = 1 << 16
+    si = np.zeros(cap, dtype=np.uint32)
+    n_si = ctypes.c_size_t(0)
+    cp, ct = p.to_c(), tr.to_c()
+    rc = oracle().oracle_solve_transient(ctypes.byref(cp), ctypes.byref(opts), ctypes.byref(ct),
+                                         threads, phis.ctypes.data_as(_dp),
+                                         dnps.ctypes.data_as(_dp), ctypes.byref(done),
+                                         si.ctypes.data_as(_u32p), cap, ctypes.byref(n_si))
+    if rc < 0:
+        raise ValueError("oracle rejected the problem")
+    return phis, dnps[:D], bool(rc), int(done.value), si[: min(n_si.value, cap)].copy()
+
+
+def ref_solve_transient(p: Problem, tr, opts: abi.DomaOptions, threads: int = 1,
+                        out_base: str | None = None):
+    """Run DOMA's solveTransient (zero initial condition).  -> (phi[G][N] of the
+    last step, dnps[D][N], converged, si_counts, log).  Without out_base the
+    reference's per-step text files go to a temporary directory."""
+    import tempfile
+    G, N, D = p.num_groups, p.num_cells, tr.num_d_groups
+    phi = np.zeros((G, N))
+    dnps = np.zeros((max(D, 1), N))
+    cap = 1 << 22
+    buf = ctypes.create_string_buffer(cap)
+    cp, ct = p.to_c(), tr.to_c()
+    with tempfile.TemporaryDirectory() as tmp:
+        base = out_base or os.path.join(tmp, "ref")
+        rc = ref().ref_solve_transient(ctypes.byref(cp), ctypes.byref(opts), ctypes.byref(ct),
+                                       tr.t1, threads, phi.ctypes.data_as(_dp),
+                                       dnps.ctypes.data_as(_dp), buf, cap, base.encode())
+    log = buf.value.decode()
+    si = np.array([int(m) for m in _SI_RE.findall(log)], dtype=np.uint32)
+    return phi, dnps[:D], bool(rc), si, log

@@ -13,7 +13,8 @@ import pytest
 import oracle_lib as ol
 from doma_gb300 import problems as P
 from doma_gb300.solver import Solver, quadrature
-from golden_cases import case_names, load_case, quadrature_sets, eigen_case_names, load_eigen_case
+from golden_cases import (case_names, eigen_case_names, load_case, load_eigen_case,
+                          load_transient_case, quadrature_sets, transient_case_names)
 
 pytestmark = pytest.mark.gpu
 
@@ -342,3 +343,164 @@ def test_eigenvalue_needs_fission_and_gauss_seidel():
     with Solver(p, P.make_options()) as s:
         with pytest.raises(abi.DomaError, match="fissile"):
             s.solve_eigenvalue(1e-6)
+
+
+# ---- transient (zero initial condition) -------------------------------------------
+
+def run_transient(p, tr, opts, stop_after=None):
+    """-> (per-step fluxes, per-step precursors, final flux, report)."""
+    phis, dnps = [], []
+
+    def on_step(step, t, phi, dn):
+        phis.append(phi)
+        dnps.append(dn)
+        return stop_after is not None and step >= stop_after
+
+    with Solver(p, opts) as s:
+        rep = s.solve_transient(tr, on_step)
+        return phis, dnps, s.scalar_flux(), rep
+
+
+@pytest.mark.parametrize("name", transient_case_names())
+def test_fp64_transient_matches_reference_golden(name):
+    """DOMA's solveTransient: same return value and SI counts, every step's
+    flux and the precursors within 1e-12 (relative L-infinity), including a
+    solve that stops part-way (its partial flux is the one DOMA keeps)."""
+    p, tr, opts, exp = load_transient_case(name)
+    phis, dnps, last, rep = run_transient(p, tr, opts)
+    assert rep.converged == exp["converged"]
+    assert len(phis) == exp["steps_done"]
+    assert list(rep.si_counts) == list(exp["si_counts"])
+    ref = exp["phi_steps"]
+    for k, phi in enumerate(phis):
+        assert rel_linf(phi, ref[k]) <= FP64_RTOL, k
+    assert rel_linf(last, ref[-1]) <= FP64_RTOL
+    if tr.num_d_groups and phis:
+        assert rel_linf(dnps[-1], exp["dnps"]) <= FP64_RTOL
+
+
+def test_fp64_transient_bit_equal_to_reference_golden():
+    """As for fixed source: the exact-order FP64 path gives DOMA's bits."""
+    unequal = []
+    for name in transient_case_names():
+        p, tr, opts, exp = load_transient_case(name)
+        phis, dnps, last, rep = run_transient(p, tr, opts)
+        for k, phi in enumerate(phis):
+            if not np.array_equal(phi, exp["phi_steps"][k]):
+                unequal.append((name, k, rel_linf(phi, exp["phi_steps"][k])))
+        if not np.array_equal(last, exp["phi_steps"][-1]):
+            unequal.append((name, "last", rel_linf(last, exp["phi_steps"][-1])))
+    assert not unequal, unequal
+
+
+@pytest.mark.parametrize("name", ["transient3d_twdd", "transient2d_dd",
+                                  "transient3d_capped_mid_dd", "transient2d_capped_si_dd"])
+def test_transient_graph_equals_host_loop(monkeypatch, name):
+    p, tr, opts, exp = load_transient_case(name)
+    a = run_transient(p, tr, opts)
+    monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    b = run_transient(p, tr, opts)
+    assert len(a[0]) == len(b[0])
+    assert all(np.array_equal(x, y) for x, y in zip(a[0], b[0]))
+    assert all(np.array_equal(x, y) for x, y in zip(a[1], b[1]))
+    assert np.array_equal(a[2], b[2])
+    ra, rb = a[3], b[3]
+    assert list(ra.si_counts) == list(rb.si_counts)
+    assert (ra.status, ra.mg_iterations, ra.si_iterations) == (rb.status, rb.mg_iterations,
+                                                               rb.si_iterations)
+
+
+@pytest.mark.parametrize("loop", ["graph", "host"])
+@pytest.mark.parametrize("name", transient_case_names())
+def test_transient_progress_lines_match_reference(monkeypatch, capfd, loop, name):
+    """solveTransient's stdout (initial conditions, time steps, MGI / SI lines)."""
+    p, tr, opts, exp = load_transient_case(name)
+    if loop == "host":
+        monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    opts.verbose = 1
+    capfd.readouterr()
+    with Solver(p, opts) as s:
+        s.solve_transient(tr)
+    assert capfd.readouterr().out == exp["log"]
+    if exp["log_verbose"] is not None:
+        opts.verbose = 2
+        with Solver(p, opts) as s:
+            s.solve_transient(tr)
+        assert capfd.readouterr().out == exp["log_verbose"]
+
+
+@pytest.mark.parametrize("seed", [31, 32])
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+@pytest.mark.parametrize("dims", [2, 3])
+def test_fp64_transient_matches_oracle_random(seed, scheme, dims):
+    p, tr = P.transient_problem(seed, dims=dims, nx=7, ny=6, nz=5, np_=2, na=2, num_steps=3,
+                                t1=0.6)
+    opts = P.make_options(scheme=scheme, theta=0.9, fs_tol=1e-10, mg_tol=1e-10)
+    phis, dnps, _, rep = run_transient(p, tr, opts)
+    o_phis, o_dnps, ok, done, si = ol.oracle_solve_transient(p, tr, opts)
+    assert rep.converged and ok and len(phis) == done == 3
+    assert list(rep.si_counts) == list(si)
+    for k in range(3):
+        assert rel_linf(phis[k], o_phis[k]) <= FP64_RTOL
+    assert rel_linf(dnps[-1], o_dnps) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+def test_fp32_transient_against_fp64(scheme):
+    """The FP32 sweep in a transient: each step's flux within 1e-5 (relative
+    L2) of the FP64 mode's."""
+    p, tr = P.transient_problem(41, dims=3, nx=12, ny=10, nz=8, np_=2, na=2, num_steps=3)
+    kw = dict(scheme=scheme, theta=0.9, fs_tol=1e-8, mg_tol=1e-8)
+    a = run_transient(p, tr, P.make_options(precision="fp64", **kw))
+    b = run_transient(p, tr, P.make_options(precision="fp32", **kw))
+    assert a[3].converged and b[3].converged
+    for x, y in zip(b[0], a[0]):
+        assert rel_l2(x, y) <= FP32_RTOL
+
+
+def test_transient_callback_stops_and_solver_is_reused():
+    """A nonzero callback return stops after that step (DOMA_BAD_INPUT with a
+    message); the same solver then runs a transient with more delayed groups
+    (tables regrown, step graph rebuilt) and a fixed-source solve, each
+    matching a fresh solver's bits."""
+    from doma_gb300 import abi
+    p, tr = P.transient_problem(5, dims=3, num_steps=4, delayed=2)
+    _, tr3 = P.transient_problem(5, dims=3, num_steps=4, delayed=3)
+    opts = P.make_options(fs_tol=1e-9, mg_tol=1e-9)
+    seen = []
+    with Solver(p, opts) as s:
+        with pytest.raises(abi.DomaError, match="callback stopped"):
+            s.solve_transient(tr, lambda k, t, phi, d: seen.append(k) or k == 1)
+        assert seen == [0, 1]
+        out = []
+        s.solve_transient(tr3, lambda k, t, phi, d: out.append((t, phi, d)) and False)
+        fixed = s.solve_fixed_source()
+        fixed_phi = s.scalar_flux()
+    fresh = run_transient(p, tr3, opts)
+    assert [t for t, _, _ in out] == tr3.times()
+    assert all(np.array_equal(x, y) for (_, x, _), y in zip(out, fresh[0]))
+    assert np.array_equal(out[-1][2], fresh[1][-1]) and out[-1][2].shape[0] == 3
+    phi, rep = run(p, opts)
+    assert np.array_equal(fixed_phi, phi) and fixed.si_counts.tolist() == rep.si_counts.tolist()
+
+
+def test_transient_rejects_bad_input():
+    """Transient input errors come back as DOMA_BAD_INPUT before any GPU work."""
+    import dataclasses
+
+    from doma_gb300 import abi
+    p, tr = P.transient_problem(6, dims=3, num_steps=2)
+    bad = [
+        dataclasses.replace(tr, t1=0.0),
+        dataclasses.replace(tr, step_remove=np.where(tr.step_type == 1, 0.0, tr.step_remove)),
+        dataclasses.replace(tr, d_groups=np.array([3, 2, 1, 0], dtype=np.uint32)),  # no fission in 2
+        dataclasses.replace(tr, lambda_=np.zeros_like(tr.lambda_)),
+    ]
+    with Solver(p, P.make_options()) as s:
+        for b in bad:
+            with pytest.raises(abi.DomaError) as e:
+                s.solve_transient(b)
+            assert e.value.status == abi.DOMA_BAD_INPUT
+    with Solver(p, P.make_options(iteration="multigroup")) as s:
+        with pytest.raises(abi.DomaError, match="Gauss-Seidel"):
+            s.solve_transient(tr)

@@ -53,6 +53,37 @@ def test_generated_deck_round_trips(host_check, tmp_path, dims):
         assert (len(mat["chi_p"]) > 0) == bool(p.has_fission[m])
 
 
+@pytest.mark.parametrize("dims", [2, 3])
+def test_transient_deck_round_trips(host_check, tmp_path, dims):
+    """A transient deck carries t1 / t_steps, each block's delayed-neutron data
+    (DOMA's [g * D_m + d] order) and the source steps of each kind."""
+    p, tr = P.transient_problem(3, dims=dims, num_steps=5, t1=2.0)
+    deck = write_deck(p, tmp_path / "t.xml", scheme="dd", transient=tr)
+    d = json.loads(run(host_check, "parse", deck).stdout)
+    assert d["mode"] == 2 and d["t0"] == 0.0 and d["t1"] == 2.0 and d["t_steps"] == 5
+    assert d["ic"] == 0
+    for m in range(p.num_materials):
+        mat = d["materials"][str(m)]
+        dm = int(tr.d_groups[m])
+        assert mat["delayed_groups"] == dm
+        assert np.array_equal(mat["inv_v"], tr.inv_v[m])
+        assert np.array_equal(mat["chi_d"], tr.chi_d[m, :, :dm].ravel())
+        assert np.array_equal(mat["beta"], tr.beta[m, :, :dm].ravel())
+        assert np.array_equal(mat["lambda"], tr.lambda_[m, :dm])
+    # DOMA's StepType values: Insert 0, Remove 1, Both 2
+    kinds = {1: 2, 2: 0, 3: 1}
+    steps = d["steps"]
+    assert sorted(map(int, steps)) == [m for m in range(p.num_materials) if tr.step_type[m]]
+    for k, v in steps.items():
+        m = int(k)
+        assert v["type"] == kinds[int(tr.step_type[m])]
+        assert np.array_equal(v["source"], tr.step_source[m])
+        if tr.step_type[m] in (1, 2):
+            assert v["insert"] == tr.step_insert[m]
+        if tr.step_type[m] in (1, 3):
+            assert v["remove"] == tr.step_remove[m]
+
+
 @pytest.mark.skipif(not REF_CASES.exists(), reason="DOMA's example decks are not present")
 def test_reference_decks_parse(host_check):
     decks = sorted(REF_CASES.glob("[23]D_*.xml")) + sorted(REF_CASES.glob("*/[23]D_*.xml"))
@@ -179,3 +210,63 @@ def test_cli_runs_eigenvalue_decks(tmp_path):
     assert ok
     assert f"Converged value of k = {k:g}" in r.stdout
     assert (tmp_path / "core_g1_flux.txt").exists()
+
+
+def _read_column(path):
+    return np.array([float(x) for x in Path(path).read_text().split()])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,scheme", [(3, "dd"), (2, "tw_dd")])
+def test_dropin_transient_matches_oracle(host_check, tmp_path, dims, scheme):
+    """TransportSolver3D/2D::solveTransient on a transient deck: the flux it
+    ends with, the SI counts and DOMA's per-step text files (initial
+    condition, _t<step>_g<g>_flux.txt, _t<step>_d<d>_dnps.txt, where a cell
+    whose material has fewer delayed groups than the most prints 0) against
+    the CPU restatement of DOMA's transient."""
+    p, tr = P.transient_problem(15, dims=dims, nx=6, ny=5, nz=4, np_=2, na=2, num_steps=3,
+                                t1=0.6)
+    kw = dict(scheme=scheme, fs_tol=1e-10, mg_tol=1e-10)
+    deck = write_deck(p, tmp_path / "tr.xml", transient=tr, **kw)
+    base = tmp_path / "out" / "tr"
+    base.parent.mkdir()
+    d = json.loads(run(host_check, "solve", deck, tmp_path / "phi.bin", "quiet", base)
+                   .stdout.splitlines()[-1])
+    phi = np.fromfile(tmp_path / "phi.bin").reshape(p.num_groups, p.num_cells)
+    o_phis, o_dnps, ok, done, si = ol.oracle_solve_transient(p, tr, P.make_options(**kw))
+    assert d["converged"] == ok and done == 3 and d["si_counts"] == list(map(int, si))
+    assert np.abs(phi - o_phis[-1]).max() <= 1e-12 * np.abs(o_phis[-1]).max()
+    assert (base.parent / "tr_dims.txt").exists()
+    assert not _read_column(base.parent / "tr_g0_flux.txt").any()   # the zero start
+    D = tr.num_d_groups
+    full = np.array([tr.d_groups[m] == D for m in p.cell_material])
+    for step in range(3):
+        for g in range(p.num_groups):
+            vals = _read_column(base.parent / f"tr_t{step}_g{g}_flux.txt")
+            assert np.allclose(vals, o_phis[step, g], rtol=6e-6, atol=0)
+        assert not (base.parent / f"tr_t{step}_dims.txt").exists()
+    for dd in range(D):
+        vals = _read_column(base.parent / f"tr_t2_d{dd}_dnps.txt")
+        assert np.allclose(vals, np.where(full, o_dnps[dd], 0.0), rtol=6e-6, atol=0)
+    assert not (base.parent / f"tr_t2_d{D}_dnps.txt").exists()
+
+
+@pytest.mark.gpu
+def test_cli_runs_transient_decks(tmp_path):
+    if not nb.CLI.exists():
+        nb.build()
+    p, tr = P.transient_problem(16, dims=3, nx=6, ny=6, nz=6, np_=1, na=2, num_steps=2, t1=0.5)
+    deck = write_deck(p, tmp_path / "pulse.xml", scheme="dd", mg_tol=1e-8, transient=tr)
+    r = subprocess.run([str(nb.CLI), "-i", str(deck)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout
+    assert out.startswith("Setting up initial conditions...\nSolving timestep 0...\n")
+    assert "Solving timestep 1..." in out and "Transient solver finished executing." in out
+    assert "Time elapsed:" in out
+    for f in ("pulse_dims.txt", "pulse_t0_g0_flux.txt", "pulse_t1_g2_flux.txt",
+              "pulse_t1_d0_dnps.txt"):
+        assert (tmp_path / f).exists(), f
+    steady = write_deck(p, tmp_path / "steady_ic.xml", scheme="dd", transient=tr)
+    steady.write_text(steady.read_text().replace('ics="zero"', 'ics="steady"'))
+    r = subprocess.run([str(nb.CLI), "-i", str(steady)], capture_output=True, text=True)
+    assert r.returncode == 1 and "zero initial conditions" in r.stderr

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 import oracle_lib as ol
-from golden_cases import case_names, eigen_case_names, load_case, load_eigen_case, quadrature_sets
+from golden_cases import (case_names, eigen_case_names, load_case, load_eigen_case,
+                          load_transient_case, quadrature_sets, transient_case_names)
 
 
 @pytest.mark.parametrize("dims,np_,na,mu,eta,xi,w,counts", quadrature_sets())
@@ -61,3 +62,36 @@ def test_oracle_eigenvalue_bitwise_equals_reference(name):
     if exp["k_is_final"]:
         assert k == exp["k"]
     assert np.array_equal(phi, exp["phi"]), np.abs(phi - exp["phi"]).max()
+
+
+@pytest.mark.parametrize("name", transient_case_names())
+def test_oracle_transient_bitwise_equals_reference(name):
+    """Transient from a zero initial condition: every step's flux, the
+    precursors and the SI counts exactly as DOMA's solveTransient produced
+    them, including a solve that fails part-way."""
+    p, tr, opts, exp = load_transient_case(name)
+    phis, dnps, ok, done, si = ol.oracle_solve_transient(p, tr, opts, threads=1)
+    assert ok == exp["converged"]
+    assert done == exp["steps_done"]
+    assert list(si) == list(exp["si_counts"])
+    n = len(exp["phi_steps"])
+    assert np.array_equal(phis[:n], exp["phi_steps"])
+    assert np.array_equal(dnps, exp["dnps"])
+
+
+def test_oracle_transient_threads_agree():
+    """Threads only split cells: the parallel oracle matches the serial one."""
+    p, tr, opts, exp = load_transient_case("transient3d_twdd")
+    a = ol.oracle_solve_transient(p, tr, opts, threads=1)
+    b = ol.oracle_solve_transient(p, tr, opts, threads=4)
+    assert np.abs(a[0] - b[0]).max() <= 1e-12 * np.abs(a[0]).max()
+    assert a[2] == b[2] and a[3] == b[3]
+
+
+def test_oracle_transient_rejects_bad_input():
+    from doma_gb300 import problems as P
+    p, tr = P.transient_problem(0, num_steps=2)
+    import dataclasses
+    bad = dataclasses.replace(tr, t1=0.0)
+    with pytest.raises(ValueError):
+        ol.oracle_solve_transient(p, bad, P.make_options())

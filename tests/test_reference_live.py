@@ -48,3 +48,40 @@ def test_oracle_eigenvalue_vs_live_reference(seed, scheme, dims):
     if ok_r:  # DOMA prints the final k only when the power iteration converged
         assert k_r == k_o
     assert np.array_equal(phi_r, phi_o)
+
+
+@pytest.mark.parametrize("seed", [51, 52])
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+@pytest.mark.parametrize("dims", [2, 3])
+def test_oracle_transient_vs_live_reference(seed, scheme, dims):
+    """Fresh seeds of the transient generator (3 delayed groups in one block,
+    2 in another, a source step of each kind) through DOMA's solveTransient:
+    the last step's flux, the precursors and every SI count, bit for bit."""
+    p, tr = P.transient_problem(seed, dims=dims, nx=6, ny=5, nz=4, np_=2, na=2, num_steps=5,
+                                t1=1.25)
+    opts = P.make_options(scheme=scheme, theta=0.9, fs_tol=1e-9, mg_tol=1e-9)
+    phis, dnps, ok, done, si = ol.oracle_solve_transient(p, tr, opts)
+    r_phi, r_dnps, r_ok, r_si, log = ol.ref_solve_transient(p, tr, opts)
+    assert ok == r_ok and done == log.count("Solving timestep")
+    assert list(si) == list(r_si)
+    assert np.array_equal(phis[done - 1], r_phi)
+    assert np.array_equal(dnps, r_dnps)
+
+
+def test_reference_transient_writes_the_files_the_dropin_writes(tmp_path):
+    """DOMA's solveTransient file set for a run (initial condition, per-step
+    flux and precursor files) -- the layout the C++ drop-in reproduces."""
+    p, tr = P.transient_problem(53, dims=3, nx=4, ny=4, nz=3, num_steps=2, t1=0.5)
+    opts = P.make_options(scheme="dd", fs_tol=1e-8, mg_tol=1e-8)
+    ol.ref_solve_transient(p, tr, opts, out_base=str(tmp_path / "ref"))
+    names = sorted(f.name for f in tmp_path.iterdir())
+    G, D = p.num_groups, tr.num_d_groups
+    want = sorted(["ref_dims.txt", "ref_blocks.txt", "ref_meshx.txt", "ref_meshy.txt",
+                   "ref_meshz.txt"] + [f"ref_g{g}_flux.txt" for g in range(G)] +
+                  [f"ref_t{s}_g{g}_flux.txt" for s in range(2) for g in range(G)] +
+                  [f"ref_t{s}_d{d}_dnps.txt" for s in range(2) for d in range(D)])
+    assert names == want
+    # cells whose block has fewer delayed groups than the most print 0
+    full = np.array([tr.d_groups[m] == D for m in p.cell_material])
+    vals = np.array([float(x) for x in (tmp_path / "ref_t1_d0_dnps.txt").read_text().split()])
+    assert np.all(vals[~full] == 0.0) and np.all(vals[full] > 0.0)
