@@ -302,11 +302,21 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
     const double V = A.vol[c];
     double * ph = A.phi + (size_t)g * N + c;
     const double t = dA(*ph, d);
-    diff = dA(diff, dM(dM(d, d), V));
-    tot = dA(tot, dM(dM(t, t), V));
     *ph = t;
     const unsigned m = A.mat[c];
-    q_out[c] = (T)dD(dM(dM(A.src_scale, A.scatter[((size_t)m * G + g) * G + g]), d), kPi);
+    if (EXACT) {
+      // DOMA's association (src/TransportSolver3D.cpp:537-539, :553-556)
+      diff = dA(diff, dM(dM(d, d), V));
+      tot = dA(tot, dM(dM(t, t), V));
+      q_out[c] = (T)dD(dM(dM(A.src_scale, A.scatter[((size_t)m * G + g) * G + g]), d), kPi);
+    } else {
+      // FP32 sweeps: the FP64 pipe is the limit here (GB300 issues about two
+      // FP64 operations per SM per clock), so fused norms and one multiply
+      // by s * S_gg / pi replace DOMA's mul-mul-divide
+      diff = __fma_rn(dM(d, d), V, diff);
+      tot = __fma_rn(dM(t, t), V, tot);
+      q_out[c] = (T)dM(d, A.qcoef[(size_t)m * G + g]);
+    }
   }
   if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
     // sourceIteration's loop test (src/TransportSolver3D.cpp:481), on the device
@@ -656,7 +666,7 @@ doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * 
   if (precision == DOMA_PREC_FP64)
     si_epilogue_kernel<double, true><<<a.grid, kBlock, 0, st>>>(a, g, (double *)q, norms, L);
   else
-    si_epilogue_kernel<float, false><<<a.grid, kBlock, 0, st>>>(a, g, (float *)q, norms, L);
+    si_epilogue_kernel<float, false><<<a.epi_grid, kBlock, 0, st>>>(a, g, (float *)q, norms, L);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }

@@ -11,6 +11,7 @@ struct IterArgs {
   int G = 0;                  // groups
   int D = 0;                  // ordinates (exact-mode row length of wpsi)
   int grid = 0;               // fixed grid of every per-cell kernel
+  int epi_grid = 0;           // fixed grid of the FP32 source-iteration epilogue
   unsigned oct_mask = 0;      // octants that carry ordinates
   int ngroups = 1;            // fp32: ordinate groups per octant (partials per octant)
   bool exact = false;         // FP64 exact mode: the sweep wrote wpsi, not octphi
@@ -23,6 +24,7 @@ struct IterArgs {
   const uint8_t * fis = nullptr;      // [M] or null
   const double * chi = nullptr;       // [M][G]
   const double * nsf = nullptr;       // [M][G]
+  const double * qcoef = nullptr;     // [M][G] src_scale * S_gg / pi (FP32 epilogue)
   double * phi = nullptr;             // [G][N]
   double * prev = nullptr;            // [G][N]
   const double * wpsi = nullptr;      // exact: [groups in flight][N][D]

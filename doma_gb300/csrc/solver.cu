@@ -427,7 +427,9 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   DOMA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
   const size_t blocks_needed = (N + iteration_block() - 1) / iteration_block();
   const int grid = (int)std::max<size_t>(1, std::min<size_t>(blocks_needed, (size_t)sms * 8));
-  DOMA_TRY(dalloc(s, &s->d_partials, 2 * (size_t)grid));
+  // the FP32 epilogue's grid: fewer, longer threads amortise its FP64 block reduction
+  const int epi_grid = (int)std::max<size_t>(1, std::min<size_t>(blocks_needed, (size_t)sms * 3));
+  DOMA_TRY(dalloc(s, &s->d_partials, 2 * (size_t)std::max(grid, epi_grid)));
   DOMA_TRY(dalloc(s, &s->d_ticket, 1));
   DOMA_CUDA_TRY(cudaMemset(s->d_ticket, 0, sizeof(unsigned)));
   DOMA_TRY(dalloc(s, &s->d_ctl, 1));
@@ -485,7 +487,8 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   else
     fill(s->a32, (float *)nullptr);
   IterArgs & it = s->it;
-  it.N = N; it.G = s->G; it.D = s->D; it.grid = grid; it.oct_mask = s->oct_mask;
+  it.N = N; it.G = s->G; it.D = s->D; it.grid = grid; it.epi_grid = epi_grid;
+  it.oct_mask = s->oct_mask;
   it.ngroups = s->sched.ngroups;
   it.exact = exact;
   it.src_scale = s->dims == 3 ? 0.25 : 0.5;
@@ -493,6 +496,16 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   it.source = s->d_source; it.fis = s->d_fis; it.chi = s->d_chi; it.nsf = s->d_nsf;
   it.phi = s->d_phi; it.prev = s->d_prev; it.wpsi = s->d_wpsi; it.octphi = s->d_octphi;
   it.partials = s->d_partials; it.ticket = s->d_ticket;
+  {
+    std::vector<double> qc(M * G);
+    const double sc = it.src_scale;
+    for (size_t m = 0; m < M; ++m)
+      for (size_t g = 0; g < G; ++g)
+        qc[m * G + g] = sc * p->scatter[(m * G + g) * G + g] / M_PI;
+    double * d_qc = nullptr;
+    DOMA_TRY(upload(s, &d_qc, qc.data(), M * G));
+    it.qcoef = d_qc;
+  }
 
   DOMA_CUDA_TRY(cudaMemset(s->d_phi, 0, G * N * sizeof(double)));
   DOMA_CUDA_TRY(cudaMemset(s->d_prev, 0, G * N * sizeof(double)));

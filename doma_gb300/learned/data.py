@@ -24,6 +24,7 @@ import torch
 
 from .. import problems as P
 from ..solver import Batch
+from .net import IN_CHANNELS
 
 # Feature scaling, identical to kFeatSigma / kFeatAbs* in csrc/accel.cuh.
 FEAT_SIGMA = 0.8
@@ -197,5 +198,122 @@ def generate(problems: list[P.Problem], k_max: int = 10, tol: float = 1e-6,
             log(f"  generated {min(c0 + chunk, len(problems))}/{len(problems)} problems, "
                 f"{time.perf_counter() - t0:.1f} s")
     stream.synchronize()
+    return PairSet(torch.stack(Rs), torch.stack(Zs), torch.stack(Fs), n, iters,
+                   time.perf_counter() - t0, kept)
+
+
+def correction(net, delta: torch.Tensor, kappa: torch.Tensor, fsig: torch.Tensor,
+               fabs_: torch.Tensor, n: int) -> torch.Tensor:
+    """The solver's correction step (csrc/accel.cuh) in torch, batched over
+    problems: delta [B][G][N] -> Delta [B][G][N] float32, with the y chain
+    across groups.  kappa, fsig, fabs_: [B][G][N] float32 on the GPU."""
+    B, G, N = delta.shape
+    dev = delta.device
+    y = torch.zeros((B, N), dtype=torch.float32, device=dev)
+    out = torch.empty((B, n, n, n), dtype=torch.float32, device=dev)
+    corr = torch.empty((B, G, N), dtype=torch.float32, device=dev)
+    for g in range(G):
+        kg = kappa[:, g]
+        r = delta[:, g].float() + kg * y
+        s = r.pow(2).mean(dim=1, keepdim=True).sqrt().clamp_min(1e-30)
+        x = torch.zeros((B, N, IN_CHANNELS), dtype=torch.float32, device=dev)
+        x[..., 0] = r / s
+        x[..., 1] = fsig[:, g]
+        x[..., 2] = fabs_[:, g]
+        net.forward(x.to(torch.bfloat16).view(B, n, n, n, IN_CHANNELS).contiguous(), out)
+        z = s * out.view(B, N)
+        corr[:, g] = z + kg * y
+        y = z + r
+    return corr
+
+
+def generate_guided(problems: list[P.Problem], net, first: int = 6, interval: int = 6,
+                    corrections: int = 8, tol: float = 1e-6, max_it: int = 20000,
+                    chunk: int = 32, log=print) -> PairSet:
+    """Pairs from the states that the corrected iteration visits (DAgger):
+    each problem is solved to convergence once for phi*, then iterated again
+    from zero with a correction from `net` after `first` iterations and every
+    `interval` iterations after that, without the guard.  A correction is
+    applied the way the solver applies it: the next sweep takes delta + Delta,
+    and the stored increment becomes the sweep's result minus Delta.  The
+    states recorded are the one right after each correction and the one
+    each later correction is computed from, 2 * corrections - 1 per problem."""
+    t0 = time.perf_counter()
+    n = problems[0].nx
+    G = problems[0].num_groups
+    N = n ** 3
+    stream = torch.cuda.Stream()
+    net.set_stream(stream.cuda_stream)
+    Rs, Zs, Fs, iters, kept = [], [], [], [], []
+    with torch.cuda.stream(stream):
+        for c0 in range(0, len(problems), chunk):
+            part = problems[c0:c0 + chunk]
+            ref = Batch(part, scheme="dd", precision="fp32", fs_tol=tol, fs_max_it=max_it,
+                        iteration="multigroup")
+            ref.set_stream(stream.cuda_stream)
+            ref.begin()
+            ref.iterate(max_it)
+            reps = ref.reports()
+            stars = [device_view(ref.state_pointers(i)[0], G * N).view(G, N).float().clone()
+                     for i in range(len(part))]
+            ref.close()
+            feats = [features(p) for p in part]
+            fsig = torch.stack([torch.from_numpy(f[0]) for f in feats]).cuda()
+            fab = torch.stack([torch.from_numpy(f[1]) for f in feats]).cuda()
+            kap = torch.stack([torch.from_numpy(f[2]) for f in feats]).cuda()
+            b = Batch(part, scheme="dd", precision="fp32", fs_tol=0.0, fs_max_it=1 << 30,
+                      iteration="multigroup")
+            b.set_stream(stream.cuda_stream)
+            b.begin()
+
+            def state():
+                ph = torch.stack([device_view(b.state_pointers(i)[0], G * N).view(G, N)
+                                  for i in range(len(part))]).float()
+                de = torch.stack([device_view(b.state_pointers(i)[1], G * N).view(G, N)
+                                  for i in range(len(part))])
+                return ph, de
+
+            rec_phi, rec_delta = [], []
+            b.iterate(first)
+            for c in range(corrections):
+                phi, delta = state()
+                if c > 0:
+                    rec_phi.append(phi)
+                    rec_delta.append(delta.float())
+                corr = correction(net, delta, kap, fsig, fab, n).double()
+                inc = delta + corr
+                for i in range(len(part)):
+                    b.set_increment(i, inc[i].data_ptr())
+                b.iterate(1)
+                phi, dout = state()
+                fixed = (dout - corr).contiguous()
+                for i in range(len(part)):
+                    b.set_increment(i, fixed[i].data_ptr())
+                rec_phi.append(phi)
+                rec_delta.append(fixed.float())
+                if c + 1 < corrections and interval > 1:
+                    b.iterate(interval - 1)
+            b.close()
+            phis = torch.stack(rec_phi, dim=1)        # [P][K][G][N]
+            deltas = torch.stack(rec_delta, dim=1)
+            for i, p in enumerate(part):
+                if not reps[i].converged:
+                    log(f"  {p.name}: not converged ({reps[i].mg_residual:.2e}), skipped")
+                    continue
+                e = stars[i][None] - phis[i]
+                y = e + deltas[i]
+                yprev = torch.zeros_like(y)
+                yprev[:, 1:] = y[:, :-1]
+                coup = kap[i][None] * yprev
+                Rs.append(deltas[i] + coup)
+                Zs.append(e - coup)
+                Fs.append(torch.stack([fsig[i], fab[i]], dim=1))
+                iters.append(reps[i].mg_iterations)
+                kept.append(c0 + i)
+            torch.cuda.current_stream().synchronize()
+            log(f"  guided pairs {min(c0 + chunk, len(problems))}/{len(problems)} problems, "
+                f"{time.perf_counter() - t0:.1f} s")
+    stream.synchronize()
+    net.set_stream(None)
     return PairSet(torch.stack(Rs), torch.stack(Zs), torch.stack(Fs), n, iters,
                    time.perf_counter() - t0, kept)
