@@ -199,6 +199,46 @@ def run_reference(args):
 WEIGHTS = ROOT / "doma_gb300" / "learned" / "weights" / "unet_c32.npz"
 
 
+def drivers_leg(args):
+    """The eigenvalue and transient drivers on one fissile problem: 48^3 cells,
+    4 groups, 128 directions, FP32 DD sweeps (FP64 norms), fission in two of
+    four materials, 3 and 2 delayed groups and a source step of each kind.
+    Reports each driver's update rate and time, and the CPU restatement's
+    update rate (all host threads) on a bounded sample of the same sweeps."""
+    from doma_gb300 import problems as P
+    from doma_gb300.solver import Solver
+    p, tr = P.transient_problem(args.seed + 7, dims=3, nx=48, ny=48, nz=48, groups=4, np_=4,
+                                na=4, materials=4, num_steps=4, t1=0.4)
+    kw = dict(scheme="dd", precision="fp32", fs_tol=1e-6, fs_max_it=5000, mg_tol=1e-5,
+              mg_max_it=500)
+    out = {"workload": "48^3 cells, 4 groups, 8x16 directions, DD FP32, random materials "
+                       "(2 fissile), 4 transient steps of dt = 0.1"}
+    # power iteration to a shape residual of 1e-3 and |dk| <= 1e-4 (the kernels are
+    # warm from the legs before; the host-driven loop has no graph to build)
+    with Solver(p, P.make_options(**{**kw, "mg_tol": 1e-3, "mg_max_it": 1000})) as s:
+        rep, k = s.solve_eigenvalue(1e-4)
+    out["eigen"] = {"k": k, "converged": rep.converged, "power_iterations": rep.mg_iterations,
+                    "mg_tol": 1e-3, "k_tol": 1e-4,
+                    "sweeps": rep.si_iterations, "ms": rep.solve_ms,
+                    "ms_per_power_iteration": rep.solve_ms / max(rep.mg_iterations, 1),
+                    "gupdates": rep.updates / rep.solve_ms / 1e6}
+    with Solver(p, P.make_options(**kw)) as s:
+        s.solve_transient(tr)                            # warm
+        rep = s.solve_transient(tr)
+    out["transient"] = {"steps": tr.num_steps, "converged": rep.converged,
+                        "sweeps": rep.si_iterations, "ms": rep.solve_ms,
+                        "ms_per_step": rep.solve_ms / tr.num_steps,
+                        "gupdates": rep.updates / rep.solve_ms / 1e6}
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, dt, upd = cpu_sample(p, P.make_options(**{**kw, "precision": "fp64"}), threads,
+                                   args.driver_cpu_iters)
+        out["cpu_rate"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": f"{args.driver_cpu_iters} source iterations of group 0 "
+                                     f"({upd / 1e6:.1f} M updates, {dt:.1f} s)"}
+    return out
+
+
 def learned_leg(args):
     """Time to args.learned_target relative L2 error against the FP64 solution,
     plain multigroup FP32 source iteration vs the same with learned corrections,
@@ -388,6 +428,7 @@ def run_ours(args):
                          f"{dt:.1f} s), {threads} OpenMP threads over ordinates"}
 
     learned = learned_leg(args) if args.learned_problems > 0 else None
+    drivers = drivers_leg(args) if args.drivers else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -413,6 +454,7 @@ def run_ours(args):
         "roofline_all_groups": roof_all,
         "cpu_baseline": cpu,
         "learned": learned,
+        "drivers": drivers,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
@@ -442,6 +484,9 @@ def main():
     ap.add_argument("--all-groups-roofline", type=int, default=1,
                     help="also time the sweep with every group in flight (multigroup mode)")
     ap.add_argument("--learned-problems", type=int, default=1)
+    ap.add_argument("--drivers", type=int, default=1,
+                    help="also time the eigenvalue and transient drivers (0: skip)")
+    ap.add_argument("--driver-cpu-iters", type=int, default=20)
     ap.add_argument("--learned-n", type=int, default=64)
     ap.add_argument("--learned-target", type=float, default=1e-5)
     ap.add_argument("--accel-first", type=int, default=10)

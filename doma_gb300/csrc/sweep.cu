@@ -548,12 +548,24 @@ template <int DIMS, int TX>
 struct TaskSmemF32 {
   static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
   static constexpr int CELLS = TX * PY * PZ;
+  // Lane (jl, kl) is at il = s - (jl + kl) on step s.  Every per-step array is
+  // padded by the largest skew on both sides, so a lane reads at its own base
+  // plus s times the stride (a constant offset in the unrolled walk) with no
+  // clamp; reads outside its pencil land in finite data it discards.
+  static constexpr int SKEW = PY + PZ - 2;
+  static constexpr int FPAD = SKEW * kGroup;                   // face pad (floats), each side
   static constexpr int YF = PZ * TX * kGroup;                  // y faces [PZ][TX][kGroup]
   static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
-  // floats: faces, {q, sigma_t} per cell, x coefficients [kGroup][TX], 1/dx [TX] (2D TW-DD),
-  // ordinate-pair sums of w psi [kGroup / 2][CELLS]
-  static constexpr size_t floats = YF + ZF + 2 * CELLS + kGroup * TX + TX + (kGroup / 2) * CELLS;
+  static constexpr int YREG = YF + 2 * FPAD;
+  static constexpr int ZREG = DIMS == 3 ? ZF + 2 * FPAD : 0;
+  static constexpr int CREG = 2 * (CELLS + 2 * SKEW);          // {q, sigma_t} per cell
+  static constexpr int HREG = kGroup * TX + 2 * SKEW;          // x coefficients [kGroup][TX]
+  static constexpr int RREG = TX + 2 * SKEW;                   // 1/dx [TX] (2D TW-DD)
+  // floats: the padded regions, then ordinate-pair sums of w psi [kGroup / 2][CELLS]
+  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + (kGroup / 2) * CELLS;
   static constexpr size_t bytes = floats * sizeof(float);
+  static_assert(FPAD % 4 == 0 && YREG % 4 == 0, "face regions stay float4-aligned");
+  static_assert(CREG % 2 == 0 && (YREG + ZREG) % 2 == 0, "cell region stays float2-aligned");
 };
 
 // Coalesced, all-loads-first copy of `count` float4s: in each round every
@@ -613,12 +625,32 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   const int ob = A.oct_offset[o] + n0;
   const int ord = ob + min(nl, gs - 1);
 
-  float * yin = reinterpret_cast<float *>(smem_raw);
-  float * zin = yin + SM::YF;
-  float2 * cell = reinterpret_cast<float2 *>(zin + SM::ZF);     // {q, sigma_t}
-  float * hxs = reinterpret_cast<float *>(cell + CELLS);         // [kGroup][TX]
-  float * rlx = hxs + kGroup * TX;                               // [TX] 1/dx
-  float * P = rlx + TX;                                          // [kGroup / 2][CELLS]
+  constexpr int SKEW = SM::SKEW, FPAD = SM::FPAD;
+  float * const sbase = reinterpret_cast<float *>(smem_raw);
+  float * yin = sbase + FPAD;                                            // [PZ][TX][kGroup]
+  float * zin = sbase + SM::YREG + (DIMS == 3 ? FPAD : 0);               // [PY][TX][kGroup]
+  float2 * cell = reinterpret_cast<float2 *>(sbase + SM::YREG + SM::ZREG) + SKEW;  // {q, sigma_t}
+  float * hxs = sbase + SM::YREG + SM::ZREG + SM::CREG + SKEW;           // [kGroup][TX]
+  float * rlx = hxs - SKEW + SM::HREG + SKEW;                            // [TX] 1/dx
+  float * P = rlx - SKEW + SM::RREG;                                     // [kGroup / 2][CELLS]
+
+  // the pads: finite values for the reads of steps outside a lane's pencil
+  for (int e = t; e < FPAD; e += blockDim.x) {
+    yin[e - FPAD] = 0.f;
+    yin[SM::YF + e] = 0.f;
+    if constexpr (DIMS == 3) {
+      zin[e - FPAD] = 0.f;
+      zin[SM::ZF + e] = 0.f;
+    }
+  }
+  for (int e = t; e < SKEW; e += blockDim.x) {
+    cell[e - SKEW] = make_float2(0.f, 1.f);
+    cell[CELLS + e] = make_float2(0.f, 1.f);
+    hxs[e - SKEW] = 0.f;
+    hxs[kGroup * TX + e] = 0.f;
+    rlx[e - SKEW] = 0.f;
+    rlx[TX + e] = 0.f;
+  }
 
   auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
   auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
@@ -693,9 +725,12 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     // from an invalid step.
     const int d = jl + kl;
     const int ebase = (kl * PY + jl) * TX;
-    const int ybase = kl * TX * kGroup + nl;
-    const int zbase = jl * TX * kGroup + nl;
-    const int hbase = nl * TX;
+    // per-lane bases shifted by -d: step s reads element s of the lane's row
+    const float * yin_l = yin + (kl * TX - d) * kGroup + nl;
+    const float * zin_l = zin + (jl * TX - d) * kGroup + nl;
+    const float2 * cell_l = cell + (ebase - d);
+    const float * hx_l = hxs + (nl * TX - d);
+    const float * rlx_l = rlx - d;
     const bool ybound = active && jl == vy - 1;
     const bool zbound = DIMS == 3 && active && kl == vz - 1;
     float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
@@ -708,17 +743,16 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     for (int s = 0; s < STEPS; ++s) {
       const int il = s - d;
       const bool valid = active && (unsigned)il < (unsigned)vx;
-      const int ic = min(max(il, 0), TX - 1);
-      float y = jl == 0 ? yin[ybase + ic * kGroup] : ysh;
-      float z = DIMS == 3 ? (kl == 0 ? zin[zbase + ic * kGroup] : zsh) : 0.f;
-      const float2 qc = cell[ebase + ic];
-      const float hx = hxs[hbase + ic];
+      float y = jl == 0 ? yin_l[s * kGroup] : ysh;
+      float z = DIMS == 3 ? (kl == 0 ? zin_l[s * kGroup] : zsh) : 0.f;
+      const float2 qc = cell_l[s];
+      const float hx = hx_l[s];
       float xo = x, psi;
       if constexpr (DIMS == 3) {
         if constexpr (TW) psi = twdd3_fast(qc.x, qc.y, hx, cy_t, cz_t, th, om, xo, y, z);
         else psi = dd3_fast(qc.x, qc.y, hx, cy_t, cz_t, cyz, xo, y, z);
       } else {
-        if constexpr (TW) psi = twdd2_fast(qc.x, qc.y, hx, cy_t, fM(txy, rlx[ic]), th, om, xo, y);
+        if constexpr (TW) psi = twdd2_fast(qc.x, qc.y, hx, cy_t, fM(txy, rlx_l[s]), th, om, xo, y);
         else psi = dd2_fast(qc.x, qc.y, hx, cy_t, xo, y);
       }
       x = valid ? xo : x;

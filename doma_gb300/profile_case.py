@@ -3,11 +3,13 @@
     python -m doma_gb300.profile_case [--n 64] [--groups 8] [--np 4] [--na 4]
         [--precision fp32|fp64] [--scheme dd|tw_dd] [--tile 8] [--sweeps 3]
         [--solve] [--schedule persistent|levels] [--loop graph|host]
+        [--iteration gauss_seidel|multigroup]
 
 Builds the seeded checkerboard problem (doma_gb300.problems.checkerboard) on
 cuda:0, sets up group 0's source with one source iteration, then runs
 `--sweeps` bare sweeps (or, with --solve, one full fixed-source solve) and
-prints the solver's block shape and launch counts.  Device memory stays
+prints the solver's block shape and launch counts.  With --iteration
+multigroup every group is in flight in each sweep launch.  Device memory stays
 well under 1 GB at the default size.
 """
 from __future__ import annotations
@@ -33,6 +35,7 @@ def main() -> None:
     ap.add_argument("--schedule", choices=["persistent", "levels"], default="persistent")
     ap.add_argument("--loop", choices=["graph", "host"], default="graph",
                     help="host: host-driven solve loop (kernels profilable one by one)")
+    ap.add_argument("--iteration", choices=["gauss_seidel", "multigroup"], default="gauss_seidel")
     a = ap.parse_args()
     if a.schedule == "levels":
         os.environ["DOMA_SWEEP_SCHEDULE"] = "levels"
@@ -49,7 +52,8 @@ def main() -> None:
     o = P.make_options(scheme=a.scheme, theta=a.theta, precision=a.precision,
                        fs_tol=1e-6 if a.precision == "fp32" else 1e-8,
                        mg_tol=1e-6 if a.precision == "fp32" else 1e-8,
-                       fs_max_it=5000, mg_max_it=500, tile=(a.tile, 0, 0))
+                       fs_max_it=5000, mg_max_it=500, tile=(a.tile, 0, 0),
+                       iteration=a.iteration)
     with Solver(p, o) as s:
         t0 = time.perf_counter()
         if a.solve:
