@@ -80,6 +80,22 @@ def dist_env():
     return rank, world, local
 
 
+def aggregate(total_ms: float, units: float, world: int, device=None) -> tuple[float, float]:
+    """Whole-job figures of `world` replicas: the slowest rank's time and the
+    units (updates) of all ranks -> (units per second / 1e9, max total ms).
+    With world > 1 it needs an initialised process group (NCCL on GPUs, gloo
+    on CPUs); every rank gets the same result."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+        dist.all_reduce(u)
+        total_ms, units = float(t.item()), float(u.item())
+    return float(units) / (total_ms / 1e3) / 1e9, total_ms
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region."""
 
@@ -140,7 +156,10 @@ class ClockSampler:
 # dram__bytes_write.sum from one ncu capture of sweep_persistent_kernel, FP32
 # TW-DD, 64^3, 128 directions).  Far below the algorithmic bytes: the sweep's
 # working set stays in L2.
-SWEEP_DRAM_BYTES_PER_LAUNCH = 2_495_488 + 276_480
+SWEEP_DRAM_BYTES_PER_LAUNCH = 2_486_016 + 284_160
+# the same kernel with all 8 groups in flight: mean of two captured launches
+# (dram__bytes_read.sum + dram__bytes_write.sum)
+ALL_GROUPS_DRAM_BYTES_PER_LAUNCH = 29_305_216 + 141_568_128
 
 
 def measured_peak_hbm():
@@ -325,17 +344,7 @@ def run_ours(args):
             launches += rep.kernel_launches
             assert rep.converged
     torch.cuda.synchronize()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        u = torch.tensor([float(updates)], device=dev)
-        dist.all_reduce(u)
-        updates_all = float(u.item())
-    else:
-        updates_all = float(updates)
-    value = updates_all / (total_ms / 1e3) / 1e9
+    value, total_ms = aggregate(sum(step_ms), updates, world, dev)
     last_rep = rep
     phi32 = solver.scalar_flux()
 
@@ -379,7 +388,10 @@ def run_ours(args):
             mg_ms = e0.elapsed_time(e1) / nsw
         mg_achieved = b_upd * upd_sweep * p.num_groups / (mg_ms / 1e3) / 1e9
         roof_all = {"bound": "hbm", "achieved": mg_achieved, "peak": peak, "unit": "GB/s",
-                    "frac": mg_achieved / peak, "sweep_ms": mg_ms, "groups_in_flight": p.num_groups,
+                    "frac": mg_achieved / peak,
+                    "traffic": ALL_GROUPS_DRAM_BYTES_PER_LAUNCH if args.precision == "fp32" else None,
+                    "traffic_source": "ncu capture of two launches (dram__bytes_read + dram__bytes_write)",
+                    "sweep_ms": mg_ms, "groups_in_flight": p.num_groups,
                     "gupdates": upd_sweep * p.num_groups / (mg_ms / 1e3) / 1e9}
 
     # -- FP64 drop-in reference solution and its rate ----------------------------

@@ -532,13 +532,12 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
       if (nn < gs && il < vx && jj < vy) A.zf[F.z(j0 + jj, i0 + il) + nn] = zout[e];
     }
 
-  // -- publish completion (dataflow mode) ---------------------------------------------
+  // -- publish completion (dataflow mode): the barrier orders every thread's
+  // face stores before thread 0's release, and a release store is cumulative
+  // (PTX memory model), so the consumer's acquire sees them ---------------------------
   if (dataflow) {
     __syncthreads();
-    if (t == 0) {
-      __threadfence();
-      st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
-    }
+    if (t == 0) st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
   }
 }
 
@@ -769,11 +768,10 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   }
   __syncthreads();
 
-  // -- publish completion first: nothing downstream reads the scalar flux -------------
-  if (dataflow && t == 0) {
-    __threadfence();
-    st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
-  }
+  // -- publish completion first: nothing downstream reads the scalar flux.  The
+  // barrier above orders every thread's face stores before thread 0's release,
+  // and a release store is cumulative (PTX memory model) ------------------------------
+  if (dataflow && t == 0) st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
 
   // -- the slot's scalar-flux partial: Kahan over ordinate pairs, fixed order ----------
   for (int e = t; e < CELLS; e += blockDim.x) {
