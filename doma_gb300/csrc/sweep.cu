@@ -271,6 +271,21 @@ __device__ __forceinline__ void st_release(unsigned * p, unsigned v)
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Stores under a per-lane predicate, as predicated instructions: the unrolled
+// wavefront has no branch (and no reconvergence point) per conditional store.
+__device__ __forceinline__ void st_global_if(float * p, float v, bool c)
+{
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.f32 [%0], %1;\n\t}"
+               ::"l"(p), "f"(v), "r"((unsigned)c));
+}
+
+__device__ __forceinline__ void st_shared_if(float * p, float v, bool c)
+{
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.shared.f32 [%0], %1;\n\t}"
+               ::"r"(a), "f"(v), "r"((unsigned)c));
+}
+
 __device__ __forceinline__ unsigned ld_acquire(const unsigned * p)
 {
   unsigned v;
@@ -742,8 +757,14 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     for (int s = 0; s < STEPS; ++s) {
       const int il = s - d;
       const bool valid = active && (unsigned)il < (unsigned)vx;
-      float y = jl == 0 ? yin_l[s * kGroup] : ysh;
-      float z = DIMS == 3 ? (kl == 0 ? zin_l[s * kGroup] : zsh) : 0.f;
+      // unconditional loads (the padded rows are always in range), then a select
+      const float yl = yin_l[s * kGroup];
+      float y = jl == 0 ? yl : ysh;
+      float z = 0.f;
+      if constexpr (DIMS == 3) {
+        const float zl = zin_l[s * kGroup];
+        z = kl == 0 ? zl : zsh;
+      }
       const float2 qc = cell_l[s];
       const float hx = hx_l[s];
       float xo = x, psi;
@@ -756,11 +777,11 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
       }
       x = valid ? xo : x;
       const float wp = valid ? fM(wgt, psi) : 0.f;
-      if (valid && ybound) yout_g[il * kGroup] = y;
-      if (DIMS == 3 && valid && zbound) zout_g[il * kGroup] = z;
+      st_global_if(yout_g + il * kGroup, y, valid && ybound);
+      if constexpr (DIMS == 3) st_global_if(zout_g + il * kGroup, z, valid && zbound);
       // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
       const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
-      if (valid && lane < 16) P_lane[il] = pair;
+      st_shared_if(P_lane + il, pair, valid && lane < 16);
       ysh = __shfl_up_sync(FULL, y, 1);
       if (DIMS == 3) zsh = __shfl_up_sync(FULL, z, PY);
     }
