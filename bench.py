@@ -258,6 +258,32 @@ def drivers_leg(args):
     return out
 
 
+def batch_leg(args):
+    """The batched solve (off by default: about a minute): `--batch-problems`
+    independent problems drawn by batch_mix (n ~ U{16..96}, G in {1, 2, 4, 8,
+    16}, 2k x 4k directions with k ~ U{2..6}), FP32 DD multigroup iteration to
+    1e-6, every problem's sweep in one persistent launch per iteration.  The
+    block length is tuned first; the solve is timed alone."""
+    import torch
+
+    from doma_gb300 import problems as P
+    from doma_gb300.solver import Batch
+    ps = P.batch_mix(args.seed, count=args.batch_problems)
+    with Batch(ps, scheme="dd", precision="fp32", fs_tol=1e-6, fs_max_it=5000,
+               iteration="multigroup") as b:
+        tx = b.tune()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = b.solve()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    upd = sum(r.updates for r in reps)
+    its = [r.mg_iterations for r in reps]
+    return {"problems": len(ps), "tile_x": tx, "solve_s": dt, "gupdates": upd / dt / 1e9,
+            "converged": sum(r.converged for r in reps), "iterations_min": min(its),
+            "iterations_max": max(its), "updates": upd}
+
+
 def learned_leg(args):
     """Time to args.learned_target relative L2 error against the FP64 solution,
     plain multigroup FP32 source iteration vs the same with learned corrections,
@@ -441,6 +467,7 @@ def run_ours(args):
 
     learned = learned_leg(args) if args.learned_problems > 0 else None
     drivers = drivers_leg(args) if args.drivers else None
+    batch = batch_leg(args) if args.batch_problems > 0 else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -467,6 +494,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "learned": learned,
         "drivers": drivers,
+        "batch": batch,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
@@ -499,6 +527,8 @@ def main():
     ap.add_argument("--drivers", type=int, default=1,
                     help="also time the eigenvalue and transient drivers (0: skip)")
     ap.add_argument("--driver-cpu-iters", type=int, default=20)
+    ap.add_argument("--batch-problems", type=int, default=0,
+                    help="also time the batched solve of this many problems (256: the batched workload)")
     ap.add_argument("--learned-n", type=int, default=64)
     ap.add_argument("--learned-target", type=float, default=1e-5)
     ap.add_argument("--accel-first", type=int, default=10)
