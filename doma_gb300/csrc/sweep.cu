@@ -575,8 +575,9 @@ struct TaskSmemF32 {
   static constexpr int CREG = 2 * (CELLS + 2 * SKEW);          // {q, sigma_t} per cell
   static constexpr int HREG = kGroup * TX + 2 * SKEW;          // x coefficients [kGroup][TX]
   static constexpr int RREG = TX + 2 * SKEW;                   // 1/dx [TX] (2D TW-DD)
-  // floats: the padded regions, then ordinate-pair sums of w psi [kGroup / 2][CELLS]
-  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + (kGroup / 2) * CELLS;
+  // floats: the padded regions, the ordinate weights [kGroup], then psi per
+  // ordinate and cell [kGroup][CELLS] (weighted and summed after the walk)
+  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + kGroup + kGroup * CELLS;
   static constexpr size_t bytes = floats * sizeof(float);
   static_assert(FPAD % 4 == 0 && YREG % 4 == 0, "face regions stay float4-aligned");
   static_assert(CREG % 2 == 0 && (YREG + ZREG) % 2 == 0, "cell region stays float2-aligned");
@@ -646,7 +647,8 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   float2 * cell = reinterpret_cast<float2 *>(sbase + SM::YREG + SM::ZREG) + SKEW;  // {q, sigma_t}
   float * hxs = sbase + SM::YREG + SM::ZREG + SM::CREG + SKEW;           // [kGroup][TX]
   float * rlx = hxs - SKEW + SM::HREG + SKEW;                            // [TX] 1/dx
-  float * P = rlx - SKEW + SM::RREG;                                     // [kGroup / 2][CELLS]
+  float * wts = rlx - SKEW + SM::RREG;                                   // [kGroup] weights
+  float * P = wts + kGroup;                                              // [kGroup][CELLS] psi
 
   // the pads: finite values for the reads of steps outside a lane's pencil
   for (int e = t; e < FPAD; e += blockDim.x) {
@@ -696,13 +698,13 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const int nn = e / TX, il = e % TX;
     hxs[e] = (nn < gs && il < vx) ? fM(HS, A.cx[(size_t)(ob + nn) * nx + phys_i(il)]) : 0.f;
   }
+  for (int e = t; e < kGroup; e += blockDim.x) wts[e] = e < gs ? (float)A.wgt[ob + e] : 0.f;
   if (DIMS == 2 && TW)
     for (int e = t; e < TX; e += blockDim.x) rlx[e] = e < vx ? __frcp_rn(A.wx[phys_i(e)]) : 0.f;
   // per-thread constants of the pencil (clamped indices for inactive lanes)
   const float cy_t = fM(HS, A.cy[(size_t)ord * ny + phys_j(min(jl, vy - 1))]);
   const float cz_t = DIMS == 3 ? fM(HS, A.cz[(size_t)ord * nz + phys_k(min(kl, vz - 1))]) : 0.f;
   const float cyz = fA(cy_t, cz_t);
-  const float wgt = (float)A.wgt[ord];
   const float th = (float)A.theta, om = fS(1.0f, th);
   // 2D TW-DD: theta |xi| / (dx dy) = txy / dx
   const float txy = DIMS == 2 && TW ? fM(fM(th, A.axi_f[ord]), __frcp_rn(A.wy[phys_j(min(jl, vy - 1))])) : 0.f;
@@ -749,7 +751,7 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const bool zbound = DIMS == 3 && active && kl == vz - 1;
     float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
     float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl : nullptr;
-    float * P_lane = P + (nl >> 1) * CELLS + ebase;
+    float * P_lane = P + nl * CELLS + ebase;
     float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
     // 3D: fully unrolled; 2D (long skew) partly, which keeps it out of local memory
@@ -776,12 +778,9 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
         else psi = dd2_fast(qc.x, qc.y, hx, cy_t, xo, y);
       }
       x = valid ? xo : x;
-      const float wp = valid ? fM(wgt, psi) : 0.f;
       st_global_if(yout_g + il * kGroup, y, valid && ybound);
       if constexpr (DIMS == 3) st_global_if(zout_g + il * kGroup, z, valid && zbound);
-      // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
-      const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
-      st_shared_if(P_lane + il, pair, valid && lane < 16);
+      st_shared_if(P_lane + il, psi, valid);
       ysh = __shfl_up_sync(FULL, y, 1);
       if (DIMS == 3) zsh = __shfl_up_sync(FULL, z, PY);
     }
@@ -794,14 +793,13 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   // and a release store is cumulative (PTX memory model) ------------------------------
   if (dataflow && t == 0) st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
 
-  // -- the slot's scalar-flux partial: Kahan over ordinate pairs, fixed order ----------
+  // -- the slot's scalar-flux partial: Kahan over the ordinates' w psi, fixed order -----
   for (int e = t; e < CELLS; e += blockDim.x) {
     const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
     if (il < vx && jj < vy && kk < vz) {
       float sum = 0.0f, comp = 0.0f;
-      const int npairs = (gs + 1) >> 1;
-      for (int nn = 0; nn < npairs; ++nn) {
-        const float yv = fS(P[nn * CELLS + e], comp);
+      for (int nn = 0; nn < gs; ++nn) {
+        const float yv = fS(fM(wts[nn], P[nn * CELLS + e]), comp);
         const float tv = fA(sum, yv);
         comp = fS(fS(tv, sum), yv);
         sum = tv;
