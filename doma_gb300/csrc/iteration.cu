@@ -13,6 +13,8 @@
 // thread owns a fixed set of cells (fixed grid, grid-stride), blocks reduce
 // with a fixed shuffle tree, block partials go to a buffer, and the last block
 // to finish (one integer ticket) sums the partials in block order.
+#include <type_traits>
+
 #include "common.cuh"
 #include "iteration.cuh"
 
@@ -117,13 +119,23 @@ __global__ void __launch_bounds__(kBlock) mg_source_kernel(const IterArgs A, int
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
        c += (size_t)gridDim.x * blockDim.x) {
     const unsigned m = A.mat[c];
-    double q = A.source ? dD(dM(s, A.source[(size_t)m * G + g]), kPi) : 0.0;
-    const bool fis = A.fis && A.fis[m];
-    for (int gp = 0; gp < G; ++gp) {
-      const double pg = A.phi[(size_t)gp * N + c];
-      if (gp != g) q = dA(q, dD(dM(dM(s, A.scatter[((size_t)m * G + g) * G + gp]), pg), kPi));
-      if (fis)
-        q = dA(q, dD(dM(dM(dM(s, A.chi[(size_t)m * G + g]), A.nsf[(size_t)m * G + gp]), pg), kPi));
+    double q;
+    if constexpr (std::is_same<T, float>::value) {
+      // FP32 sweeps: one fused multiply-add per source group against the
+      // per-material table (GB300's FP64 pipe makes DOMA's divisions costly)
+      const double * cf = A.mgcoef + ((size_t)m * G + g) * G;
+      q = A.srcq[(size_t)m * G + g];
+      for (int gp = 0; gp < G; ++gp) q = __fma_rn(cf[gp], A.phi[(size_t)gp * N + c], q);
+    } else {
+      // DOMA's association (src/TransportSolver3D.cpp:350-380)
+      q = A.source ? dD(dM(s, A.source[(size_t)m * G + g]), kPi) : 0.0;
+      const bool fis = A.fis && A.fis[m];
+      for (int gp = 0; gp < G; ++gp) {
+        const double pg = A.phi[(size_t)gp * N + c];
+        if (gp != g) q = dA(q, dD(dM(dM(s, A.scatter[((size_t)m * G + g) * G + gp]), pg), kPi));
+        if (fis)
+          q = dA(q, dD(dM(dM(dM(s, A.chi[(size_t)m * G + g]), A.nsf[(size_t)m * G + gp]), pg), kPi));
+      }
     }
     q_out[c] = (T)q;
     sigt_out[c] = (T)A.total[(size_t)m * G + g];
@@ -138,9 +150,20 @@ __global__ void __launch_bounds__(kBlock) mg_source_kernel(const IterArgs A, int
 // reset it there); the external source does not enter.  Same association as
 // DOMA: ((s S) phi) / pi and ((((s chi) nu_sigma_f) phi) / pi) / k.
 template <typename T>
-__global__ void __launch_bounds__(kBlock) mg_source_eigen_kernel(const IterArgs A, int g, double k,
-                                                                 T * q, T * sigt_out)
+__global__ void __launch_bounds__(kBlock) mg_source_eigen_kernel(const IterArgs A, int g, double k_arg,
+                                                                 const double * k_dev, T * q,
+                                                                 T * sigt_out, const LoopParams L)
 {
+  if (L.graph) {
+    // a failed group ends the power iteration: leave the flux alone
+    const bool stop = L.ctl->failed != 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (!stop) L.ctl->si_it = 0u;
+      cudaGraphSetConditional(L.si_handle, stop ? 0u : 1u);
+    }
+    if (stop) return;
+  }
+  const double k = k_dev ? *k_dev : k_arg;   // a captured graph reads k from the device
   const size_t N = A.N;
   const int G = A.G;
   const double s = A.src_scale;
@@ -614,13 +637,16 @@ doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q,
   return DOMA_OK;
 }
 
-doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k, void * q,
-                                   void * sigt, cudaStream_t st)
+doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k,
+                                   const double * k_dev, void * q, void * sigt,
+                                   const LoopParams & L, cudaStream_t st)
 {
   if (precision == DOMA_PREC_FP64)
-    mg_source_eigen_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, k, (double *)q, (double *)sigt);
+    mg_source_eigen_kernel<double><<<a.grid, kBlock, 0, st>>>(a, g, k, k_dev, (double *)q,
+                                                             (double *)sigt, L);
   else
-    mg_source_eigen_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, k, (float *)q, (float *)sigt);
+    mg_source_eigen_kernel<float><<<a.grid, kBlock, 0, st>>>(a, g, k, k_dev, (float *)q,
+                                                            (float *)sigt, L);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }

@@ -25,6 +25,10 @@ struct IterArgs {
   const double * chi = nullptr;       // [M][G]
   const double * nsf = nullptr;       // [M][G]
   const double * qcoef = nullptr;     // [M][G] src_scale * S_gg / pi (FP32 epilogue)
+  // FP32 mode's group source: [M][G][G] s (S[g][g'] (g' != g) + chi_g nu_sigma_f_g') / pi
+  // and [M][G] s Q_g / pi
+  const double * mgcoef = nullptr;
+  const double * srcq = nullptr;
   double * phi = nullptr;             // [G][N]
   double * prev = nullptr;            // [G][N]
   const double * wpsi = nullptr;      // exact: [groups in flight][N][D]
@@ -101,9 +105,12 @@ doma_status launch_mg_source(const IterArgs & a, int g, int precision, void * q,
 doma_status launch_si_epilogue(const IterArgs & a, int g, int precision, void * q,
                                double * norms, const LoopParams & L, cudaStream_t st);
 // k-eigenvalue mode: group g's source added to the current one (in-scatter +
-// fission / k), and the starting flux (1 everywhere).
-doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k, void * q,
-                                   void * sigt, cudaStream_t st);
+// fission / k), and the starting flux (1 everywhere).  k comes from *k_dev
+// when that is not null (a captured graph), else from k; graph-aware like
+// launch_mg_source.
+doma_status launch_mg_source_eigen(const IterArgs & a, int g, int precision, double k,
+                                   const double * k_dev, void * q, void * sigt,
+                                   const LoopParams & L, cudaStream_t st);
 doma_status launch_eigen_init(const IterArgs & a, cudaStream_t st);
 // Transient mode: group g's source at the clock's t (external, source steps,
 // in-scatter, prompt fission (1 - beta), delayed neutrons, previous-step

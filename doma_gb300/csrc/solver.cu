@@ -134,6 +134,10 @@ struct doma_solver {
   // transient mode: device tables and state, allocated on first use for
   // tr_D delayed groups (grown, with the graph rebuilt, when a call needs
   // more); the captured Gauss-Seidel graph of a transient step
+  cudaGraph_t eg_graph = nullptr;        // k-eigenvalue: one power iteration's group loop
+  cudaGraphExec_t eg_exec = nullptr;
+  double * d_k = nullptr;                 // the k that graph reads
+  double * h_k = nullptr;                 // pinned staging of k
   TransientArgs tr{};
   int tr_D = 0;
   std::vector<void *> tr_allocs;
@@ -506,6 +510,26 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
     DOMA_TRY(upload(s, &d_qc, qc.data(), M * G));
     it.qcoef = d_qc;
   }
+  if (!exact && !s->mgi) {
+    // the FP32 Gauss-Seidel mode's group-source tables (mg_source_kernel<float>)
+    const double sc = it.src_scale;
+    std::vector<double> mc(M * G * G, 0.0), sq(M * G, 0.0);
+    for (size_t m = 0; m < M; ++m)
+      for (size_t g = 0; g < G; ++g) {
+        if (p->source) sq[m * G + g] = sc * p->source[m * G + g] / M_PI;
+        const bool fis = p->has_fission && p->has_fission[m];
+        for (size_t gp = 0; gp < G; ++gp) {
+          double v = gp != g ? p->scatter[(m * G + g) * G + gp] : 0.0;
+          if (fis) v += p->chi_p[m * G + g] * p->nu_sigma_f[m * G + gp];
+          mc[(m * G + g) * G + gp] = sc * v / M_PI;
+        }
+      }
+    double *d_mc = nullptr, *d_sq = nullptr;
+    DOMA_TRY(upload(s, &d_mc, mc.data(), M * G * G));
+    DOMA_TRY(upload(s, &d_sq, sq.data(), M * G));
+    it.mgcoef = d_mc;
+    it.srcq = d_sq;
+  }
 
   DOMA_CUDA_TRY(cudaMemset(s->d_phi, 0, G * N * sizeof(double)));
   DOMA_CUDA_TRY(cudaMemset(s->d_prev, 0, G * N * sizeof(double)));
@@ -525,6 +549,9 @@ void release(doma_solver * s)
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->h_phi) cudaFreeHost(s->h_phi);
   if (s->h_prev) cudaFreeHost(s->h_prev);
+  if (s->eg_exec) cudaGraphExecDestroy(s->eg_exec);
+  if (s->eg_graph) cudaGraphDestroy(s->eg_graph);
+  if (s->h_k) cudaFreeHost(s->h_k);
   if (s->tr_exec) cudaGraphExecDestroy(s->tr_exec);
   if (s->tr_graph) cudaGraphDestroy(s->tr_graph);
   for (void * p : s->tr_allocs) cudaFree(p);
@@ -835,13 +862,40 @@ struct GraphRun {
   std::vector<double> pres, mgh, sih;
 };
 
-void print_history(doma_solver * s, const GraphRun & run, bool banner)
+// sourceIteration's lines (src/TransportSolver3D.cpp:466-494) for one pass over
+// the groups, from a graph run's history starting at (pair, hist); false when
+// a group failed (the solve stops there).
+bool print_si_pass(doma_solver * s, const GraphRun & run, size_t & pair, size_t & hist)
 {
   const DevCtl & c = run.c;
   const std::vector<unsigned> & counts = run.counts;
-  const std::vector<double> &pres = run.pres, &mgh = run.mgh, &sih = run.sih;
-  const int G = s->G;
+  const std::vector<double> &pres = run.pres, &sih = run.sih;
   const int verbose = (int)s->opts.verbose;
+  for (int g = 0; g < s->G && pair < c.pairs; ++g, ++pair) {
+    const unsigned n = pair < counts.size() ? counts[pair] : 0u;
+    const double r = pair < pres.size() ? pres[pair] : 0.0;
+    if (verbose >= 2)
+      for (unsigned k = 0; k < n; ++k, ++hist) {
+        if (k != 0u && hist - 1 < sih.size())
+          std::printf("Performing SI %u for G%d, residual = %g\n", k, g, sih[hist - 1]);
+        else
+          std::printf("Performing SI %u for G%d\n", k, g);
+      }
+    if (n < s->opts.fs_max_it && !(c.failed && pair + 1 == c.pairs)) {
+      std::printf("SI converged after %u iterations with a residual of %g for G%d\n", n, r, g);
+    } else {
+      std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n", n, r, g);
+      return false;
+    }
+  }
+  return true;
+}
+
+void print_history(doma_solver * s, const GraphRun & run, bool banner)
+{
+  const DevCtl & c = run.c;
+  const std::vector<double> & mgh = run.mgh;
+  const int G = s->G;
   if (banner) std::printf("Solving...\nInitializing the solver...\n");
   size_t pair = 0, hist = 0;
   for (unsigned m = 0;; ++m) {
@@ -851,25 +905,7 @@ void print_history(doma_solver * s, const GraphRun & run, bool banner)
     else
       std::printf("Performing MGI %u\n", m);
     std::printf("----------------------------------------------------------------------------------\n");
-    bool stop = false;
-    for (int g = 0; g < G && pair < c.pairs; ++g, ++pair) {
-      const unsigned n = pair < counts.size() ? counts[pair] : 0u;
-      const double r = pair < pres.size() ? pres[pair] : 0.0;
-      if (verbose >= 2)
-        for (unsigned k = 0; k < n; ++k, ++hist) {
-          if (k != 0u && hist - 1 < sih.size())
-            std::printf("Performing SI %u for G%d, residual = %g\n", k, g, sih[hist - 1]);
-          else
-            std::printf("Performing SI %u for G%d\n", k, g);
-        }
-      if (n < s->opts.fs_max_it && !(c.failed && pair + 1 == c.pairs)) {
-        std::printf("SI converged after %u iterations with a residual of %g for G%d\n", n, r, g);
-      } else {
-        std::printf("SI failed to converge after %u iterations with a residual of %g for G%d\n", n, r, g);
-        stop = true;
-      }
-    }
-    if (stop) break;
+    if (!print_si_pass(s, run, pair, hist)) break;
   }
   if (!c.failed) {
     if (c.mg_it < s->opts.mg_max_it) {
@@ -948,6 +984,53 @@ uint64_t graph_launches(const doma_solver * s, const DevCtl & c)
       per_sweep += s->sched.level_begin[L + 1] > s->sched.level_begin[L];
   return c.sweeps * (per_sweep + 1) +
          (uint64_t)(c.mg_it + (c.failed ? 1 : 0)) * (uint64_t)(s->G + 1);
+}
+
+// One power iteration's group loop as a graph: per group the eigen source
+// (k read from the device) and the source-iteration WHILE loop; the power
+// iteration itself, with DOMA's host-side k update, stays on the host.
+doma_status build_eigen_graph(doma_solver * s)
+{
+  cudaStream_t c0 = nullptr, c2 = nullptr;
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
+  DOMA_CUDA_TRY(cudaStreamCreateWithFlags(&c2, cudaStreamNonBlocking));
+  auto run = [&]() -> doma_status {
+    cudaGraph_t root = nullptr;
+    DOMA_CUDA_TRY(cudaGraphCreate(&root, 0));
+    s->eg_graph = root;
+    std::vector<cudaGraphConditionalHandle> si_h(s->G);
+    for (int g = 0; g < s->G; ++g)
+      DOMA_CUDA_TRY(cudaGraphConditionalHandleCreate(&si_h[g], root, 0u, 0u));
+    DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c0, root, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+    doma_status st = DOMA_OK;
+    for (int g = 0; g < s->G && st == DOMA_OK; ++g) {
+      LoopParams L = loop_params(s, s->G);
+      L.si_handle = si_h[g];
+      st = launch_mg_source_eigen(s->it, g, s->opts.precision, 0.0, s->d_k, s->d_q, s->d_sigt, L, c0);
+      cudaGraph_t si_body = nullptr;
+      if (st == DOMA_OK) st = add_while(c0, si_h[g], &si_body);
+      if (st == DOMA_OK) {
+        DOMA_CUDA_TRY(cudaStreamBeginCaptureToGraph(c2, si_body, nullptr, nullptr, 0,
+                                                    cudaStreamCaptureModeThreadLocal));
+        st = launch_sweep(s->dims, s->opts.precision, s->opts.scheme, s->sched, &s->a64, &s->a32,
+                          c2, nullptr);
+        if (st == DOMA_OK)
+          st = launch_si_epilogue(s->it, g, s->opts.precision, s->d_q, s->d_ctl->norms, L, c2);
+        cudaGraph_t out = nullptr;
+        DOMA_CUDA_TRY(cudaStreamEndCapture(c2, &out));
+      }
+    }
+    cudaGraph_t out = nullptr;
+    DOMA_CUDA_TRY(cudaStreamEndCapture(c0, &out));
+    if (st != DOMA_OK) return st;
+    DOMA_CUDA_TRY(cudaGraphInstantiate(&s->eg_exec, root, 0));
+    return DOMA_OK;
+  };
+  const doma_status st = run();
+  cudaStreamDestroy(c0);
+  cudaStreamDestroy(c2);
+  return st;
 }
 
 doma_status solve_graph(doma_solver * s, doma_report * r)
@@ -1316,6 +1399,11 @@ doma_status solve_eigen_impl(doma_solver * s, double k_tol, doma_report * r, dou
   const size_t N = s->N;
   const auto t0 = std::chrono::steady_clock::now();
   const uint64_t launches0 = s->launches;
+  if (s->use_graph && !s->eg_exec) {
+    if (!s->d_k) DOMA_TRY(dalloc(s, &s->d_k, 1));
+    if (!s->h_k) DOMA_CUDA_TRY(cudaMallocHost(&s->h_k, sizeof(double)));
+    DOMA_TRY(build_eigen_graph(s));
+  }
   if (verbose) std::printf("Solving...\nInitializing the solver...\n");
   DOMA_TRY(launch_eigen_init(s->it, s->stream));
   ++s->launches;
@@ -1334,11 +1422,37 @@ doma_status solve_eigen_impl(doma_solver * s, double k_tol, doma_report * r, dou
         std::printf("Performing PI %u\n", t.mg);
       std::printf("----------------------------------------------------------------------------------\n");
     }
-    for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
-      DOMA_TRY(launch_mg_source_eigen(s->it, g, o.precision, k, s->d_q, s->d_sigt, s->stream));
-      ++s->launches;
-      status = group_source_iteration(s, g, r, t);  // a failed group: solveEigenvalue returns false
-      if (!reportable(status)) return status;
+    if (s->use_graph) {
+      // the group loop as one graph launch; k reaches it through device memory
+      *s->h_k = k;
+      DOMA_CUDA_TRY(cudaMemcpyAsync(s->d_k, s->h_k, sizeof(double), cudaMemcpyHostToDevice,
+                                    s->stream));
+      GraphRun run;
+      DOMA_TRY(graph_run(s, s->eg_exec, run));
+      if (verbose) {
+        size_t pair = 0, hist = 0;
+        print_si_pass(s, run, pair, hist);
+      }
+      if (run.c.failed) status = graph_status(s, run.c);   // solveEigenvalue returns false
+      uint64_t per_sweep = s->sched.persistent ? 1 : 0;
+      if (!s->sched.persistent)
+        for (size_t L = 0; L + 1 < s->sched.level_begin.size(); ++L)
+          per_sweep += s->sched.level_begin[L + 1] > s->sched.level_begin[L];
+      s->launches += run.c.sweeps * (per_sweep + 1) + (uint64_t)s->G;
+      t.sweeps += run.c.sweeps;
+      t.si_res = run.c.si_res;
+      if (r && r->si_counts)
+        for (size_t q = 0; q < run.counts.size(); ++q)
+          if (t.si_len + q < r->si_counts_capacity) r->si_counts[t.si_len + q] = run.counts[q];
+      t.si_len += run.c.pairs;
+    } else {
+      for (int g = 0; g < s->G && status == DOMA_OK; ++g) {
+        DOMA_TRY(launch_mg_source_eigen(s->it, g, o.precision, k, nullptr, s->d_q, s->d_sigt,
+                                        LoopParams{}, s->stream));
+        ++s->launches;
+        status = group_source_iteration(s, g, r, t);  // a failed group: solveEigenvalue returns false
+        if (!reportable(status)) return status;
+      }
     }
     if (status != DOMA_OK) break;
     k_prev = k;

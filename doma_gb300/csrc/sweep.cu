@@ -575,9 +575,13 @@ struct TaskSmemF32 {
   static constexpr int CREG = 2 * (CELLS + 2 * SKEW);          // {q, sigma_t} per cell
   static constexpr int HREG = kGroup * TX + 2 * SKEW;          // x coefficients [kGroup][TX]
   static constexpr int RREG = TX + 2 * SKEW;                   // 1/dx [TX] (2D TW-DD)
-  // floats: the padded regions, the ordinate weights [kGroup], then psi per
-  // ordinate and cell [kGroup][CELLS] (weighted and summed after the walk)
-  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + kGroup + kGroup * CELLS;
+  // The walk stores psi per ordinate and cell ([kGroup][CELLS]; weighted and
+  // summed after the walk) -- or, for long blocks whose array would cost a CTA
+  // per SM, w psi summed over ordinate pairs across half-warps ([kGroup / 2][CELLS]).
+  static constexpr bool PAIRS = CELLS >= 512;
+  static constexpr int PROWS = PAIRS ? kGroup / 2 : kGroup;
+  // floats: the padded regions, the ordinate weights [kGroup], then those sums
+  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + kGroup + PROWS * CELLS;
   static constexpr size_t bytes = floats * sizeof(float);
   static_assert(FPAD % 4 == 0 && YREG % 4 == 0, "face regions stay float4-aligned");
   static_assert(CREG % 2 == 0 && (YREG + ZREG) % 2 == 0, "cell region stays float2-aligned");
@@ -648,7 +652,8 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   float * hxs = sbase + SM::YREG + SM::ZREG + SM::CREG + SKEW;           // [kGroup][TX]
   float * rlx = hxs - SKEW + SM::HREG + SKEW;                            // [TX] 1/dx
   float * wts = rlx - SKEW + SM::RREG;                                   // [kGroup] weights
-  float * P = wts + kGroup;                                              // [kGroup][CELLS] psi
+  float * P = wts + kGroup;                                              // [PROWS][CELLS]
+  constexpr bool PAIRS = SM::PAIRS;
 
   // the pads: finite values for the reads of steps outside a lane's pencil
   for (int e = t; e < FPAD; e += blockDim.x) {
@@ -751,7 +756,8 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const bool zbound = DIMS == 3 && active && kl == vz - 1;
     float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
     float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl : nullptr;
-    float * P_lane = P + nl * CELLS + ebase;
+    float * P_lane = P + (PAIRS ? nl >> 1 : nl) * CELLS + ebase;
+    const float wgt = PAIRS ? wts[min(nl, kGroup - 1)] : 0.f;
     float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
     // 3D: fully unrolled; 2D (long skew) partly, which keeps it out of local memory
@@ -780,7 +786,14 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
       x = valid ? xo : x;
       st_global_if(yout_g + il * kGroup, y, valid && ybound);
       if constexpr (DIMS == 3) st_global_if(zout_g + il * kGroup, z, valid && zbound);
-      st_shared_if(P_lane + il, psi, valid);
+      if constexpr (PAIRS) {
+        // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
+        const float wp = valid ? fM(wgt, psi) : 0.f;
+        const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
+        st_shared_if(P_lane + il, pair, valid && lane < 16);
+      } else {
+        st_shared_if(P_lane + il, psi, valid);
+      }
       ysh = __shfl_up_sync(FULL, y, 1);
       if (DIMS == 3) zsh = __shfl_up_sync(FULL, z, PY);
     }
@@ -797,9 +810,21 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   for (int e = t; e < CELLS; e += blockDim.x) {
     const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
     if (il < vx && jj < vy && kk < vz) {
+      // Kahan over ordinate pairs: the stored pair sums, or the same pair sums
+      // formed here from per-ordinate psi (so every block length gives the same bits)
       float sum = 0.0f, comp = 0.0f;
-      for (int nn = 0; nn < gs; ++nn) {
-        const float yv = fS(fM(wts[nn], P[nn * CELLS + e]), comp);
+      const int npairs = (gs + 1) >> 1;
+      for (int nn = 0; nn < npairs; ++nn) {
+        float v;
+        if constexpr (PAIRS) {
+          v = P[nn * CELLS + e];
+        } else {
+          const int n0 = 2 * nn, n1 = n0 + 1;
+          const float a = fM(wts[n0], P[n0 * CELLS + e]);
+          const float b = n1 < gs ? fM(wts[n1], P[n1 * CELLS + e]) : 0.f;
+          v = fA(a, b);
+        }
+        const float yv = fS(v, comp);
         const float tv = fA(sum, yv);
         comp = fS(fS(tv, sum), yv);
         sum = tv;

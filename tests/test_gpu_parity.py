@@ -309,10 +309,14 @@ def test_fp64_eigenvalue_matches_reference_golden(name):
     assert rel_linf(phi, exp["phi"]) <= FP64_RTOL
 
 
+@pytest.mark.parametrize("loop", ["graph", "host"])
 @pytest.mark.parametrize("name", eigen_case_names())
-def test_eigenvalue_progress_lines_match_reference(capfd, name):
-    """The PI / SI progress lines of solveEigenvalue, line for line."""
+def test_eigenvalue_progress_lines_match_reference(monkeypatch, capfd, loop, name):
+    """The PI / SI progress lines of solveEigenvalue, line for line, with each
+    power iteration's group loop as a graph launch and as the host loop."""
     p, opts, k_tol, exp = load_eigen_case(name)
+    if loop == "host":
+        monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
     opts.verbose = 1
     capfd.readouterr()
     run_eigen(p, opts, k_tol)
@@ -321,6 +325,22 @@ def test_eigenvalue_progress_lines_match_reference(capfd, name):
         opts.verbose = 2
         run_eigen(p, opts, k_tol)
         assert capfd.readouterr().out == exp["log_verbose"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", ["eigen3d_twdd", "eigen2d_dd", "eigen_capped_dd"])
+def test_eigenvalue_graph_equals_host_loop(monkeypatch, precision, name):
+    """The group loop captured as a graph (k read from device memory) and the
+    host-driven loop give the same bits, k, counts and status."""
+    p, opts, k_tol, exp = load_eigen_case(name)
+    opts.precision = 0 if precision == "fp64" else 1
+    a, ra, ka = run_eigen(p, opts, k_tol)
+    monkeypatch.setenv("DOMA_SOLVE_LOOP", "host")
+    b, rb, kb = run_eigen(p, opts, k_tol)
+    assert np.array_equal(a, b) and ka == kb
+    assert list(ra.si_counts) == list(rb.si_counts)
+    assert (ra.status, ra.mg_iterations, ra.si_iterations) == (rb.status, rb.mg_iterations,
+                                                               rb.si_iterations)
 
 
 @pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
