@@ -310,18 +310,10 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
   const size_t N = A.N;
   const int G = A.G;
   double diff = 0.0, tot = 0.0;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
-       c += (size_t)gridDim.x * blockDim.x) {
-    double d = 0.0;
-    if (EXACT) {
-      const double * w = A.wpsi + c * (size_t)A.D;
-      for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
-    } else {
-      for (int o = 0; o < 8; ++o)
-        if (A.oct_mask & (1 << o))
-          for (int og = 0; og < A.ngroups; ++og)
-            d = dA(d, A.octphi[((size_t)o * A.ngroups + og) * N + c]);
-    }
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  // One cell's update after its increment d: phi, the norms (accumulated in
+  // the thread's cell order), the next source.
+  auto finish = [&](size_t c, double d) {
     const double V = A.vol[c];
     double * ph = A.phi + (size_t)g * N + c;
     const double t = dA(*ph, d);
@@ -339,6 +331,31 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
       diff = __fma_rn(dM(d, d), V, diff);
       tot = __fma_rn(dM(t, t), V, tot);
       q_out[c] = (T)dM(d, A.qcoef[(size_t)m * G + g]);
+    }
+  };
+  if constexpr (EXACT) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += stride) {
+      double d = 0.0;
+      const double * w = A.wpsi + c * (size_t)A.D;
+      for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
+      finish(c, d);
+    }
+  } else {
+    // two of the thread's cells per pass: their slot sums are independent
+    // chains of FP64 adds, interleaved; the cells still finish in order
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += 2 * stride) {
+      const size_t c2 = c + stride;
+      const bool two = c2 < N;
+      double da = 0.0, db = 0.0;
+      for (int o = 0; o < 8; ++o)
+        if (A.oct_mask & (1 << o))
+          for (int og = 0; og < A.ngroups; ++og) {
+            const double * part = A.octphi + ((size_t)o * A.ngroups + og) * N;
+            da = dA(da, part[c]);
+            if (two) db = dA(db, part[c2]);
+          }
+      finish(c, da);
+      if (two) finish(c2, db);
     }
   }
   if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
