@@ -690,14 +690,15 @@ doma_status launch_wgrad(const WgradArgs & a, int tiles, int splits, cudaStream_
 }  // namespace
 
 doma_status conv3_forward(const ConvShape & s, const bf16 * x, int cin, const bf16 * w,
-                          const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st)
+                          const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st,
+                          ConvScratch scratch)
 {
   static const bool mma_only = [] {
     const char * e = std::getenv("DOMA_CONV_PATH");
     return e && std::string(e) == "mma";
   }();
   if (!mma_only && conv3_tc_supported(s, cin, cout))
-    return conv3_forward_tc(s, x, cin, w, bias, cout, relu, y, st);
+    return conv3_forward_tc(s, x, cin, w, bias, cout, relu, y, st, scratch);
   return conv3_forward_mma(s, x, cin, w, bias, cout, relu, y, st);
 }
 

@@ -19,20 +19,30 @@ struct ConvShape {
   size_t voxels() const { return (size_t)batch * nz * ny * nx; }
 };
 
+// Device scratch (FP32) that lets the tensor-memory convolution split its
+// reduction on shapes with few voxels; without it the reduction is not split.
+struct ConvScratch {
+  float * p = nullptr;
+  size_t floats = 0;
+};
+
 // y = act(conv(x, w) + bias); bias may be null; relu selects the activation.
 // cout in {32, 64, 128, 256}; cin in {16, 32, 64, 128, 256}.
 doma_status conv3_forward(const ConvShape & s, const __nv_bfloat16 * x, int cin,
                           const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
-                          __nv_bfloat16 * y, cudaStream_t st);
+                          __nv_bfloat16 * y, cudaStream_t st, ConvScratch scratch = {});
 
 // The tensor-memory (tcgen05 + TMA) variant of conv3_forward (conv_tc.cu),
 // for shapes whose 128-voxel boxes tile the volume exactly; conv3_forward
 // uses it for those unless DOMA_CONV_PATH=mma.  conv3_tc_error reads the
 // flag its bounded waits set when one gave up.
+// conv3_tc_split_scratch is the scratch (floats) with which the shape's
+// reduction is split as far as the kernel would split it.
 bool conv3_tc_supported(const ConvShape & s, int cin, int cout);
+size_t conv3_tc_split_scratch(const ConvShape & s, int cin, int cout);
 doma_status conv3_forward_tc(const ConvShape & s, const __nv_bfloat16 * x, int cin,
                              const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
-                             __nv_bfloat16 * y, cudaStream_t st);
+                             __nv_bfloat16 * y, cudaStream_t st, ConvScratch scratch = {});
 doma_status conv3_forward_mma(const ConvShape & s, const __nv_bfloat16 * x, int cin,
                               const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
                               __nv_bfloat16 * y, cudaStream_t st);

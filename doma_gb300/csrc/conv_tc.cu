@@ -157,10 +157,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
 struct TcArgs {
   const float * bias;
   bf16 * y;
+  float * partial;            // split reduction: FP32 partials [splits][voxels][cout], else null
+  long long voxels;           // batch * nz * ny * nx
   int nz, ny, nx;             // volume extents
   int bx, by, bz, bb;         // voxel box of one tile (bx*by*bz*bb = 128)
   int tx, ty, tz;             // tiles per axis
   int cin, cout;
+  int splits;                 // the (tap, chunk) steps are cut into this many contiguous ranges
 };
 
 template <int N, int KC, bool RELU>
@@ -218,16 +221,21 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int b0 = (t / a.tz) * a.bb;
   const int steps_per_tap = a.cin / KC;
   const int k_steps = 27 * steps_per_tap;
+  // this CTA's range of (tap, chunk) steps: all of them unless the reduction is split
+  const int split = (int)blockIdx.z;
+  const int kb = (int)((long long)split * k_steps / a.splits);
+  const int kn = (int)((long long)(split + 1) * k_steps / a.splits) - kb;
 
   if (warp == 0) {
     if (lane == 0) {
       asm volatile("prefetch.tensormap [%0];" ::"l"(&tmA) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"(&tmB) : "memory");
-      int ks = 0;
-      for (; ks < k_steps; ++ks) {
-        const int s = ks % STAGES;
-        const uint32_t use = (uint32_t)(ks / STAGES);
-        if (ks >= STAGES && !mbar_wait(empty + s, (use & 1u) ^ 1u)) break;
+      int j = 0;
+      for (; j < kn; ++j) {
+        const int s = j % STAGES;
+        const uint32_t use = (uint32_t)(j / STAGES);
+        if (j >= STAGES && !mbar_wait(empty + s, (use & 1u) ^ 1u)) break;
+        const int ks = kb + j;
         const int tap = ks / steps_per_tap, c0 = (ks % steps_per_tap) * KC;
         const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
         uint8_t * As = smem + s * STAGE;
@@ -235,14 +243,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         tma_load_5d(As, &tmA, full + s, c0, x0 + dx, y0 + dy, z0 + dz, b0);
         tma_load_2d(As + A_BYTES, &tmB, full + s, c0, tap * a.cout + (int)blockIdx.y * N);
       }
-      s_issued = ks;
+      s_issued = j;
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      int ks = 0;
-      for (; ks < k_steps; ++ks) {
-        const int s = ks % STAGES;
-        const uint32_t use = (uint32_t)(ks / STAGES);
+      int j = 0;
+      for (; j < kn; ++j) {
+        const int s = j % STAGES;
+        const uint32_t use = (uint32_t)(j / STAGES);
         if (!mbar_wait(full + s, use & 1u)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t a_addr = saddr(smem + s * STAGE);
@@ -251,11 +259,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int k = 0; k < KC / 16; ++k) {
           const uint64_t ad = smem_desc(a_addr + k * 32, SBO, MODE);
           const uint64_t bd = smem_desc(b_addr + k * 32, SBO, MODE);
-          umma_bf16(tmem, ad, bd, IDESC, (ks | k) != 0 ? 1u : 0u);
+          umma_bf16(tmem, ad, bd, IDESC, (j | k) != 0 ? 1u : 0u);
         }
         umma_commit(empty + s);
       }
-      s_consumed = ks;
+      s_consumed = j;
       umma_commit(tmem_full);  // also after a failed wait, so the epilogue is released
     }
   } else {
@@ -275,6 +283,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int bb = r / a.bz;
     const long long vox =
         (((long long)(b0 + bb) * a.nz + (z0 + zz)) * a.ny + (y0 + yy)) * a.nx + (x0 + x);
+    if (a.partial) {
+      // split reduction: this range's FP32 sums, summed in split order by conv_split_reduce
+      float * outp = a.partial + ((long long)split * a.voxels + vox) * a.cout + (int)blockIdx.y * N;
+#pragma unroll 1
+      for (int c0 = 0; ok && c0 < N; c0 += 32) {
+        uint32_t v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        uint4 * dst = reinterpret_cast<uint4 *>(outp + c0);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) dst[j] = make_uint4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+      }
+      ok = 0;
+    }
     bf16 * out = a.y + vox * a.cout + (int)blockIdx.y * N;
     const float * bias = a.bias ? a.bias + (int)blockIdx.y * N : nullptr;
 #pragma unroll 1
@@ -352,8 +373,9 @@ doma_status launch_tc(const CUtensorMap & ma, const CUtensorMap & mb, const TcAr
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     configured = true;
   }
-  conv3_tc_kernel<N, KC, RELU><<<dim3((unsigned)tiles, (unsigned)(a.cout / N)), kThreads, smem, st>>>(
-      ma, mb, a);
+  conv3_tc_kernel<N, KC, RELU>
+      <<<dim3((unsigned)tiles, (unsigned)(a.cout / N), (unsigned)a.splits), kThreads, smem, st>>>(ma, mb,
+                                                                                                 a);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }
@@ -367,10 +389,10 @@ doma_status launch_tc_act(const CUtensorMap & ma, const CUtensorMap & mb, const 
 }
 
 template <int KC>
-doma_status dispatch_n(const CUtensorMap & ma, const CUtensorMap & mb, const TcArgs & a, int tiles,
-                       bool relu, cudaStream_t st)
+doma_status dispatch_n(const CUtensorMap & ma, const CUtensorMap & mb, const TcArgs & a, int n,
+                       int tiles, bool relu, cudaStream_t st)
 {
-  switch (a.cout) {
+  switch (n) {
     case 32: return launch_tc_act<32, KC>(ma, mb, a, tiles, relu, st);
     case 64: return launch_tc_act<64, KC>(ma, mb, a, tiles, relu, st);
     case 128: return launch_tc_act<128, KC>(ma, mb, a, tiles, relu, st);
@@ -378,7 +400,91 @@ doma_status dispatch_n(const CUtensorMap & ma, const CUtensorMap & mb, const TcA
   }
 }
 
+// y = act(sum over splits of the FP32 partials + bias), the splits added in
+// order; four channels per thread.
+__global__ void conv_split_reduce_kernel(const float4 * __restrict__ p, int splits, size_t count4,
+                                         int cout, const float * __restrict__ bias, int relu,
+                                         uint2 * __restrict__ y)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count4;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float4 acc = p[i];
+    for (int sp = 1; sp < splits; ++sp) {
+      const float4 v = p[(size_t)sp * count4 + i];
+      acc.x += v.x;
+      acc.y += v.y;
+      acc.z += v.z;
+      acc.w += v.w;
+    }
+    if (bias) {
+      const int c = (int)((i * 4) % (size_t)cout);
+      acc.x += bias[c];
+      acc.y += bias[c + 1];
+      acc.z += bias[c + 2];
+      acc.w += bias[c + 3];
+    }
+    if (relu) {
+      acc.x = fmaxf(acc.x, 0.0f);
+      acc.y = fmaxf(acc.y, 0.0f);
+      acc.z = fmaxf(acc.z, 0.0f);
+      acc.w = fmaxf(acc.w, 0.0f);
+    }
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(acc.x, acc.y);
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(acc.z, acc.w);
+    y[i] = make_uint2(*reinterpret_cast<const uint32_t *>(&lo), *reinterpret_cast<const uint32_t *>(&hi));
+  }
+}
+
+int sm_count()
+{
+  static int n = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+      n = v;
+    else
+      n = 148;
+  });
+  return n;
+}
+
+// How one convolution is cut into CTAs.  Shapes with few 128-voxel tiles (the
+// coarse U-Net levels) would leave most SMs idle: the output channels are cut
+// into N-wide slices first (down to 64; the same sums, the same bits); if that
+// still leaves SMs idle, the (tap, chunk) steps are cut into `splits` ranges
+// whose FP32 partials a second kernel adds in order.  A range keeps at least
+// four steps.
+struct TcPlan {
+  int n = 0, splits = 1;
+};
+
+TcPlan tc_plan(const ConvShape & s, int cin, int cout, size_t scratch_floats)
+{
+  const long long tiles = (long long)(s.voxels() / 128);
+  const long long target = 2LL * sm_count();  // two CTAs per SM are resident
+  TcPlan p;
+  p.n = cout;
+  while (p.n > 64 && tiles * (cout / p.n) < target) p.n >>= 1;
+  const long long ctas = tiles * (cout / p.n);
+  const int kc = cin >= 64 ? 64 : cin;
+  const int k_steps = 27 * (cin / kc);
+  if (ctas < sm_count()) {
+    p.splits = (int)std::min<long long>((target + ctas - 1) / ctas, std::max(1, k_steps / 4));
+    while (p.splits > 1 && (size_t)p.splits * s.voxels() * (size_t)cout > scratch_floats) --p.splits;
+  }
+  return p;
+}
+
 }  // namespace
+
+size_t conv3_tc_split_scratch(const ConvShape & s, int cin, int cout)
+{
+  if (!conv3_tc_supported(s, cin, cout)) return 0;
+  const TcPlan p = tc_plan(s, cin, cout, SIZE_MAX);
+  return p.splits > 1 ? (size_t)p.splits * s.voxels() * (size_t)cout : 0;
+}
 
 bool conv3_tc_supported(const ConvShape & s, int cin, int cout)
 {
@@ -398,8 +504,10 @@ bool conv3_tc_supported(const ConvShape & s, int cin, int cout)
 }
 
 doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const bf16 * w,
-                             const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st)
+                             const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st,
+                             ConvScratch scratch)
 {
+  if (!scratch.p) scratch.floats = 0;
   if (!conv3_tc_supported(s, cin, cout)) {
     set_error("conv3_forward_tc: shape not supported by the tensor-memory kernel");
     return DOMA_BAD_INPUT;
@@ -420,7 +528,11 @@ doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const
   a.tz = s.nz / a.bz;
   a.cin = cin;
   a.cout = cout;
+  a.voxels = (long long)s.voxels();
   const int tiles = a.tx * a.ty * a.tz * (s.batch / a.bb);
+  const TcPlan plan = tc_plan(s, cin, cout, scratch.floats);
+  a.splits = plan.splits;
+  a.partial = plan.splits > 1 ? scratch.p : nullptr;
 
   CUtensorMap ma, mb;
   const cuuint64_t gdim_a[5] = {(cuuint64_t)cin, (cuuint64_t)s.nx, (cuuint64_t)s.ny,
@@ -439,7 +551,8 @@ doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const
   }
   const cuuint64_t gdim_b[2] = {(cuuint64_t)cin, (cuuint64_t)27 * cout};
   const cuuint64_t gstr_b[1] = {row};
-  const cuuint32_t box_b[2] = {(cuuint32_t)kc, (cuuint32_t)cout};
+  // one CTA's slice: N output channels of one tap
+  const cuuint32_t box_b[2] = {(cuuint32_t)kc, (cuuint32_t)plan.n};
   r = encoder()(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(w), gdim_b, gstr_b,
                 box_b, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(kc),
                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -447,9 +560,18 @@ doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const
     set_error("cuTensorMapEncodeTiled (weights) failed: " + std::to_string((int)r));
     return DOMA_CUDA_ERROR;
   }
-  if (kc == 64) return dispatch_n<64>(ma, mb, a, tiles, relu, st);
-  if (kc == 32) return dispatch_n<32>(ma, mb, a, tiles, relu, st);
-  return dispatch_n<16>(ma, mb, a, tiles, relu, st);
+  if (kc == 64) DOMA_TRY(dispatch_n<64>(ma, mb, a, plan.n, tiles, relu, st));
+  else if (kc == 32) DOMA_TRY(dispatch_n<32>(ma, mb, a, plan.n, tiles, relu, st));
+  else DOMA_TRY(dispatch_n<16>(ma, mb, a, plan.n, tiles, relu, st));
+  if (a.partial) {
+    const size_t count4 = s.voxels() * (size_t)cout / 4;
+    const unsigned blocks = (unsigned)std::min<size_t>((count4 + 255) / 256, (size_t)sm_count() * 8);
+    conv_split_reduce_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<const float4 *>(a.partial),
+                                                     a.splits, count4, cout, bias, relu ? 1 : 0,
+                                                     reinterpret_cast<uint2 *>(y));
+    DOMA_CUDA_TRY(cudaGetLastError());
+  }
+  return DOMA_OK;
 }
 
 doma_status conv3_tc_error(int * flag)

@@ -97,13 +97,19 @@ doma_status ensure_work(doma_unet * n, int batch, int nz, int ny, int nx)
     if (l < 3) DOMA_TRY(walloc(w, &w.gs[l], V * kWidth[l]));
   }
   DOMA_TRY(walloc(w, &w.out, V0));
-  size_t ws = 0;
+  size_t ws = 0, fs = 0;
   for (int l = 0; l < kUnetConvs; ++l) {
     const UnetLayer & L = n->layers[l];
     const int lvl = l < 8 ? l / 2 : (l == 8 ? 3 : l == 9 ? 2 : l == 10 ? 2 : l == 11 ? 1 : l == 12 ? 1 : 0);
     ws = std::max(ws, conv3_wgrad_scratch(w.s[lvl], L.cin, L.cout));
+    fs = std::max(fs, conv3_tc_split_scratch(w.s[lvl], L.cin, L.cout));
+    fs = std::max(fs, conv3_tc_split_scratch(w.s[lvl], L.cout, L.cin));
   }
   DOMA_TRY(walloc(w, &w.wpartial, ws));
+  if (fs > 0) {
+    DOMA_TRY(walloc(w, &w.fsplit.p, fs));
+    w.fsplit.floats = fs;
+  }
   DOMA_TRY(walloc(w, &w.bpartial, bias_grad_scratch(256)));
   DOMA_TRY(walloc(w, &w.hpartial, head_backward_scratch(kUnetBase)));
   n->batch = batch;
@@ -132,7 +138,8 @@ doma_status conv(doma_unet * n, int l, const ConvShape & s, const bf16 * x, bf16
                  cudaStream_t st)
 {
   const UnetLayer & L = n->layers[l];
-  return conv3_forward(s, x, L.cin, L.w, n->params + L.b_off, L.cout, L.relu, y, st);
+  return conv3_forward(s, x, L.cin, L.w, n->params + L.b_off, L.cout, L.relu, y, st,
+                       n->work.fsplit);
 }
 
 // dgrad of layer l: gx = conv(gz, mirrored transposed weights), no bias
@@ -140,7 +147,7 @@ doma_status dgrad(doma_unet * n, int l, const ConvShape & s, const bf16 * gz, bf
                   cudaStream_t st)
 {
   const UnetLayer & L = n->layers[l];
-  return conv3_forward(s, gz, L.cout, L.wt, nullptr, L.cin, false, gx, st);
+  return conv3_forward(s, gz, L.cout, L.wt, nullptr, L.cin, false, gx, st, n->work.fsplit);
 }
 
 doma_status wgrad(doma_unet * n, int l, const ConvShape & s, const bf16 * x, const bf16 * gz,
@@ -417,9 +424,26 @@ doma_status doma_conv3_forward(const void * x, uint32_t batch, uint32_t nz, uint
   bf16 * yb = static_cast<bf16 *>(y);
   if (path == DOMA_CONV_MMA)
     return conv3_forward_mma(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
-  if (path == DOMA_CONV_TENSOR_MEMORY)
-    return conv3_forward_tc(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
-  return conv3_forward(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
+  // the split-reduction scratch the U-Net keeps in its workspace, stream-ordered here
+  ConvScratch sc;
+  sc.floats = conv3_tc_split_scratch(s, (int)cin, (int)cout);
+  if (sc.floats > 0) {
+    void * p = nullptr;
+    DOMA_CUDA_TRY(cudaMallocAsync(&p, sc.floats * sizeof(float), st));
+    sc.p = static_cast<float *>(p);
+  }
+  const doma_status r =
+      path == DOMA_CONV_TENSOR_MEMORY
+          ? conv3_forward_tc(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st, sc)
+          : conv3_forward(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st, sc);
+  if (sc.p) {
+    const cudaError_t e = cudaFreeAsync(sc.p, st);
+    if (r == DOMA_OK && e != cudaSuccess) {
+      set_error(std::string("cudaFreeAsync: ") + cudaGetErrorString(e));
+      return DOMA_CUDA_ERROR;
+    }
+  }
+  return r;
 }
 
 doma_status doma_conv_wait_error(int * flag)

@@ -39,6 +39,7 @@ struct UnetWork {
   __nv_bfloat16 *gA[4] = {}, *gB[4] = {}, *gs[4] = {};
   float * out = nullptr;
   float * wpartial = nullptr;
+  ConvScratch fsplit;  // split reductions of the coarse levels' convolutions
   float * bpartial = nullptr;
   double * hpartial = nullptr;
   std::vector<void *> allocs;

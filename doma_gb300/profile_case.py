@@ -4,6 +4,7 @@
         [--precision fp32|fp64] [--scheme dd|tw_dd] [--tile 8] [--sweeps 3]
         [--solve] [--schedule persistent|levels] [--loop graph|host]
         [--iteration gauss_seidel|multigroup]
+    python -m doma_gb300.profile_case --unet-forward 3 [--n 64] [--batch 1]
 
 Builds the seeded checkerboard problem (doma_gb300.problems.checkerboard) on
 cuda:0, sets up group 0's source with one source iteration, then runs
@@ -11,6 +12,10 @@ cuda:0, sets up group 0's source with one source iteration, then runs
 prints the solver's block shape and launch counts.  With --iteration
 multigroup every group is in flight in each sweep launch.  Device memory stays
 well under 1 GB at the default size.
+
+With --unet-forward K it instead runs K forward passes of the learned
+accelerator's U-Net (the committed weights) on an n^3 volume of `--batch`
+samples, one per group of a correction, and prints their CUDA-event time.
 """
 from __future__ import annotations
 
@@ -36,7 +41,12 @@ def main() -> None:
     ap.add_argument("--loop", choices=["graph", "host"], default="graph",
                     help="host: host-driven solve loop (kernels profilable one by one)")
     ap.add_argument("--iteration", choices=["gauss_seidel", "multigroup"], default="gauss_seidel")
+    ap.add_argument("--unet-forward", type=int, default=0)
+    ap.add_argument("--batch", type=int, default=1)
     a = ap.parse_args()
+    if a.unet_forward > 0:
+        unet_forward(a)
+        return
     if a.schedule == "levels":
         os.environ["DOMA_SWEEP_SCHEDULE"] = "levels"
     if a.loop == "host":
@@ -68,6 +78,31 @@ def main() -> None:
         dt = time.perf_counter() - t0
         print(json.dumps({"workload": p.name, "precision": a.precision, "scheme": a.scheme,
                           "seconds": round(dt, 4), **extra, **s.describe()}))
+
+
+def unet_forward(a) -> None:
+    import torch
+
+    from .learned.net import UNet
+
+    torch.cuda.set_device(0)
+    weights = os.path.join(os.path.dirname(__file__), "learned", "weights", "unet_c32.npz")
+    with UNet(seed=0) as net:
+        net.load(weights)
+        net.set_stream(torch.cuda.current_stream().cuda_stream)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.randn((a.batch, a.n, a.n, a.n, 16), generator=g, device="cuda").to(torch.bfloat16)
+        y = torch.empty((a.batch, a.n, a.n, a.n), dtype=torch.float32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(a.unet_forward):
+            net.forward(x, y)
+        e1.record()
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": f"unet_forward_{a.n}cube_batch{a.batch}",
+                          "forwards": a.unet_forward,
+                          "ms_per_forward": e0.elapsed_time(e1) / a.unet_forward}))
 
 
 if __name__ == "__main__":

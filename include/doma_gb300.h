@@ -355,8 +355,11 @@ doma_status doma_unet_adam(doma_unet *net, float lr, float beta1, float beta2, f
  * selects the kernel: DOMA_CONV_AUTO (tensor-memory kernel where the shape
  * tiles into 128-voxel boxes, else the warp-MMA kernel), DOMA_CONV_MMA or
  * DOMA_CONV_TENSOR_MEMORY (tcgen05 + TMA; BAD_INPUT for shapes it does not
- * tile).  Asynchronous on `stream`.  doma_conv_wait_error reads the flag the
- * tensor-memory kernel sets if one of its bounded waits gave up. */
+ * tile).  On shapes with fewer 128-voxel tiles than SMs the tensor-memory
+ * kernel splits its reduction over the taps and adds the FP32 partials in a
+ * fixed order, in scratch allocated and freed on `stream`.  Asynchronous on
+ * `stream`.  doma_conv_wait_error reads the flag the tensor-memory kernel
+ * sets if one of its bounded waits gave up. */
 enum { DOMA_CONV_AUTO = 0, DOMA_CONV_MMA = 1, DOMA_CONV_TENSOR_MEMORY = 2 };
 doma_status doma_conv3_forward(const void *x, uint32_t batch, uint32_t nz, uint32_t ny,
                                uint32_t nx, uint32_t cin, const void *w, const float *bias,

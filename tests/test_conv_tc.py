@@ -19,6 +19,7 @@ CASES = [
     (4, 4, 4, 4, 256, 128),     # box spans the batch
     (1, 8, 16, 32, 256, 256),   # non-cubic
     (1, 16, 16, 16, 64, 32),
+    (1, 8, 8, 8, 256, 256),     # 4 tiles: reduction split into 19 tap ranges
 ]
 
 
@@ -63,13 +64,23 @@ def test_tensor_memory_conv_matches_the_oracle(case):
 
 
 @pytest.mark.gpu
-def test_tensor_memory_and_mma_kernels_agree():
+@pytest.mark.parametrize("case", [(2, 16, 16, 16, 64, 64), (1, 16, 16, 16, 128, 128)])
+def test_tensor_memory_and_mma_kernels_agree(case):
+    # the second shape has 32 tiles, so the tensor-memory kernel splits its reduction
     from doma_gb300 import abi
-    case = (2, 16, 16, 16, 64, 64)
     a, want = run(case, abi.DOMA_CONV_TENSOR_MEMORY, relu=False, seed=3)
     b, _ = run(case, abi.DOMA_CONV_MMA, relu=False, seed=3)
     assert np.linalg.norm(a - b) / np.linalg.norm(want) < 5e-3
     assert np.linalg.norm(b - want) / np.linalg.norm(want) < 5e-3
+
+
+@pytest.mark.gpu
+def test_split_reduction_is_deterministic():
+    from doma_gb300 import abi
+    case = (1, 8, 8, 8, 256, 128)
+    a, _ = run(case, abi.DOMA_CONV_TENSOR_MEMORY, relu=True, seed=7)
+    b, _ = run(case, abi.DOMA_CONV_TENSOR_MEMORY, relu=True, seed=7)
+    assert np.array_equal(a, b)
 
 
 def test_conv_path_constants_are_exported():
