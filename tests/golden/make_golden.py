@@ -6,6 +6,7 @@ Run from the repository root where the DOMA source tree is present:
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py --eigen    # the k-eigenvalue fixtures only
     python tests/golden/make_golden.py --transient  # the transient fixtures only
+    python tests/golden/make_golden.py --only NAME[,NAME...]  # the named fixed-source fixtures
 
 Each case is a seeded synthetic problem (doma_gb300.problems) solved by DOMA
 (single thread, the bit-reproducible order).  A fixture stores the generator
@@ -71,6 +72,19 @@ CASES = {
                      {"seed": 7, "dims": 3, "nx": 6, "ny": 5, "nz": 4, "groups": 4, "np_": 1,
                       "na": 2, "materials": 3},
                      {"scheme": "dd", "fs_tol": 1e-9, "mg_tol": 1e-12, "mg_max_it": 2}),
+    # more ordinates per octant than one GPU task holds (16): 36 = 16 + 16 + 4, 25 = 16 + 9
+    "random3d_np6_dd": ("random_problem",
+                        {"seed": 8, "dims": 3, "nx": 6, "ny": 5, "nz": 4, "groups": 2, "np_": 6,
+                         "na": 6, "materials": 3},
+                        {"scheme": "dd", "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    "random3d_np5_twdd": ("random_problem",
+                          {"seed": 9, "dims": 3, "nx": 5, "ny": 6, "nz": 7, "groups": 2,
+                           "np_": 5, "na": 5, "materials": 3},
+                          {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    "random2d_np6_twdd": ("random_problem",
+                          {"seed": 10, "dims": 2, "nx": 11, "ny": 8, "groups": 2, "np_": 6,
+                           "na": 6, "materials": 3},
+                          {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-10, "mg_tol": 1e-10}),
 }
 
 # k-eigenvalue cases: name -> (generator, kwargs, options kwargs, k_tol).  DOMA's
@@ -198,16 +212,25 @@ def main() -> None:
     if "--transient" in sys.argv:
         make_transient()
         return
-    quad = {}
-    for dims, np_, na in QUAD_SETS:
-        mu, eta, xi, w, counts = ol.ref_quadrature(np_, na, dims)
-        key = f"d{dims}_np{np_}_na{na}"
-        quad[key + "_mu"], quad[key + "_eta"], quad[key + "_xi"] = mu, eta, xi
-        quad[key + "_w"], quad[key + "_counts"] = w, counts
-    np.savez_compressed(HERE / "quadrature.npz", **quad)
-    print("quadrature.npz", len(QUAD_SETS), "sets")
+    only = None
+    if "--only" in sys.argv:
+        only = set(sys.argv[sys.argv.index("--only") + 1].split(","))
+        unknown = only - set(CASES)
+        if unknown:
+            raise SystemExit(f"unknown fixtures: {sorted(unknown)}")
+    if only is None:
+        quad = {}
+        for dims, np_, na in QUAD_SETS:
+            mu, eta, xi, w, counts = ol.ref_quadrature(np_, na, dims)
+            key = f"d{dims}_np{np_}_na{na}"
+            quad[key + "_mu"], quad[key + "_eta"], quad[key + "_xi"] = mu, eta, xi
+            quad[key + "_w"], quad[key + "_counts"] = w, counts
+        np.savez_compressed(HERE / "quadrature.npz", **quad)
+        print("quadrature.npz", len(QUAD_SETS), "sets")
 
     for name, (gen, kw, okw) in CASES.items():
+        if only is not None and name not in only:
+            continue
         p = make_problem(gen, kw)
         opts = P.make_options(**okw)
         t0 = time.time()
@@ -223,8 +246,9 @@ def main() -> None:
                             meta=np.array(json.dumps(meta)))
         print(f"{name:28s} converged={ok} mg={mg} si={list(map(int, si))[:8]}... "
               f"{dt:.2f}s")
-    make_eigen()
-    make_transient()
+    if only is None:
+        make_eigen()
+        make_transient()
 
 
 if __name__ == "__main__":
