@@ -85,6 +85,15 @@ CASES = {
                           {"seed": 10, "dims": 2, "nx": 11, "ny": 8, "groups": 2, "np_": 6,
                            "na": 6, "materials": 3},
                           {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    # one cell thick along x (3D) and along y (2D)
+    "slab3d_thin_twdd": ("random_problem",
+                         {"seed": 12, "dims": 3, "nx": 1, "ny": 9, "nz": 2, "groups": 2,
+                          "np_": 2, "na": 2, "materials": 3},
+                         {"scheme": "tw_dd", "theta": 0.9, "fs_tol": 1e-10, "mg_tol": 1e-10}),
+    "line2d_thin_dd": ("random_problem",
+                       {"seed": 13, "dims": 2, "nx": 17, "ny": 1, "groups": 3, "np_": 3,
+                        "na": 2, "materials": 3},
+                       {"scheme": "dd", "fs_tol": 1e-10, "mg_tol": 1e-10}),
 }
 
 # k-eigenvalue cases: name -> (generator, kwargs, options kwargs, k_tol).  DOMA's
