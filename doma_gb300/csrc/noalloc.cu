@@ -260,7 +260,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
           for (int bk = 0; bk < nbz; ++bk)
             for (int bj = 0; bj < nby; ++bj) {
               const int bi = L - bj - bk;
-              if (bi >= 0 && bi < nbx) g_tasks[t++] = Task{o, og, bi, bj, bk};
+              if (bi >= 0 && bi < nbx) g_tasks[t++] = Task{o, og, bi, bj, bk, 0};
             }
       }
     if (t != num_tasks) return fail("internal task count mismatch");
