@@ -109,6 +109,7 @@ class ClockSampler:
         self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"doma_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
+        self.fh = None
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
@@ -117,6 +118,8 @@ class ClockSampler:
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            if self.fh is not None:
+                self.fh.close()
         return self
 
     def __exit__(self, *exc):
@@ -130,6 +133,7 @@ class ClockSampler:
 
     def summary(self):
         if self.proc is None or not self.path.exists():
+            self.path.unlink(missing_ok=True)
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
