@@ -30,6 +30,9 @@ fluxes and every norm in FP64.
 --impl reference runs DOMA's CPU algorithm (the oracle port, the reference's
 own code cannot be compiled on this host) on the same workload and metric.
 Replicas only: with --gpus N each rank solves its own replica (weak scaling).
+
+`python bench.py profile [...]` runs a small fixed workload for ncu captures
+instead (see profile_main).
 """
 from __future__ import annotations
 
@@ -263,15 +266,18 @@ def drivers_leg(args):
 
 
 def batch_leg(args):
-    """The batched solve (off by default: about a minute): `--batch-problems`
-    independent problems drawn by batch_mix (n ~ U{16..96}, G in {1, 2, 4, 8,
-    16}, 2k x 4k directions with k ~ U{2..6}), FP32 DD multigroup iteration to
-    1e-6, every problem's sweep in one persistent launch per iteration.  The
-    block length is tuned first; the solve is timed alone."""
+    """The batched solve: `--batch-problems` independent problems drawn by
+    batch_mix (n ~ U{16..96}, G in {1, 2, 4, 8, 16}, 2k x 4k directions with
+    k ~ U{2..6}), FP32 DD multigroup iteration to 1e-6, every problem's sweep
+    in one persistent launch per iteration.  The block shapes are tuned first;
+    the solve is timed alone.  Each problem's error against an FP64 solution
+    is reported for `--batch-error-problems` of them (the cheapest FP64 solve
+    of each group count first, then by FP64 cost): the FP64 drop-in mode costs
+    about 1000 s for all 256."""
     import torch
 
     from doma_gb300 import problems as P
-    from doma_gb300.solver import Batch
+    from doma_gb300.solver import Batch, Solver
     ps = P.batch_mix(args.seed, count=args.batch_problems)
     with Batch(ps, scheme="dd", precision="fp32", fs_tol=1e-6, fs_max_it=5000,
                iteration="multigroup") as b:
@@ -281,11 +287,174 @@ def batch_leg(args):
         reps = b.solve()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        cost = [p.updates_per_sweep() * p.num_groups for p in ps]
+        order = sorted(range(len(ps)), key=lambda i: cost[i])
+        picked = []
+        for g in sorted({p.num_groups for p in ps}):
+            picked += [i for i in order if ps[i].num_groups == g][:1]
+        picked += [i for i in order if i not in picked]
+        picked = picked[:max(0, args.batch_error_problems)]
+        errors = []
+        for i in picked:
+            p = ps[i]
+            phi32 = b.scalar_flux(i)
+            with Solver(p, P.make_options(scheme="dd", precision="fp64", fs_tol=1e-10,
+                                          fs_max_it=20000, iteration="multigroup")) as s64:
+                s64.solve_fixed_source()
+                phi64 = s64.scalar_flux()
+            errors.append({"problem": i, "name": p.name, "cells": p.num_cells,
+                           "groups": p.num_groups, "directions": p.num_directions,
+                           "iterations": reps[i].mg_iterations,
+                           "error_vs_fp64_rel_l2": float(np.linalg.norm(phi32 - phi64)
+                                                         / np.linalg.norm(phi64))})
     upd = sum(r.updates for r in reps)
     its = [r.mg_iterations for r in reps]
     return {"problems": len(ps), "tile_x": tx, "solve_s": dt, "gupdates": upd / dt / 1e9,
             "converged": sum(r.converged for r in reps), "iterations_min": min(its),
-            "iterations_max": max(its), "updates": upd}
+            "iterations_max": max(its), "updates": upd,
+            "errors_vs_fp64": errors,
+            "error_max": max((e["error_vs_fp64_rel_l2"] for e in errors), default=None)}
+
+
+def timed_solve(solver, stream, flush, warm: bool = True):
+    """One fixed-source solve timed with CUDA events on the solver's stream,
+    after a warm-up solve and an L2 flush."""
+    import torch
+    if warm:
+        solver.solve_fixed_source()
+    flush.fill_(1.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rep = solver.solve_fixed_source()
+    e1.record(stream)
+    e1.synchronize()
+    return rep, e0.elapsed_time(e1)
+
+
+def timed_sweeps(solver, stream, group: int, count: int) -> float:
+    """ms per bare sweep of `group` (CUDA events on the solver's stream)."""
+    import torch
+    solver.source_iterations(group, 1)
+    solver.sweeps(group, 2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.sweeps(group, count)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / count
+
+
+def timed_source_iterations(solver, stream, group: int, count: int) -> float:
+    """ms per source iteration (sweep + epilogue) of `group`, warm, CUDA events."""
+    import torch
+    solver.source_iterations(group, 2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.source_iterations(group, count)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / count
+
+
+def roofline_entry(ms: float, updates: float, d_oct: int, s_bytes: int, peak: float, peak_kind: str,
+                   traffic=None, traffic_source=None):
+    b_upd = 6 * s_bytes + 3 * s_bytes / d_oct
+    achieved = b_upd * updates / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_source,
+            "peak_source": peak_kind, "bytes_per_update": b_upd, "sweep_ms": ms,
+            "updates_per_launch": updates}
+
+
+# DRAM traffic of one sweep launch on the 100^3, 288-direction duct problem
+# (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture); None until
+# captured.
+STREAMING_SWEEP_DRAM_BYTES = None
+
+
+def streaming_leg(args, stream, flush):
+    """The streaming/shielding workload: 100^3 cells of 1 cm, one group,
+    12 x 24 = 288 directions (36 ordinates per octant), DD, a 10 cm near-void
+    duct (sigma_t = 1e-4, c = 0.5) on a seeded 3-segment path from a 10^3
+    corner source through an absorber (sigma_t = 0.1, c = 0.5).  FP32 sweeps
+    with FP64 norms to the FP32 floor (1e-6), the FP64 drop-in mode to DOMA's
+    1e-8, the bare sweep's roofline, and the CPU restatement's rate."""
+    import torch
+
+    from doma_gb300 import problems as P
+    from doma_gb300.solver import Solver
+    p = P.streaming_duct(args.seed, n=100, np_=6, na=6)
+    o32 = P.make_options(scheme="dd", precision="fp32", fs_tol=1e-6, fs_max_it=5000, mg_tol=1e-6)
+    o64 = P.make_options(scheme="dd", precision="fp64", fs_tol=1e-8, fs_max_it=5000, mg_tol=1e-8)
+    peak, peak_kind = measured_peak_hbm()
+    with Solver(p, o32) as s:
+        s.set_stream(stream.cuda_stream)
+        rep, ms = timed_solve(s, stream, flush)
+        phi32 = s.scalar_flux()
+        sweep_ms = timed_sweeps(s, stream, 0, args.roofline_sweeps)
+        desc = s.describe()
+    with Solver(p, o64) as s64:
+        s64.set_stream(stream.cuda_stream)
+        rep64, ms64 = timed_solve(s64, stream, flush)
+        phi64 = s64.scalar_flux()
+    out = {"workload": "streaming_duct_100cube_1g_288dir_dd", "cells": p.num_cells,
+           "directions": p.num_directions, "directions_per_octant": p.directions_per_octant,
+           "fp32": {"time_to_tolerance_ms": ms, "tolerance": 1e-6, "sweeps": rep.si_iterations,
+                    "converged": rep.converged, "gupdates": rep.updates / ms / 1e6,
+                    "tile": list(desc["tile"])},
+           "fp64_dropin": {"time_to_tolerance_ms": ms64, "tolerance": 1e-8,
+                           "sweeps": rep64.si_iterations, "converged": rep64.converged,
+                           "gupdates": rep64.updates / ms64 / 1e6},
+           "error_fp32_vs_fp64_rel_l2": float(np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64)),
+           "roofline": roofline_entry(sweep_ms, p.updates_per_sweep(), p.directions_per_octant, 4,
+                                      peak, peak_kind, STREAMING_SWEEP_DRAM_BYTES,
+                                      "ncu capture of one launch" if STREAMING_SWEEP_DRAM_BYTES
+                                      else None)}
+    out["roofline"]["gupdates"] = p.updates_per_sweep() / (sweep_ms / 1e3) / 1e9
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, dt, upd = cpu_sample(p, o64, threads, args.streaming_cpu_iters)
+        out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{args.streaming_cpu_iters} source iterations of the "
+                                         f"group ({upd / 1e6:.0f} M updates, {dt:.1f} s), "
+                                         f"{threads} OpenMP threads over the 36 ordinates of "
+                                         f"each octant"}
+        out["cpu_time_to_tolerance_estimate_s"] = rep64.updates / (rate * 1e9)
+    return out
+
+
+def small_leg(args, stream, flush):
+    """The small CPU-runnable workload: a 10 cm cube of 20^3 cells, 2 groups,
+    4 x 8 = 32 directions, DD, downscatter, a central 5^3 unit source; the
+    FP64 drop-in mode to DOMA's 1e-8 (time to tolerance, warm), and the CPU
+    restatement's full solve on all host threads."""
+    from doma_gb300 import problems as P
+    from doma_gb300.solver import Solver
+    sys.path.insert(0, str(ROOT / "tests"))
+    p = P.small_cube(args.seed, n=20)
+    o64 = P.make_options(scheme="dd", precision="fp64", fs_tol=1e-8, mg_tol=1e-8)
+    with Solver(p, o64) as s:
+        s.set_stream(stream.cuda_stream)
+        rep, ms = timed_solve(s, stream, flush)
+    out = {"workload": "small_cube_20cube_2g_32dir_dd", "cells": p.num_cells,
+           "fp64_dropin": {"time_to_tolerance_ms": ms, "sweeps": rep.si_iterations,
+                           "mg_iterations": rep.mg_iterations, "converged": rep.converged,
+                           "gupdates": rep.updates / ms / 1e6}}
+    if not args.no_cpu_baseline:
+        import oracle_lib as ol
+        threads = os.cpu_count() or 1
+        ol.oracle()
+        t0 = time.perf_counter()
+        _, ok, si, mg, _ = ol.oracle_solve(p, o64, threads=threads)
+        dt = time.perf_counter() - t0
+        upd = int(sum(si)) * p.updates_per_sweep()
+        out["cpu_baseline"] = {"time_to_tolerance_ms": dt * 1e3, "value": upd / dt / 1e9,
+                               "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": "one full solve to 1e-8 (the oracle's OpenMP "
+                                         "parallel-in-angle sweep: 4 ordinates per octant)"}
+    return out
 
 
 def learned_leg(args):
@@ -310,7 +479,12 @@ def learned_leg(args):
         plain = E.time_to_error(p, ref, args.learned_target, max_it=20000)
         lrn = E.time_to_error(p, ref, args.learned_target, net=net, first=args.accel_first,
                               interval=args.accel_interval, max_corrections=64, max_it=20000)
+        gs = E.time_to_error_gs(p, ref, args.learned_target) if args.learned_gs else None
         rows.append({"problem": p.name, "fp64_reference_s": ref_s,
+                     "gauss_seidel_ms": gs["ms"] if gs else None,
+                     "gauss_seidel_tolerance": gs["tolerance"] if gs else None,
+                     "gauss_seidel_error": gs["error"] if gs else None,
+                     "gauss_seidel_sweeps": gs.get("sweeps") if gs else None,
                      "fp64_reference_iterations": info["iterations"],
                      "plain_ms": plain["ms"], "plain_iterations": plain["iterations"],
                      "plain_error": plain["error"],
@@ -320,7 +494,14 @@ def learned_leg(args):
     net.close()
     plain_ms = sum(r["plain_ms"] for r in rows)
     learned_ms = sum(r["learned_ms"] for r in rows)
+    per = [r["plain_ms"] / r["learned_ms"] for r in rows if r["learned_ms"]]
+    per_gs = [r["gauss_seidel_ms"] / r["learned_ms"] for r in rows
+              if r["learned_ms"] and r["gauss_seidel_ms"]]
     return {"target_rel_l2": args.learned_target,
+            "speedup_mean": float(np.mean(per)) if per else None,
+            "speedup_min": float(np.min(per)) if per else None,
+            "speedup_vs_gauss_seidel_mean": float(np.mean(per_gs)) if per_gs else None,
+            "speedup_vs_gauss_seidel_min": float(np.min(per_gs)) if per_gs else None,
             "workload": f"{args.learned_n}^3 cells, 8 groups, 6x12 directions, DD, sigma_t lognormal "
                         "field (log-sigma 0.8, correlation 4 cells), c ~ U[0.9, 0.999]",
             "plain_ms": plain_ms, "learned_ms": learned_ms,
@@ -426,9 +607,10 @@ def run_ours(args):
 
     # -- FP64 drop-in reference solution and its rate ----------------------------
     err = None
-    fp64_rate = None
+    fp64 = None
     if args.fp64_check:
-        # the FP64 oracle converged tightly (1e-8), independent of --tol
+        # the FP64 reference converged tightly (1e-8), independent of --tol; its
+        # rate is then taken warm with CUDA events over source iterations of group 0
         with Solver(p, options("fp64", 1e-8)) as s64:
             s64.set_stream(stream.cuda_stream)
             t0 = time.perf_counter()
@@ -436,8 +618,15 @@ def run_ours(args):
             torch.cuda.synchronize()
             dt64 = time.perf_counter() - t0
             phi64 = s64.scalar_flux()
-        fp64_rate = r64.updates / dt64 / 1e9
+            si_ms = timed_source_iterations(s64, stream, 0, args.fp64_iters)
+            sw_ms = timed_sweeps(s64, stream, 0, max(3, args.fp64_iters // 2))
         err = float(np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64))
+        upd_sweep = p.updates_per_sweep()
+        fp64 = {"gupdates": upd_sweep / (si_ms / 1e3) / 1e9, "source_iteration_ms": si_ms,
+                "sweep_ms": sw_ms, "sweep_gupdates": upd_sweep / (sw_ms / 1e3) / 1e9,
+                "sample": f"{args.fp64_iters} warm source iterations of group 0, CUDA events",
+                "reference_solve": {"tolerance": 1e-8, "sweeps": r64.si_iterations,
+                                    "wall_s_first_solve": dt64}}
 
     # -- e2e through the C ABI with host buffers ---------------------------------
     h2d = (p.dx.nbytes + p.dy.nbytes + p.dz.nbytes + p.cell_material.nbytes + p.total.nbytes
@@ -469,6 +658,8 @@ def run_ours(args):
                "sample": f"{args.cpu_iters} source iterations of group 0 ({upd / 1e6:.1f} M updates, "
                          f"{dt:.1f} s), {threads} OpenMP threads over ordinates"}
 
+    streaming = streaming_leg(args, stream, flush) if args.streaming else None
+    small = small_leg(args, stream, flush) if args.small else None
     learned = learned_leg(args) if args.learned_problems > 0 else None
     drivers = drivers_leg(args) if args.drivers else None
     batch = batch_leg(args) if args.batch_problems > 0 else None
@@ -484,7 +675,7 @@ def run_ours(args):
                                         "mg_iterations": last_rep.mg_iterations}),
         "time_to_tolerance_ms": total_ms / args.steps,
         "error_vs_fp64_rel_l2": err,
-        "fp64_dropin_gupdates": fp64_rate,
+        "fp64_dropin": fp64,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -496,6 +687,8 @@ def run_ours(args):
                      "sweep_launches": desc["launches_per_sweep"]},
         "roofline_all_groups": roof_all,
         "cpu_baseline": cpu,
+        "streaming": streaming,
+        "small": small,
         "learned": learned,
         "drivers": drivers,
         "batch": batch,
@@ -508,7 +701,106 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def profile_main(argv) -> None:
+    """`python bench.py profile ...`: a small, self-contained workload for ncu.
+
+    Builds the seeded checkerboard problem on cuda:0, sets up group 0's source
+    with one source iteration, then runs `--sweeps` bare sweeps (or, with
+    --solve, one full fixed-source solve) and prints the solver's block shape
+    and launch counts.  With --iteration multigroup every group is in flight in
+    each sweep launch.  --streaming selects the 100^3, 288-direction DD duct
+    problem instead.  With --unet-forward K it runs K forward passes of the
+    learned accelerator's U-Net (the committed weights) on an n^3 volume of
+    `--batch` samples.  Device memory stays well under a few GB."""
+    ap = argparse.ArgumentParser(prog="bench.py profile")
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--groups", type=int, default=8)
+    ap.add_argument("--np", dest="np_", type=int, default=4)
+    ap.add_argument("--na", type=int, default=4)
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--scheme", choices=["dd", "tw_dd"], default="tw_dd")
+    ap.add_argument("--theta", type=float, default=0.7)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--sweeps", type=int, default=3)
+    ap.add_argument("--solve", action="store_true")
+    ap.add_argument("--schedule", choices=["persistent", "levels"], default="persistent")
+    ap.add_argument("--loop", choices=["graph", "host"], default="graph",
+                    help="host: host-driven solve loop (kernels profilable one by one)")
+    ap.add_argument("--iteration", choices=["gauss_seidel", "multigroup"], default="gauss_seidel")
+    ap.add_argument("--unet-forward", type=int, default=0)
+    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--streaming", action="store_true",
+                    help="the 100^3 duct problem (one group, 12 x 24 directions, DD)")
+    a = ap.parse_args(argv)
+    if a.unet_forward > 0:
+        profile_unet_forward(a)
+        return
+    if a.schedule == "levels":
+        os.environ["DOMA_SWEEP_SCHEDULE"] = "levels"
+    if a.loop == "host":
+        os.environ["DOMA_SOLVE_LOOP"] = "host"
+
+    import torch
+
+    from doma_gb300 import problems as P
+    from doma_gb300.solver import Solver
+
+    torch.cuda.set_device(0)
+    if a.streaming:
+        p = P.streaming_duct(0, n=100, np_=6, na=6)
+    else:
+        p = P.checkerboard(0, n=a.n, groups=a.groups, np_=a.np_, na=a.na, block=8)
+    o = P.make_options(scheme=a.scheme, theta=a.theta, precision=a.precision,
+                       fs_tol=1e-6 if a.precision == "fp32" else 1e-8,
+                       mg_tol=1e-6 if a.precision == "fp32" else 1e-8,
+                       fs_max_it=5000, mg_max_it=500, tile=(a.tile, 0, 0),
+                       iteration=a.iteration)
+    with Solver(p, o) as s:
+        t0 = time.perf_counter()
+        if a.solve:
+            r = s.solve_fixed_source()
+            extra = {"converged": r.converged, "si_iterations": r.si_iterations,
+                     "mg_iterations": r.mg_iterations}
+        else:
+            s.source_iterations(0, 1)
+            s.sweeps(0, a.sweeps)
+            extra = {"sweeps": a.sweeps}
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        print(json.dumps({"workload": p.name, "precision": a.precision, "scheme": a.scheme,
+                          "seconds": round(dt, 4), **extra, **s.describe()}))
+
+
+def profile_unet_forward(a) -> None:
+    import torch
+
+    from doma_gb300.learned.net import UNet
+
+    torch.cuda.set_device(0)
+    weights = str(WEIGHTS)
+    with UNet(seed=0) as net:
+        net.load(weights)
+        net.set_stream(torch.cuda.current_stream().cuda_stream)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.randn((a.batch, a.n, a.n, a.n, 16), generator=g, device="cuda").to(torch.bfloat16)
+        y = torch.empty((a.batch, a.n, a.n, a.n), dtype=torch.float32, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(a.unet_forward):
+            net.forward(x, y)
+        e1.record()
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": f"unet_forward_{a.n}cube_batch{a.batch}",
+                          "forwards": a.unet_forward,
+                          "ms_per_forward": e0.elapsed_time(e1) / a.unet_forward}))
+
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "profile":
+        profile_main(sys.argv[2:])
+        return
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -527,13 +819,24 @@ def main():
     ap.add_argument("--fp64-check", type=int, default=1)
     ap.add_argument("--all-groups-roofline", type=int, default=1,
                     help="also time the sweep with every group in flight (multigroup mode)")
-    ap.add_argument("--learned-problems", type=int, default=1)
+    ap.add_argument("--fp64-iters", type=int, default=20,
+                    help="warm FP64 source iterations timed for the drop-in rate")
+    ap.add_argument("--streaming", type=int, default=1,
+                    help="also time the 100^3, 288-direction duct problem (0: skip)")
+    ap.add_argument("--streaming-cpu-iters", type=int, default=6)
+    ap.add_argument("--small", type=int, default=1,
+                    help="also time the 20^3, 2-group, 32-direction problem (0: skip)")
+    ap.add_argument("--batch-error-problems", type=int, default=10,
+                    help="batched problems whose error against FP64 is measured")
+    ap.add_argument("--learned-problems", type=int, default=3)
     ap.add_argument("--drivers", type=int, default=1,
                     help="also time the eigenvalue and transient drivers (0: skip)")
     ap.add_argument("--driver-cpu-iters", type=int, default=20)
-    ap.add_argument("--batch-problems", type=int, default=0,
-                    help="also time the batched solve of this many problems (256: the batched workload)")
+    ap.add_argument("--batch-problems", type=int, default=256,
+                    help="also time the batched solve of this many problems (0: skip)")
     ap.add_argument("--learned-n", type=int, default=64)
+    ap.add_argument("--learned-gs", type=int, default=1,
+                    help="also time DOMA's Gauss-Seidel order (FP32) to the same error")
     ap.add_argument("--learned-target", type=float, default=1e-5)
     ap.add_argument("--accel-first", type=int, default=10)
     ap.add_argument("--accel-interval", type=int, default=10)

@@ -143,7 +143,8 @@ doma_status launch_sweep_batch(int dims, int scheme, int tx, int grid, int threa
                                unsigned * epoch, const BatchLoop * loops, cudaStream_t stream);
 int sweep_batch_resident_ctas(int dims, int scheme, int tx, int threads, size_t smem);
 
-// Host quadrature (quadrature.cpp).
+// Host quadrature (quadrature.cpp): np, na <= kMaxQuadPolar; allocates nothing.
+constexpr unsigned kMaxQuadPolar = 512;
 int gc_quadrature(unsigned np, unsigned na, unsigned dims, double * mu, double * eta,
                   double * xi, double * w, unsigned counts[8]);
 

@@ -35,7 +35,9 @@ doma_status conv3_forward(const ConvShape & s, const __nv_bfloat16 * x, int cin,
 // The tensor-memory (tcgen05 + TMA) variant of conv3_forward (conv_tc.cu),
 // for shapes whose 128-voxel boxes tile the volume exactly; conv3_forward
 // uses it for those unless DOMA_CONV_PATH=mma.  conv3_tc_error reads the
-// flag its bounded waits set when one gave up.
+// flag its bounded waits set when one gave up; conv3_tc_error_reset clears it
+// on a stream (each U-Net forward pass and each C-ABI convolution starts with
+// a clear flag, so the flag describes the latest pass).
 // conv3_tc_split_scratch is the scratch (floats) with which the shape's
 // reduction is split as far as the kernel would split it.
 bool conv3_tc_supported(const ConvShape & s, int cin, int cout);
@@ -47,6 +49,7 @@ doma_status conv3_forward_mma(const ConvShape & s, const __nv_bfloat16 * x, int 
                               const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
                               __nv_bfloat16 * y, cudaStream_t st);
 doma_status conv3_tc_error(int * flag);
+doma_status conv3_tc_error_reset(cudaStream_t st);
 
 // Weight gradient: dw[tap][cout][cin] = sum over voxels m of
 // dz[m][cout] * x[m + offset(tap)][cin], reduced over voxel splits in a fixed

@@ -584,4 +584,12 @@ doma_status conv3_tc_error(int * flag)
   return DOMA_OK;
 }
 
+doma_status conv3_tc_error_reset(cudaStream_t st)
+{
+  void * p = nullptr;
+  DOMA_CUDA_TRY(cudaGetSymbolAddress(&p, g_tc_error));
+  DOMA_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(int), st));
+  return DOMA_OK;
+}
+
 }  // namespace doma

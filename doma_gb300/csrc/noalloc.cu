@@ -24,10 +24,12 @@
 // the host-side part of a call is serialised by a mutex, the device side is
 // the caller's to order.
 //
-// Set-up: the first call on each device (with that device current) resolves
-// the array's device address with cudaGetSymbolAddress and caches it; make
-// that first call before any stream capture.  The call synchronises its
-// stream before returning, to report a timed-out device wait.
+// Set-up: every call resolves the array's device address on the current
+// device with cudaGetSymbolAddress (host code cannot use the array's name as
+// a device address).  A call copies small tables from host memory and
+// synchronises its stream before returning, to report a timed-out device
+// wait, so it must not be issued on a stream that is being captured into a
+// CUDA graph; it returns DOMA_BAD_INPUT there.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -40,14 +42,12 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[DOMA_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
 constexpr unsigned kMaxPolar = 8, kMaxAzimuthal = 8;
 constexpr int kMaxOrdinates = 8 * kMaxPolar * kMaxAzimuthal;  // 512
 constexpr int kMaxAxisCells = 4096;
 constexpr size_t kMaxTasks = 1u << 17;
 
 std::mutex g_lock;
-unsigned char * g_scratch_addr[kMaxDevices] = {};
 
 // Host staging (static storage, reused by every call under g_lock).
 Task g_tasks[kMaxTasks];
@@ -66,82 +66,33 @@ doma_status fail(const std::string & msg)
   return DOMA_BAD_INPUT;
 }
 
-// The device address of the scratch array on the current device (resolved
-// once per device).
+// The device address of the scratch array on the current device.  It is
+// resolved on every call (cheap next to a sweep), so a device reset or a
+// re-created primary context never leaves a stale address behind.
 doma_status scratch_address(unsigned char ** out)
 {
-  int dev = 0;
-  DOMA_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail("device ordinal out of range for the no-alloc sweep");
-  if (!g_scratch_addr[dev]) {
-    void * p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      set_error(std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e));
-      return DOMA_CUDA_ERROR;
-    }
-    g_scratch_addr[dev] = static_cast<unsigned char *>(p);
+  void * p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e));
+    return DOMA_CUDA_ERROR;
   }
-  *out = g_scratch_addr[dev];
+  *out = static_cast<unsigned char *>(p);
   return DOMA_OK;
 }
 
-// Gauss-Legendre x Chebyshev quadrature in fixed storage, the same
-// construction as the solver's (GCAngularQuadrature, src/GCAngularQuadrature.cpp:9-55;
-// src/AngularPolynomials.cpp:8-110), with absolute direction cosines.
-double lg_value(unsigned deg, double x, double * slope)
-{
-  double v = 1.0, d = 0.0, v1 = x, v2 = 1.0;
-  const double f = 1.0 / (x * x - 1.0);
-  for (unsigned i = 2; i <= deg; ++i) {
-    v = ((2.0 * (double)i - 1.0) * x * v1 - ((double)i - 1.0) * v2) / (double)i;
-    d = (double)i * f * (x * v - v1);
-    v2 = v1;
-    v1 = v;
-  }
-  *slope = d;
-  return v;
-}
-
+// Gauss-Legendre x Chebyshev quadrature into the fixed host tables, with
+// absolute direction cosines: the solver's own construction (gc_quadrature,
+// quadrature.cpp), which allocates nothing.
 int quadrature_fixed(unsigned np, unsigned na, unsigned dims, int counts[8])
 {
-  const unsigned n_l = 2u * np, n_c = 2u * na;
-  double root[2 * kMaxPolar], lw[2 * kMaxPolar];
-  for (unsigned i = 1; i <= n_l; ++i) {
-    double dr, d;
-    double x = std::cos(kPi * ((double)i - 0.25) / ((double)n_l + 0.5));
-    double v = lg_value(n_l, x, &d);
-    int guard = 0;
-    do {
-      dr = v / d;
-      x -= dr;
-      v = lg_value(n_l, x, &d);
-    } while (std::abs(dr) > 2e-16 && ++guard < 1000);
-    root[i - 1] = x;
-    lw[i - 1] = 2.0 / ((1.0 - x * x) * d * d);
-  }
-  const double cw = kPi / (double)n_c;
-  int k = 0;
-  for (int o = 0; o < 8; ++o) {
-    counts[o] = 0;
-    for (unsigned i = 1; i <= n_l; ++i)
-      for (unsigned j = 1; j <= n_c; ++j)
-        for (int copy = 0; copy < (dims > 2 ? 2 : 1); ++copy) {
-          const double m = copy ? -1.0 * root[i - 1] : root[i - 1];
-          const double omega = (2 * (double)j - 1.0) / (2.0 * (double)n_c) * kPi;
-          const double e = (copy ? -1.0 : 1.0) * std::sqrt(1.0 - (root[i - 1] * root[i - 1])) * std::cos(omega);
-          const double z = (copy ? -1.0 : 1.0) * std::sqrt(1.0 - (root[i - 1] * root[i - 1])) * std::sin(omega);
-          const int oc = (m < 0.0 ? 4 : 0) + (e < 0.0 ? 2 : 0) + (z < 0.0 ? 1 : 0);
-          if (oc != o) continue;
-          g_quad[0][k] = std::abs(m);
-          g_quad[1][k] = std::abs(e);
-          g_quad[2][k] = std::abs(z);
-          g_quad[3][k] = lw[i - 1] * cw;
-          ++k;
-          ++counts[o];
-        }
-  }
-  return k;
+  unsigned c[8];
+  const int D = gc_quadrature(np, na, dims, g_quad[0], g_quad[1], g_quad[2], g_quad[3], c);
+  if (D < 0) return D;
+  for (int k = 0; k < D; ++k)
+    for (int a = 0; a < 3; ++a) g_quad[a][k] = std::abs(g_quad[a][k]);
+  for (int o = 0; o < 8; ++o) counts[o] = (int)c[o];
+  return D;
 }
 
 // Float tables for the FP32 sweep: 2|cosine|/width formed in double exactly
@@ -231,9 +182,19 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   for (int j = 0; j < ny; ++j) if (!(p->dy[j] > 0.0)) return fail("cell widths must be positive");
   if (dims == 3) for (int k = 0; k < nz; ++k) if (!(p->dz[k] > 0.0)) return fail("cell widths must be positive");
 
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  {
+    // the call copies from host buffers and synchronises: never inside a capture
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    DOMA_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+      return fail("doma_sweep_noalloc cannot run on a stream that is being captured");
+  }
+
   std::lock_guard<std::mutex> guard(g_lock);
   int counts[8];
   const int D = quadrature_fixed(p->num_polar, p->num_azimuthal, (unsigned)dims, counts);
+  if (D <= 0) return fail("bad quadrature order");
   const int d_oct = (int)(p->num_polar * p->num_azimuthal);
   const int ngroups = (d_oct + kGroup - 1) / kGroup;
   unsigned oct_mask = 0;
@@ -292,7 +253,6 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   unsigned char * base = nullptr;
   doma_status st = scratch_address(&base);
   if (st != DOMA_OK) return st;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   // upload the small host tables; zero what must start at zero
   std::memcpy(g_widths, p->dx, sizeof(double) * nx);

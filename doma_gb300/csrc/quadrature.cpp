@@ -13,7 +13,6 @@
 // to DOMA's (checked against tests/golden/quadrature.npz); this file is built
 // with -ffp-contract=off for that reason.
 #include <cmath>
-#include <vector>
 
 #include "common.cuh"
 
@@ -61,9 +60,14 @@ int octant_of(double mu, double eta, double xi)
 int gc_quadrature(unsigned np, unsigned na, unsigned dims, double * mu, double * eta,
                   double * xi, double * w, unsigned counts[8])
 {
-  if (np == 0 || na == 0 || (dims != 2 && dims != 3) || np > 512 || na > 512) return -1;
+  // No heap use: the no-allocation sweep entry point calls this too.  The
+  // Legendre roots and weights live on the stack (n_l <= 2 * kMaxQuadPolar),
+  // and the directions are generated once per octant in generation order,
+  // which bins them exactly as generating all and filtering would.
+  if (np == 0 || na == 0 || (dims != 2 && dims != 3) || np > kMaxQuadPolar || na > kMaxQuadPolar)
+    return -1;
   const unsigned n_l = 2u * np, n_c = 2u * na;
-  std::vector<double> root(n_l), lw(n_l);
+  double root[2 * kMaxQuadPolar], lw[2 * kMaxQuadPolar];
   for (unsigned i = 1; i <= n_l; ++i) {
     double dr;
     double x = std::cos(kPi * (static_cast<double>(i) - 0.25) / (static_cast<double>(n_l) + 0.5));
@@ -80,36 +84,36 @@ int gc_quadrature(unsigned np, unsigned na, unsigned dims, double * mu, double *
     lw[i - 1] = 2.0 / ((1.0 - x * x) * d * d);
   }
   const double cheb_w = kPi / static_cast<double>(n_c);
-  struct Dir { double m, e, x, w; int o; };
-  std::vector<Dir> gen;
-  gen.reserve((dims == 3 ? 2u : 1u) * n_l * n_c);
-  for (unsigned i = 1; i <= n_l; ++i) {
-    for (unsigned j = 1; j <= n_c; ++j) {
-      const double weight = lw[i - 1] * cheb_w;
-      const double m = root[i - 1];
-      const double omega = (2 * static_cast<double>(j) - 1.0) / (2.0 * static_cast<double>(n_c)) * kPi;
-      Dir a{m, std::sqrt(1.0 - (m * m)) * std::cos(omega), std::sqrt(1.0 - (m * m)) * std::sin(omega),
-            weight, 0};
-      gen.push_back(a);
-      if (dims > 2) {
-        Dir b{-1.0 * m, -1.0 * std::sqrt(1.0 - (m * m)) * std::cos(omega),
-              -1.0 * std::sqrt(1.0 - (m * m)) * std::sin(omega), weight, 0};
-        gen.push_back(b);
-      }
-    }
-  }
-  for (auto & d : gen) {
-    d.o = octant_of(d.m, d.e, d.x);
-    if (d.o < 0) return -1;
-  }
   unsigned k = 0;
-  for (int o = 0; o < 8; ++o) {
-    counts[o] = 0;
-    for (const auto & d : gen) {
-      if (d.o != o) continue;
-      mu[k] = d.m; eta[k] = d.e; xi[k] = d.x; w[k] = d.w;
-      ++k;
-      ++counts[o];
+  for (int o = -1; o < 8; ++o) {  // o = -1: validity pass only
+    if (o >= 0) counts[o] = 0;
+    for (unsigned i = 1; i <= n_l; ++i) {
+      for (unsigned j = 1; j <= n_c; ++j) {
+        const double weight = lw[i - 1] * cheb_w;
+        const double m = root[i - 1];
+        const double omega = (2 * static_cast<double>(j) - 1.0) / (2.0 * static_cast<double>(n_c)) * kPi;
+        for (unsigned copy = 0; copy < (dims > 2 ? 2u : 1u); ++copy) {
+          double dm, de, dx;
+          if (copy == 0) {
+            dm = m;
+            de = std::sqrt(1.0 - (m * m)) * std::cos(omega);
+            dx = std::sqrt(1.0 - (m * m)) * std::sin(omega);
+          } else {
+            dm = -1.0 * m;
+            de = -1.0 * std::sqrt(1.0 - (m * m)) * std::cos(omega);
+            dx = -1.0 * std::sqrt(1.0 - (m * m)) * std::sin(omega);
+          }
+          const int oc = octant_of(dm, de, dx);
+          if (o < 0) {
+            if (oc < 0) return -1;
+            continue;
+          }
+          if (oc != o) continue;
+          mu[k] = dm; eta[k] = de; xi[k] = dx; w[k] = weight;
+          ++k;
+          ++counts[o];
+        }
+      }
     }
   }
   return static_cast<int>(k);

@@ -1214,6 +1214,15 @@ doma_status accel_correction(doma_solver * s, cudaStream_t st)
     y_prev = ya;
     std::swap(ya, yb);
   }
+  // a tensor-memory convolution whose bounded wait gave up leaves garbage in
+  // the correction: report it instead of sweeping from it
+  DOMA_CUDA_TRY(cudaStreamSynchronize(st));
+  int conv_err = 0;
+  DOMA_TRY(conv3_tc_error(&conv_err));
+  if (conv_err) {
+    set_error("a convolution's wait for its tensor-memory pipeline timed out");
+    return DOMA_DEVICE_WAIT_TIMEOUT;
+  }
   return accel_source(s->it, s->opts.precision, s->d_dscratch, s->d_corr, s->d_q, st);
 }
 

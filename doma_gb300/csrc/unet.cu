@@ -161,6 +161,7 @@ doma_status wgrad(doma_unet * n, int l, const ConvShape & s, const bf16 * x, con
 doma_status forward_impl(doma_unet * n, const bf16 * x, cudaStream_t st)
 {
   UnetWork & w = n->work;
+  DOMA_TRY(conv3_tc_error_reset(st));
   DOMA_TRY(conv(n, 0, w.s[0], x, w.e0a, st));
   DOMA_TRY(conv(n, 1, w.s[0], w.e0a, w.e0, st));
   const bf16 * prev = w.e0;
@@ -424,6 +425,7 @@ doma_status doma_conv3_forward(const void * x, uint32_t batch, uint32_t nz, uint
   bf16 * yb = static_cast<bf16 *>(y);
   if (path == DOMA_CONV_MMA)
     return conv3_forward_mma(s, xb, (int)cin, wb, bias, (int)cout, relu != 0, yb, st);
+  DOMA_TRY(conv3_tc_error_reset(st));
   // the split-reduction scratch the U-Net keeps in its workspace, stream-ordered here
   ConvScratch sc;
   sc.floats = conv3_tc_split_scratch(s, (int)cin, (int)cout);

@@ -40,3 +40,29 @@ def time_to_error(p: P.Problem, ref: np.ndarray, target: float = 1e-5, net=None,
     return {"ms": rep.solve_ms, "iterations": rep.mg_iterations, "converged": rep.converged,
             "accepted": st["accepted"], "rejected": st["rejected"], "error": err,
             "reported_error": st["error"], "updates": rep.updates}
+
+
+def time_to_error_gs(p: P.Problem, ref: np.ndarray, target: float = 1e-5,
+                     tolerances=(1e-4, 3e-5, 1e-5, 3e-6, 1e-6, 3e-7), max_it: int = 100000) -> dict:
+    """DOMA's own iteration order in FP32: Gauss-Seidel over groups wrapping
+    within-group source iteration, stopped by its increment tolerance
+    (fs_tol = mg_tol).  It has no error-based stop, so the tolerances are
+    tried from loose to tight and the first solve whose relative L2 error
+    against ref is <= target gives the time (each solve warm, timed on the
+    device).  Returns the tried solves as well."""
+    tried = []
+    for tol in tolerances:
+        opts = P.make_options(scheme="dd", precision="fp32", fs_tol=tol, fs_max_it=max_it,
+                              mg_tol=tol, mg_max_it=max_it)
+        with Solver(p, opts) as s:
+            s.solve_fixed_source()
+            rep = s.solve_fixed_source()
+            phi = s.scalar_flux()
+        err = float(np.linalg.norm(phi - ref) / np.linalg.norm(ref))
+        tried.append({"tolerance": tol, "ms": rep.solve_ms, "sweeps": rep.si_iterations,
+                      "mg_iterations": rep.mg_iterations, "error": err,
+                      "converged": rep.converged})
+        if err <= target:
+            return {"ms": rep.solve_ms, "tolerance": tol, "error": err,
+                    "sweeps": rep.si_iterations, "tried": tried}
+    return {"ms": None, "tolerance": None, "error": tried[-1]["error"], "tried": tried}

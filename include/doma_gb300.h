@@ -312,8 +312,10 @@ void doma_batch_destroy(doma_batch *batch);
  * flux phi_out[N] (device, double) -- what one source iteration from a zero
  * flux gives.  Problems that need more scratch are rejected with
  * DOMA_BAD_INPUT.  All calls share the array: calls that overlap on the GPU
- * race.  The first call on a device sets up the array's address and should
- * come before any stream capture.  Synchronises `stream` before returning. */
+ * race.  Every call looks up the array's device address on the current
+ * device (cudaGetSymbolAddress), copies small tables from host memory and
+ * synchronises `stream` before returning, so it cannot be called on a stream
+ * that is being captured into a CUDA graph (it returns DOMA_BAD_INPUT). */
 #define DOMA_NOALLOC_SCRATCH_BYTES (64u << 20)
 doma_status doma_sweep_noalloc(const doma_problem *problem, uint32_t scheme, double theta,
                                const float *q, const float *sigma_t, double *phi_out,

@@ -1,0 +1,107 @@
+"""Parity at the full sizes of the two named single-problem workloads.
+
+* Checkerboard: 64^3 cells of 1 cm, 8 groups, 8 x 16 = 128 directions
+  (np = na = 4), TW-DD, four materials on 8^3 blocks with upscatter between
+  the last two groups.  DOMA's theta (0.9) and the workload's theta (0.7).
+  A full solve to 1e-8 takes thousands of sweeps, so the comparison runs at
+  fixed iteration counts: two Gauss-Seidel passes (mg_max_it = 2) with a
+  loose within-group tolerance, which exercises every group, the in-scatter
+  and upscatter sources, the residuals and the failed-MG exit path.
+* Streaming duct: 100^3 cells, one group, 12 x 24 = 288 directions
+  (np = na = 6: 36 ordinates per octant, three ordinate groups per octant, the
+  last one partial, and 298 wavefront planes per octant), DD, a near-void
+  duct through an absorber.  It converges in about 20 source iterations, so
+  it runs to DOMA's 1e-8 tolerance.
+
+The FP64 drop-in mode must give the oracle's bits and counts; the FP32 mode
+must stay within 1e-5 relative L2 of the oracle's flux.  The oracle is the C
+restatement of DOMA (bit-equal to DOMA on every golden fixture), run once per
+case with all host threads and shared between the tests of this file.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+from doma_gb300 import problems as P
+from doma_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12   # relative L-infinity, FP64 drop-in mode
+FP32_RTOL = 1e-5    # relative L2, FP32 sweep vs the FP64 oracle
+
+THREADS = os.cpu_count() or 1
+
+
+def rel_linf(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def checkerboard_case(theta):
+    p = P.checkerboard(0, n=64, groups=8, np_=4, na=4, block=8)
+    opts = P.make_options(scheme="tw_dd", theta=theta, fs_tol=1e-2, fs_max_it=1000,
+                          mg_tol=1e-12, mg_max_it=2)
+    return p, opts
+
+
+def streaming_case():
+    p = P.streaming_duct(0, n=100, np_=6, na=6)
+    opts = P.make_options(scheme="dd", fs_tol=1e-8, fs_max_it=1000, mg_tol=1e-8, mg_max_it=100)
+    return p, opts
+
+
+_ORACLE = {}
+
+
+def oracle_result(key):
+    if key not in _ORACLE:
+        p, opts = checkerboard_case(key[1]) if key[0] == "checkerboard" else streaming_case()
+        _ORACLE[key] = (p, opts, ol.oracle_solve(p, opts, threads=THREADS))
+    return _ORACLE[key]
+
+
+CASES = [("checkerboard", 0.9), ("checkerboard", 0.7), ("streaming", None)]
+IDS = ["checkerboard64_twdd_theta0.9", "checkerboard64_twdd_theta0.7", "streaming100_dd"]
+
+
+@pytest.mark.parametrize("key", CASES, ids=IDS)
+def test_fp64_full_size_bit_equal_to_oracle(key):
+    p, opts, (o_phi, o_ok, o_si, o_mg, o_res) = oracle_result(key)
+    with Solver(p, opts) as s:
+        rep = s.solve_fixed_source()
+        phi = s.scalar_flux()
+    assert rep.converged == o_ok
+    assert list(rep.si_counts) == list(o_si)
+    assert rep.mg_iterations == o_mg
+    assert rel_linf(phi, o_phi) <= FP64_RTOL
+    assert np.array_equal(phi, o_phi), rel_linf(phi, o_phi)
+    if key[0] == "checkerboard":
+        # the comparison covers every group at least twice
+        assert len(o_si) == 2 * p.num_groups and not o_ok
+    else:
+        assert o_ok and p.directions_per_octant == 36
+
+
+@pytest.mark.parametrize("key", CASES, ids=IDS)
+def test_fp32_full_size_against_oracle(key):
+    p, opts, (o_phi, o_ok, o_si, o_mg, _) = oracle_result(key)
+    o32 = P.make_options(scheme={0: "dd", 1: "tw_dd"}[opts.scheme], theta=opts.theta,
+                         precision="fp32", fs_tol=max(opts.fs_tol, 1e-6), fs_max_it=opts.fs_max_it,
+                         mg_tol=max(opts.mg_tol, 1e-6) if key[0] == "streaming" else opts.mg_tol,
+                         mg_max_it=opts.mg_max_it)
+    with Solver(p, o32) as s:
+        rep = s.solve_fixed_source()
+        phi = s.scalar_flux()
+    if key[0] == "checkerboard":
+        # same loose tolerance, same fixed pass count: the same sweeps are compared
+        assert list(rep.si_counts) == list(o_si)
+    else:
+        assert rep.converged
+    err = rel_l2(phi, o_phi)
+    assert err <= FP32_RTOL, err
