@@ -281,7 +281,11 @@ def batch_leg(args):
     ps = P.batch_mix(args.seed, count=args.batch_problems)
     with Batch(ps, scheme="dd", precision="fp32", fs_tol=1e-6, fs_max_it=5000,
                iteration="multigroup") as b:
+        t0 = time.perf_counter()
         tx = b.tune()
+        tune_s = time.perf_counter() - t0
+        tiles = b.tiles()
+        tune = b.tune_report()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         reps = b.solve()
@@ -310,6 +314,8 @@ def batch_leg(args):
     upd = sum(r.updates for r in reps)
     its = [r.mg_iterations for r in reps]
     return {"problems": len(ps), "tile_x": tx, "solve_s": dt, "gupdates": upd / dt / 1e9,
+            "tune_s": tune_s, "tune": tune,
+            "tiles_used": {str(k): tiles.count(k) for k in (8, 16, 32)},
             "converged": sum(r.converged for r in reps), "iterations_min": min(its),
             "iterations_max": max(its), "updates": upd,
             "errors_vs_fp64": errors,

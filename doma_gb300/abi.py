@@ -180,6 +180,9 @@ SIGNATURES = {
     ),
     "doma_batch_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "doma_batch_tune": (ctypes.c_int, [ctypes.c_void_p, _u32p]),
+    "doma_batch_tiles": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_size_t]),
+    "doma_batch_tune_report": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.POINTER(ctypes.c_float), _u32p]),
     "doma_batch_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DomaReport), ctypes.c_size_t]),
     "doma_batch_get_scalar_flux": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_size_t, _dp, ctypes.c_size_t]),
     "doma_batch_destroy": (None, [ctypes.c_void_p]),

@@ -13,8 +13,10 @@ namespace doma {
 
 constexpr double kPi = 3.14159265358979323846;  // M_PI
 
-// Largest sweep CTA: 16 ordinates x 16 pencils.
+// Largest sweep CTA: 16 ordinates x 16 pencils (scalar bodies), or 8
+// ordinate pairs x 16 pencils (the packed single-precision body).
 constexpr int kMaxSweepThreads = 256;
+constexpr int kMaxSweepThreadsF32 = 128;
 
 // Error reporting (per thread, read through doma_last_error()).
 void set_error(const std::string & msg);
@@ -68,6 +70,7 @@ struct SweepArgs {
   int d_total;         // ordinates over all octants (exact mode row length)
   int ngroups;         // ordinate groups per octant (ceil(d_oct / kGroup))
   int nbx, nby, nbz;   // blocks per axis
+  int tx;              // block length along x of this schedule (the batched kernel dispatches on it)
   int num_tasks;
   const Task * tasks;  // all tasks, sorted by level (a topological order)
   int task_offset;     // level-synchronous mode: first task of this launch
@@ -130,18 +133,24 @@ doma_status launch_sweep(int dims, int precision, int scheme, const Schedule & s
                          const SweepArgs<double> * a64, const SweepArgs<float> * a32,
                          cudaStream_t stream, uint64_t * launches);
 int sweep_tile_x(int requested);  // supported block length along x: 8, 16 or 32
+// Threads of a sweep CTA for an ordinate group of gs: one per (ordinate,
+// pencil), or per (ordinate pair, pencil) for the packed single-precision body
+// (the persistent and batched kernels), in whole warps.
+int sweep_threads(int precision, int gs, bool packed);
 size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx);
 doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem);
 // CTAs of the persistent sweep kernel that fit on the device at once.
 int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem);
 
 // One persistent sweep over every active problem of a batch (FP32).  The
-// counters are the batch's own; args[p] is problem p's sweep arguments.
-doma_status launch_sweep_batch(int dims, int scheme, int tx, int grid, int threads, size_t smem,
+// counters are the batch's own; args[p] is problem p's sweep arguments, whose
+// tx (8, 16 or 32) may differ from problem to problem.
+doma_status launch_sweep_batch(int dims, int scheme, int grid, int threads, size_t smem,
                                const SweepArgs<float> * args, const BatchTask * tasks,
                                int num_tasks, unsigned * ticket, unsigned * exit_count,
                                unsigned * epoch, const BatchLoop * loops, cudaStream_t stream);
-int sweep_batch_resident_ctas(int dims, int scheme, int tx, int threads, size_t smem);
+size_t sweep_batch_smem_bytes(int dims);
+int sweep_batch_resident_ctas(int dims, int scheme, int threads, size_t smem);
 
 // Host quadrature (quadrature.cpp): np, na <= kMaxQuadPolar; allocates nothing.
 constexpr unsigned kMaxQuadPolar = 512;

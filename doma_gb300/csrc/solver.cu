@@ -24,7 +24,10 @@
 #include <type_traits>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
+#include <tuple>
+#include <array>
 #include <string>
 #include <vector>
 
@@ -239,7 +242,7 @@ void build_schedule(doma_solver * s)
   sc.nbx = (s->nx + sc.tx - 1) / sc.tx;
   sc.nby = (s->ny + sc.ty - 1) / sc.ty;
   sc.nbz = (s->nz + sc.tz - 1) / sc.tz;
-  sc.threads = ((16 * sc.gs + 31) / 32) * 32;
+  sc.threads = sweep_threads(s->opts.precision, sc.gs, true);
   sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx);
   const int levels = sc.nbx + sc.nby + sc.nbz - 2;
   std::vector<std::vector<Task>> by_level(levels);
@@ -464,6 +467,7 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
     a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
     a.d_oct = s->d_oct; a.d_total = s->D; a.ngroups = s->sched.ngroups;
     a.nbx = s->sched.nbx; a.nby = s->sched.nby; a.nbz = s->sched.nbz;
+    a.tx = s->sched.tx;
     a.num_tasks = (int)s->sched.tasks.size();
     a.tasks = s->d_tasks; a.task_offset = 0; a.oct_offset = s->d_oct_offset;
     a.amu = s->d_amu; a.aeta = s->d_aeta; a.axi = s->d_axi; a.wgt = s->d_w;
@@ -1960,7 +1964,7 @@ struct doma_batch {
   std::vector<doma_solver *> solvers;
   doma_options opts{};
   int dims = 3;
-  int tx = 8, threads = 256, grid = 0;
+  int tx = 8, threads = kMaxSweepThreadsF32, grid = 0;
   size_t smem = 0;
   int num_tasks = 0, epi_blocks = 0;
   SweepArgs<float> * d_args = nullptr;
@@ -1975,6 +1979,11 @@ struct doma_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   unsigned iters = 0;   // batched iterations since doma_batch_begin
+  // the last doma_batch_tune: ms of two batched sweeps per uniform block
+  // length (8, 16, 32) and with the per-class lengths; number of classes
+  float tune_uniform_ms[3] = {0.f, 0.f, 0.f};
+  float tune_mixed_ms = 0.f;
+  unsigned tune_classes = 0;
   std::chrono::steady_clock::time_point t_begin{};
   std::vector<void *> allocs;
 };
@@ -2040,6 +2049,7 @@ doma_status reschedule(doma_solver * s, int tx)
   s->sched.grid = std::max(1, std::min<int>(fit, (int)s->sched.tasks.size()));
   for (auto * a : {&s->a32}) {
     a->nbx = s->sched.nbx; a->nby = s->sched.nby; a->nbz = s->sched.nbz;
+    a->tx = s->sched.tx;
     a->num_tasks = (int)s->sched.tasks.size();
     a->tasks = s->d_tasks;
     a->done = s->d_done;
@@ -2052,7 +2062,7 @@ doma_status reschedule(doma_solver * s, int tx)
 doma_status build_batch_schedule(doma_batch * b)
 {
   const size_t P = b->solvers.size();
-  b->smem = sweep_smem_bytes(b->dims, DOMA_PREC_FP32, b->opts.scheme, b->tx);
+  b->smem = sweep_batch_smem_bytes(b->dims);
   std::vector<BatchTask> tasks;
   int max_levels = 0;
   for (auto * s : b->solvers) max_levels = std::max(max_levels, (int)s->sched.level_begin.size() - 1);
@@ -2078,7 +2088,7 @@ doma_status build_batch_schedule(doma_batch * b)
   }
   DOMA_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), P * sizeof(SweepArgs<float>),
                            cudaMemcpyHostToDevice));
-  const int fit = sweep_batch_resident_ctas(b->dims, b->opts.scheme, b->tx, b->threads, b->smem);
+  const int fit = sweep_batch_resident_ctas(b->dims, b->opts.scheme, b->threads, b->smem);
   if (fit <= 0) return bad("the batched sweep block does not fit on this device");
   b->grid = std::max(1, std::min(fit, b->num_tasks));
   return DOMA_OK;
@@ -2086,7 +2096,7 @@ doma_status build_batch_schedule(doma_batch * b)
 
 doma_status batch_sweep(doma_batch * b)
 {
-  return launch_sweep_batch(b->dims, b->opts.scheme, b->tx, b->grid, b->threads, b->smem, b->d_args,
+  return launch_sweep_batch(b->dims, b->opts.scheme, b->grid, b->threads, b->smem, b->d_args,
                             b->d_tasks, b->num_tasks, &b->d_ctl->ticket, &b->d_ctl->exit_count,
                             &b->d_ctl->epoch, b->d_loops, b->stream);
 }
@@ -2107,7 +2117,7 @@ doma_status batch_init_sources(doma_batch * b)
 doma_status batch_iteration(doma_batch * b, cudaStream_t st)
 {
   const size_t P = b->solvers.size();
-  DOMA_TRY(launch_sweep_batch(b->dims, b->opts.scheme, b->tx, b->grid, b->threads, b->smem,
+  DOMA_TRY(launch_sweep_batch(b->dims, b->opts.scheme, b->grid, b->threads, b->smem,
                               b->d_args, b->d_tasks, b->num_tasks, &b->d_ctl->ticket,
                               &b->d_ctl->exit_count, &b->d_ctl->epoch, b->d_loops, st));
   DOMA_TRY(launch_batch_epilogue(b->d_slots, b->d_block_prob, b->epi_blocks, b->d_loops,
@@ -2245,37 +2255,121 @@ doma_status doma_batch_set_stream(doma_batch * b, void * stream)
   return DOMA_OK;
 }
 
+// The batch's autotuner: a block length per class of problems.  A class is
+// (16-cell bucket of the longest mesh axis, ordinates per octant, groups).
+// For each length in {8, 16, 32} every solver is rescheduled to it and the
+// batched sweep is timed with all problems active (the uniform choice) and
+// with each class alone active (the others' tasks only publish their flags);
+// each class takes its fastest length.  The mixed assignment is then timed
+// against the best uniform length and kept only if it is faster.  The
+// results do not depend on the choice (every block length gives the same
+// bits).
 doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
 {
   if (!b) return bad("null batch");
-  float best_ms = 0.0f;
-  int best = b->tx;
+  const size_t P = b->solvers.size();
+  std::map<std::tuple<int, int, int>, std::vector<size_t>> classes;
+  for (size_t p = 0; p < P; ++p) {
+    const doma_solver * s = b->solvers[p];
+    const int n = (int)std::max(s->nx, std::max(s->ny, s->nz));
+    classes[std::make_tuple((n + 15) / 16, s->d_oct, s->G)].push_back(p);
+  }
+  const int txs[3] = {8, 16, 32};
+  std::vector<std::array<float, 3>> class_ms(classes.size());
+  float uniform_ms[3] = {0.f, 0.f, 0.f};
   cudaEvent_t e0, e1;
   DOMA_CUDA_TRY(cudaEventCreate(&e0));
   DOMA_CUDA_TRY(cudaEventCreate(&e1));
-  for (int tx : {8, 16, 32}) {
-    for (auto * s : b->solvers) DOMA_TRY(reschedule(s, tx));
-    b->tx = tx;
-    DOMA_TRY(build_batch_schedule(b));
-    DOMA_TRY(batch_init_sources(b));
+  auto time_sweeps = [&](float * ms) -> doma_status {
     DOMA_TRY(batch_sweep(b));  // warm-up
     DOMA_CUDA_TRY(cudaEventRecord(e0, b->stream));
-    for (int k = 0; k < 3; ++k) DOMA_TRY(batch_sweep(b));
+    for (int k = 0; k < 2; ++k) DOMA_TRY(batch_sweep(b));
     DOMA_CUDA_TRY(cudaEventRecord(e1, b->stream));
     DOMA_CUDA_TRY(cudaEventSynchronize(e1));
-    float ms = 0.0f;
-    DOMA_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-    if (best_ms == 0.0f || ms < best_ms) {
-      best_ms = ms;
-      best = tx;
+    DOMA_CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+    return DOMA_OK;
+  };
+  std::vector<BatchLoop> loops(P);
+  auto set_active = [&](const std::vector<size_t> * only) -> doma_status {
+    for (size_t p = 0; p < P; ++p) loops[p] = BatchLoop{only ? 0u : 1u, 0u, 0u, 0u, 0.0};
+    if (only)
+      for (size_t p : *only) loops[p].active = 1u;
+    DOMA_CUDA_TRY(cudaMemcpyAsync(b->d_loops, loops.data(), P * sizeof(BatchLoop),
+                                  cudaMemcpyHostToDevice, b->stream));
+    return DOMA_OK;
+  };
+  auto apply = [&](const std::vector<int> & per_problem) -> doma_status {
+    for (size_t p = 0; p < P; ++p) DOMA_TRY(reschedule(b->solvers[p], per_problem[p]));
+    DOMA_TRY(build_batch_schedule(b));
+    return batch_init_sources(b);
+  };
+  for (int k = 0; k < 3; ++k) {
+    DOMA_TRY(apply(std::vector<int>(P, txs[k])));
+    DOMA_TRY(set_active(nullptr));
+    DOMA_TRY(time_sweeps(&uniform_ms[k]));
+    size_t c = 0;
+    for (auto & kv : classes) {
+      DOMA_TRY(set_active(&kv.second));
+      DOMA_TRY(time_sweeps(&class_ms[c][k]));
+      ++c;
     }
   }
+  int best_uniform = 0;
+  for (int k = 1; k < 3; ++k)
+    if (uniform_ms[k] < uniform_ms[best_uniform]) best_uniform = k;
+  std::vector<int> mixed(P, txs[best_uniform]);
+  {
+    size_t c = 0;
+    for (auto & kv : classes) {
+      int bk = 0;
+      for (int k = 1; k < 3; ++k)
+        if (class_ms[c][k] < class_ms[c][bk]) bk = k;
+      for (size_t p : kv.second) mixed[p] = txs[bk];
+      ++c;
+    }
+  }
+  DOMA_TRY(apply(mixed));
+  DOMA_TRY(set_active(nullptr));
+  float mixed_ms = 0.f;
+  DOMA_TRY(time_sweeps(&mixed_ms));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  for (auto * s : b->solvers) DOMA_TRY(reschedule(s, best));
-  b->tx = best;
-  DOMA_TRY(build_batch_schedule(b));
-  if (tile_x) *tile_x = (uint32_t)best;
+  if (!(mixed_ms < uniform_ms[best_uniform])) {
+    mixed.assign(P, txs[best_uniform]);
+    DOMA_TRY(apply(mixed));
+  }
+  // the most common length (by problem count) stands for the batch
+  int count[3] = {0, 0, 0};
+  for (int tx : mixed) ++count[tx == 8 ? 0 : tx == 16 ? 1 : 2];
+  int most = 0;
+  for (int k = 1; k < 3; ++k)
+    if (count[k] > count[most]) most = k;
+  b->tx = txs[most];
+  b->tune_uniform_ms[0] = uniform_ms[0];
+  b->tune_uniform_ms[1] = uniform_ms[1];
+  b->tune_uniform_ms[2] = uniform_ms[2];
+  b->tune_mixed_ms = mixed_ms;
+  b->tune_classes = (unsigned)classes.size();
+  if (tile_x) *tile_x = (uint32_t)b->tx;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_tiles(doma_batch * b, uint32_t * tiles, size_t count)
+{
+  if (!b || !tiles) return bad("null batch or buffer");
+  if (count < b->solvers.size()) return bad("tiles buffer shorter than the batch");
+  for (size_t p = 0; p < b->solvers.size(); ++p) tiles[p] = (uint32_t)b->solvers[p]->sched.tx;
+  return DOMA_OK;
+}
+
+doma_status doma_batch_tune_report(doma_batch * b, float * uniform_ms, float * mixed_ms,
+                                   uint32_t * classes)
+{
+  if (!b) return bad("null batch");
+  if (uniform_ms)
+    for (int k = 0; k < 3; ++k) uniform_ms[k] = b->tune_uniform_ms[k];
+  if (mixed_ms) *mixed_ms = b->tune_mixed_ms;
+  if (classes) *classes = b->tune_classes;
   return DOMA_OK;
 }
 

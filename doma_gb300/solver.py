@@ -238,9 +238,25 @@ class Batch:
                   "doma_batch_set_stream", self.lib)
 
     def tune(self) -> int:
+        """Per-class block lengths (see doma_batch_tune); returns the most common."""
         tx = ctypes.c_uint32(0)
         abi.check(self.lib.doma_batch_tune(self._h, ctypes.byref(tx)), "doma_batch_tune", self.lib)
         return tx.value
+
+    def tiles(self) -> list[int]:
+        out = (ctypes.c_uint32 * len(self.problems))()
+        abi.check(self.lib.doma_batch_tiles(self._h, out, len(self.problems)), "doma_batch_tiles",
+                  self.lib)
+        return list(out)
+
+    def tune_report(self) -> dict:
+        u = (ctypes.c_float * 3)()
+        m = ctypes.c_float()
+        c = ctypes.c_uint32()
+        abi.check(self.lib.doma_batch_tune_report(self._h, u, ctypes.byref(m), ctypes.byref(c)),
+                  "doma_batch_tune_report", self.lib)
+        return {"uniform_ms": {8: u[0], 16: u[1], 32: u[2]}, "per_class_ms": m.value,
+                "classes": c.value}
 
     def solve(self) -> list[Report]:
         n = len(self.problems)

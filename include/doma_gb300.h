@@ -271,9 +271,18 @@ typedef struct doma_batch doma_batch;
 doma_status doma_batch_create(const doma_problem *problems, size_t count,
                               const doma_options *opts, doma_batch **out);
 doma_status doma_batch_set_stream(doma_batch *batch, void *stream);
-/* Time a few batched sweeps with each supported block length (8, 16, 32
- * cells along x) on this batch and keep the fastest; *tile_x gets it. */
+/* Autotune the block length (8, 16 or 32 cells along x) per class of
+ * problems -- (16-cell bucket of the longest axis, ordinates per octant,
+ * groups) -- by timing batched sweeps with each class alone active, then
+ * keep the per-class lengths if the whole batch sweeps faster with them than
+ * with the best single length.  *tile_x gets the most common length;
+ * doma_batch_tiles gives each problem's.  Results do not depend on it. */
 doma_status doma_batch_tune(doma_batch *batch, uint32_t *tile_x);
+doma_status doma_batch_tiles(doma_batch *batch, uint32_t *tiles, size_t count);
+/* What the last doma_batch_tune measured: ms of two batched sweeps with each
+ * uniform length (uniform_ms[3]: 8, 16, 32) and with the per-class lengths. */
+doma_status doma_batch_tune_report(doma_batch *batch, float *uniform_ms, float *mixed_ms,
+                                   uint32_t *classes);
 /* Solve every problem; reports[i] (count entries, may be NULL) get each
  * problem's status, iterations (mg_iterations) and updates.  Returns DOMA_OK
  * when all converged, else the first failing status. */

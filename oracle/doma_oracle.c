@@ -164,9 +164,22 @@ typedef struct {
   double *cur;        /* [N] current (increment) scalar flux */
   double *sigt;       /* [N] total xs of the group being solved */
   double **swept;     /* [T][N] per-thread swept flux */
+  double *octpsi;     /* single-thread-order mode with T > 1: [ordinates of an octant][N] w*psi */
   double **zf;        /* [T][nx*ny] per-thread z-face plane (3D) */
   double **yf;        /* [T][nx] per-thread y-face line */
 } oracle_state;
+
+/* Single-thread-order mode (oracle_set_single_thread_order): with T > 1
+ * threads the ordinates of an octant are still swept in parallel, but each
+ * writes w*psi to its own row, the rows are added to every cell's running sum
+ * in ordinate order, and the residual norms are summed sequentially.  The
+ * result is then bit-equal to a one-thread run (DOMA's T = 1 order), at
+ * multi-thread speed.  Off, the threads accumulate privately and the partial
+ * sums are added in thread order, as DOMA does with T threads
+ * (src/TransportSolver3D.cpp:610-621). */
+static int g_single_thread_order = 0;
+
+void oracle_set_single_thread_order(int on) { g_single_thread_order = on != 0; }
 
 static int validate(const doma_problem *p, const doma_options *o)
 {
@@ -233,6 +246,12 @@ static int state_init(oracle_state *s, const doma_problem *p, const doma_options
     s->zf[t] = calloc((size_t)s->nx * s->ny, sizeof(double));
     s->yf[t] = calloc(s->nx, sizeof(double));
   }
+  if (g_single_thread_order && s->T > 1) {
+    uint32_t most = 0;
+    for (int oc = 0; oc < 8; ++oc) most = s->counts[oc] > most ? s->counts[oc] : most;
+    s->octpsi = malloc(sizeof(double) * N * most);
+    if (!s->octpsi) return -1;
+  }
   return 0;
 }
 
@@ -242,7 +261,7 @@ static void state_free(oracle_state *s)
   free(s->vol); free(s->phi); free(s->prev); free(s->q); free(s->cur); free(s->sigt);
   if (s->swept)
     for (unsigned t = 0; t < s->T; ++t) { free(s->swept[t]); free(s->zf[t]); free(s->yf[t]); }
-  free(s->swept); free(s->zf); free(s->yf);
+  free(s->swept); free(s->zf); free(s->yf); free(s->octpsi);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -376,6 +395,9 @@ static void sweep_ordinate(oracle_state *s, int oct, unsigned n, unsigned tid)
   const int tw = s->o->scheme == DOMA_SCHEME_TW_DD;
   const double th = s->o->theta;
   double *sw = s->swept[tid], *zf = s->zf[tid], *yf = s->yf[tid];
+  /* single-thread-order mode: this ordinate's own row, summed in order later */
+  const int own_row = s->octpsi != NULL;
+  if (own_row) sw = s->octpsi + (size_t)(n - s->offs[oct]) * s->N;
 
   if (s->dims == 3) {
     memset(zf, 0, sizeof(double) * nx * ny);
@@ -396,7 +418,8 @@ static void sweep_ordinate(oracle_state *s, int oct, unsigned n, unsigned tid)
           else
             psi = dd3(s->q[c], s->sigt[c], amu, aeta, axi, p->dx[i], p->dy[j], p->dz[k],
                       &xface, &yf[i], zc);
-          sw[c] += wt * psi;
+          if (own_row) sw[c] = wt * psi;
+          else sw[c] += wt * psi;
         }
       }
     }
@@ -414,7 +437,8 @@ static void sweep_ordinate(oracle_state *s, int oct, unsigned n, unsigned tid)
                       &xface, &yf[i]);
         else
           psi = dd2(s->q[c], s->sigt[c], amu, aeta, p->dx[i], p->dy[j], &xface, &yf[i]);
-        sw[c] += wt * psi;
+        if (own_row) sw[c] = wt * psi;
+        else sw[c] += wt * psi;
       }
     }
   }
@@ -430,6 +454,13 @@ static void sweep(oracle_state *s)
     #pragma omp parallel for schedule(static)
     for (int n = 0; n < cnt; ++n)
       sweep_ordinate(s, oct, off + (unsigned)n, (unsigned)omp_get_thread_num());
+    if (s->octpsi) {
+      /* the one-thread order: ordinates of this octant, in order, onto the running sum */
+      double *sw = s->swept[0];
+      #pragma omp parallel for schedule(static)
+      for (size_t c = 0; c < s->N; ++c)
+        for (int n = 0; n < cnt; ++n) sw[c] += s->octpsi[(size_t)n * s->N + c];
+    }
   }
   #pragma omp parallel for schedule(static)
   for (size_t c = 0; c < s->N; ++c) {
@@ -445,7 +476,7 @@ static double si_residual(oracle_state *s, unsigned g)
 {
   double diff = 0.0, tot = 0.0;
   const double *phi = s->phi + (size_t)g * s->N;
-  #pragma omp parallel for reduction(+:diff, tot) schedule(static)
+  #pragma omp parallel for reduction(+:diff, tot) schedule(static) if(!g_single_thread_order)
   for (size_t c = 0; c < s->N; ++c) {
     const double d = s->cur[c];
     const double t = phi[c] + s->cur[c];
@@ -474,7 +505,7 @@ static void si_update(oracle_state *s, unsigned g)
 static double mg_residual(oracle_state *s)
 {
   double diff = 0.0, tot = 0.0;
-  #pragma omp parallel for reduction(+:diff, tot) schedule(static)
+  #pragma omp parallel for reduction(+:diff, tot) schedule(static) if(!g_single_thread_order)
   for (size_t c = 0; c < s->N; ++c) {
     for (unsigned g = 0; g < s->G; ++g) {
       const double a = s->phi[(size_t)g * s->N + c];

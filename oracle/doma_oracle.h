@@ -68,6 +68,13 @@ int oracle_source_iterations(const doma_problem *p, const doma_options *o,
 int oracle_multigroup_solve(const doma_problem *p, const doma_options *o, uint32_t num_threads,
                             double *phi_out, uint32_t *iterations, double *residual);
 
+/* Single-thread summation order with any thread count (on != 0): the
+ * ordinates of an octant still sweep in parallel, but every cell's angular
+ * sum and the residual norms follow the one-thread order, so results are
+ * bit-equal to num_threads = 1.  Off (the default) the threads keep private
+ * sums added in thread order, as DOMA does with T threads. */
+void oracle_set_single_thread_order(int on);
+
 #ifdef __cplusplus
 }
 #endif

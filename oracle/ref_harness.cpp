@@ -39,6 +39,7 @@ template <>
 class TransportSolver3D<OracleTap>
 {
 public:
+  static std::size_t numCells(const BrickMesh3D & mesh) { return mesh._cells.size(); }
   static void readFlux(const BrickMesh3D & mesh, unsigned int G, double * out)
   {
     const std::size_t N = mesh._cells.size();
@@ -60,6 +61,7 @@ template <>
 class TransportSolver2D<OracleTap>
 {
 public:
+  static std::size_t numCells(const BrickMesh2D & mesh) { return mesh._cells.size(); }
   static void readFlux(const BrickMesh2D & mesh, unsigned int G, double * out)
   {
     const std::size_t N = mesh._cells.size();
@@ -143,6 +145,37 @@ copyLog(const std::string & s, char * log, std::size_t cap)
   log[n] = '\0';
 }
 } // namespace
+
+// A deck as DOMA's XML reader leaves it in InputParameters
+// (src/InputParameters.cpp:92-524): the solver block, the quadrature, the
+// mesh intervals (widths and cell counts, already scaled by refinement + 1)
+// with one block id per interval triple, and the materials keyed by block id.
+// The XML itself is read by the project's reader, because DOMA's needs
+// pugixml; everything after that -- the mesh expansion
+// (BrickMesh3D/2D constructors), the solve and the text output -- is DOMA's.
+struct ref_deck
+{
+  uint32_t dims, num_groups, num_polar, num_azimuthal, scheme, mode;  // mode: 0 fixed, 1 eigen
+  double fs_tol, mg_tol, k_tol;
+  uint32_t fs_max_it, mg_max_it;
+  uint32_t nxi, nyi, nzi;                 // intervals per axis (nzi = 1 in 2D)
+  const double * dx;                      // interval widths
+  const double * dy;
+  const double * dz;
+  const uint32_t * ix;                    // cells per interval
+  const uint32_t * iy;
+  const uint32_t * iz;
+  const uint32_t * blocks;                // [nzi][nyi][nxi]
+  uint32_t num_mats;
+  const uint32_t * mat_ids;               // block id of each material
+  const double * total;                   // [num_mats][G]
+  const double * scatter;                 // [num_mats][G*G], DOMA's stored order
+  const uint8_t * has_source;             // [num_mats]
+  const double * source;                  // [num_mats][G]
+  const uint8_t * has_fission;            // [num_mats]
+  const double * chi_p;                   // [num_mats][G]
+  const double * prod;                    // [num_mats][G]
+};
 
 extern "C" {
 
@@ -382,6 +415,126 @@ ref_quadrature(unsigned int np, unsigned int na, unsigned int dims, double * mu,
     }
   }
   return static_cast<int>(k);
+}
+
+
+// Solve a deck with the reference.  Returns 1 / 0 for DOMA's true / false and
+// -1 if phi_cap is too small.  phi_out receives [G][N] of the expanded mesh
+// and *num_cells its N.  DOMA keeps k private: eigen decks print it in the
+// captured log, with `precision` digits when precision > 0 (k_out is set to 0).
+// With a non-empty out_base DOMA also writes its text output there.
+int
+ref_solve_deck(const ref_deck * d, unsigned int num_threads, double * phi_out, std::size_t phi_cap,
+               std::size_t * num_cells, double * k_out, char * log, std::size_t log_cap,
+               const char * out_base, int precision)
+{
+  if (k_out) *k_out = 0.0;
+  omp_set_num_threads(static_cast<int>(num_threads));
+  InputParameters params;
+  params._mode = d->mode == 1 ? RunMode::Eigen : RunMode::FixedSrc;
+  params._num_e_groups = d->num_groups;
+  params._t0 = 0.0;
+  params._t1 = 1.0;
+  params._num_steps = 1u;
+  params._ic = TransientIC::Zero;
+  params._src_it_tol = d->fs_tol;
+  params._gs_tol = d->mg_tol;
+  params._k_tol = d->k_tol;
+  params._dsa = false;
+  params._num_src_it = d->fs_max_it;
+  params._num_mg_it = d->mg_max_it;
+  params._num_polar = d->num_polar;
+  params._num_azimuthal = d->num_azimuthal;
+  params._eq_type = d->scheme == DOMA_SCHEME_TW_DD ? EquationType::TW_DD : EquationType::DD;
+  params._num_dims = d->dims;
+  params._refinement = 0u;
+  params._x_intervals.assign(d->ix, d->ix + d->nxi);
+  params._y_intervals.assign(d->iy, d->iy + d->nyi);
+  params._dx.assign(d->dx, d->dx + d->nxi);
+  params._dy.assign(d->dy, d->dy + d->nyi);
+  std::size_t nb = std::size_t(d->nxi) * d->nyi;
+  if (d->dims == 3)
+  {
+    params._z_intervals.assign(d->iz, d->iz + d->nzi);
+    params._dz.assign(d->dz, d->dz + d->nzi);
+    nb *= d->nzi;
+  }
+  params._blocks.assign(d->blocks, d->blocks + nb);
+  const unsigned int G = d->num_groups;
+  for (unsigned int m = 0; m < d->num_mats; ++m)
+  {
+    MaterialProps mp;
+    mp._num_d_groups = 0u;
+    mp._g_total.assign(d->total + m * G, d->total + (m + 1) * G);
+    mp._g_g_scatter_mat.assign(d->scatter + m * G * G, d->scatter + (m + 1) * G * G);
+    if (d->has_source[m])
+      mp._g_src.assign(d->source + m * G, d->source + (m + 1) * G);
+    if (d->has_fission[m])
+    {
+      mp._g_chi_p.assign(d->chi_p + m * G, d->chi_p + (m + 1) * G);
+      mp._g_prod.assign(d->prod + m * G, d->prod + (m + 1) * G);
+    }
+    params._block_mat_info.emplace(d->mat_ids[m], mp);
+  }
+  const std::string base = out_base ? std::string(out_base) : std::string();
+  const bool eigen = d->mode == 1;
+
+  std::ostringstream captured;
+  std::streambuf * old = std::cout.rdbuf(captured.rdbuf());
+  const std::streamsize old_precision = std::cout.precision();
+  if (precision > 0)
+    std::cout.precision(precision);
+  bool ok = false;
+  int rc = 0;
+  auto finish = [&](auto & mesh, auto & solver, auto reader, auto counter) {
+    ok = eigen ? solver.solveEigenvalue(base) : solver.solveFixedSource(base);
+    const std::size_t N = counter(mesh);
+    *num_cells = N;
+    if (N * G > phi_cap)
+    {
+      rc = -1;
+      return;
+    }
+    reader(mesh, G, phi_out);
+  };
+  if (d->dims == 3)
+  {
+    std::array<BoundaryCondition, 6u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh3D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver3D solver(mesh, params, false, num_threads);
+      finish(mesh, solver, TransportSolver3D<OracleTap>::readFlux, TransportSolver3D<OracleTap>::numCells);
+    }
+    else
+    {
+      TWDDTransportSolver3D solver(mesh, params, false, num_threads);
+      finish(mesh, solver, TransportSolver3D<OracleTap>::readFlux, TransportSolver3D<OracleTap>::numCells);
+    }
+  }
+  else
+  {
+    std::array<BoundaryCondition, 4u> bcs;
+    bcs.fill(BoundaryCondition::Vacuum);
+    BrickMesh2D mesh(params, bcs, num_threads);
+    mesh.validateProps();
+    if (params._eq_type == EquationType::DD)
+    {
+      DDTransportSolver2D solver(mesh, params, false, num_threads);
+      finish(mesh, solver, TransportSolver2D<OracleTap>::readFlux, TransportSolver2D<OracleTap>::numCells);
+    }
+    else
+    {
+      TWDDTransportSolver2D solver(mesh, params, false, num_threads);
+      finish(mesh, solver, TransportSolver2D<OracleTap>::readFlux, TransportSolver2D<OracleTap>::numCells);
+    }
+  }
+  std::cout.precision(old_precision);
+  std::cout.rdbuf(old);
+  copyLog(captured.str(), log, log_cap);
+  return rc < 0 ? rc : (ok ? 1 : 0);
 }
 
 } // extern "C"

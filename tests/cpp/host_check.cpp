@@ -6,9 +6,10 @@
 //   host_check point <deck> <flux.bin> x y [z] g fluxAtPoint
 //   host_check solve <deck> <flux.bin> [verbose|quiet] [base]
 //                                                drop-in solver on the GPU (the deck's
-//                                                mode; a transient writes its step files
-//                                                under base); writes the flux and prints
-//                                                SI counts (JSON)
+//                                                mode; a fixed-source solve writes DOMA's
+//                                                text output and a transient its step
+//                                                files under base); writes the flux and
+//                                                prints SI counts (JSON)
 #include <array>
 #include <cstdio>
 #include <cstdlib>
@@ -63,8 +64,17 @@ int main(int argc, char ** argv)
                 << ", \"refinement\": " << p._refinement << ", \"theta\": " << p._theta
                 << ", \"precision\": " << (int)p._precision << ", \"dx\": ";
       json_list(p._dx);
+      std::cout << ", \"dy\": ";
+      json_list(p._dy);
+      std::cout << ", \"dz\": ";
+      json_list(p._dz);
       std::cout << ", \"ix\": ";
       json_list(p._x_intervals);
+      std::cout << ", \"iy\": ";
+      json_list(p._y_intervals);
+      std::cout << ", \"iz\": ";
+      json_list(p._z_intervals);
+      std::cout << ", \"k_tol\": " << p._k_tol;
       std::cout << ", \"blocks\": ";
       json_list(p._blocks);
       std::cout << ", \"materials\": {";
@@ -80,6 +90,8 @@ int main(int argc, char ** argv)
         json_list(kv.second->_g_src);
         std::cout << ", \"chi_p\": ";
         json_list(kv.second->_g_chi_p);
+        std::cout << ", \"prod\": ";
+        json_list(kv.second->_g_prod);
         std::cout << ", \"delayed_groups\": " << kv.second->_num_d_groups << ", \"inv_v\": ";
         json_list(kv.second->_g_inv_v);
         std::cout << ", \"chi_d\": ";
@@ -134,12 +146,12 @@ int main(int argc, char ** argv)
         double k = 0.0;
         if (p._eq_type == EquationType::DD) {
           DDTransportSolver3D s(mesh, p, verbose, 1);
-          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource(base);
           st = s.stats();
           k = s.eigenvalue();
         } else {
           TWDDTransportSolver3D s(mesh, p, verbose, 1);
-          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource(base);
           st = s.stats();
           k = s.eigenvalue();
         }
@@ -179,12 +191,12 @@ int main(int argc, char ** argv)
         double k = 0.0;
         if (p._eq_type == EquationType::DD) {
           DDTransportSolver2D s(mesh, p, verbose, 1);
-          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource(base);
           st = s.stats();
           k = s.eigenvalue();
         } else {
           TWDDTransportSolver2D s(mesh, p, verbose, 1);
-          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource();
+          ok = transient ? s.solveTransient(base) : eigen ? s.solveEigenvalue() : s.solveFixedSource(base);
           st = s.stats();
           k = s.eigenvalue();
         }

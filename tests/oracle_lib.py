@@ -65,6 +65,8 @@ def oracle() -> ctypes.CDLL:
             ctypes.POINTER(abi.DomaTransient), ctypes.c_uint32, _dp, _dp, _u32p, _u32p,
             ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t),
         ]
+        lib.oracle_set_single_thread_order.restype = None
+        lib.oracle_set_single_thread_order.argtypes = [ctypes.c_int]
         lib.oracle_multigroup_solve.restype = ctypes.c_int
         lib.oracle_multigroup_solve.argtypes = [
             ctypes.POINTER(abi.DomaProblem), ctypes.POINTER(abi.DomaOptions), ctypes.c_uint32,
@@ -122,8 +124,12 @@ def ref_quadrature(np_, na, dims):
     return _quad(ref().ref_quadrature, np_, na, dims)
 
 
-def oracle_solve(p: Problem, opts: abi.DomaOptions, threads: int = 1):
-    """-> (phi[G][N], converged, si_counts, mg_iterations, mg_residual)"""
+def oracle_solve(p: Problem, opts: abi.DomaOptions, threads: int = 1, ordered: bool = False):
+    """-> (phi[G][N], converged, si_counts, mg_iterations, mg_residual)
+
+    ordered: sum in the one-thread order with any thread count (bit-equal to
+    threads=1, which DOMA's single-thread results and the GPU's exact mode
+    follow); otherwise threads > 1 sum as DOMA does with that many threads."""
     phi = np.zeros((p.num_groups, p.num_cells))
     cap = 1 << 16
     si = np.zeros(cap, dtype=np.uint32)
@@ -131,9 +137,14 @@ def oracle_solve(p: Problem, opts: abi.DomaOptions, threads: int = 1):
     mg = ctypes.c_uint32(0)
     res = ctypes.c_double(0)
     cp = p.to_c()
-    rc = oracle().oracle_solve(ctypes.byref(cp), ctypes.byref(opts), threads,
-                               phi.ctypes.data_as(_dp), si.ctypes.data_as(_u32p), cap,
-                               ctypes.byref(n_si), ctypes.byref(mg), ctypes.byref(res))
+    lib = oracle()
+    lib.oracle_set_single_thread_order(1 if ordered else 0)
+    try:
+        rc = lib.oracle_solve(ctypes.byref(cp), ctypes.byref(opts), threads,
+                              phi.ctypes.data_as(_dp), si.ctypes.data_as(_u32p), cap,
+                              ctypes.byref(n_si), ctypes.byref(mg), ctypes.byref(res))
+    finally:
+        lib.oracle_set_single_thread_order(0)
     if rc < 0:
         raise ValueError("oracle rejected the problem")
     return phi, bool(rc), si[: min(n_si.value, cap)].copy(), int(mg.value), float(res.value)

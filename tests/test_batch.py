@@ -56,6 +56,10 @@ def test_batch_tuner_keeps_results():
         a = [b.scalar_flux(i) for i in range(len(ps))]
         tx = b.tune()
         assert tx in (8, 16, 32)
+        tiles = b.tiles()
+        assert len(tiles) == len(ps) and all(t in (8, 16, 32) for t in tiles)
+        rep = b.tune_report()
+        assert rep["classes"] >= 1 and min(rep["uniform_ms"].values()) > 0
         second = [r.mg_iterations for r in b.solve()]
         c = [b.scalar_flux(i) for i in range(len(ps))]
     assert first == second

@@ -16,7 +16,9 @@
 The FP64 drop-in mode must give the oracle's bits and counts; the FP32 mode
 must stay within 1e-5 relative L2 of the oracle's flux.  The oracle is the C
 restatement of DOMA (bit-equal to DOMA on every golden fixture), run once per
-case with all host threads and shared between the tests of this file.
+case with all host threads in the one-thread summation order (bit-equal to a
+single-thread run, which is the order DOMA's single-thread results and the
+GPU's exact mode follow) and shared between the tests of this file.
 """
 import os
 
@@ -62,7 +64,7 @@ _ORACLE = {}
 def oracle_result(key):
     if key not in _ORACLE:
         p, opts = checkerboard_case(key[1]) if key[0] == "checkerboard" else streaming_case()
-        _ORACLE[key] = (p, opts, ol.oracle_solve(p, opts, threads=THREADS))
+        _ORACLE[key] = (p, opts, ol.oracle_solve(p, opts, threads=THREADS, ordered=True))
     return _ORACLE[key]
 
 

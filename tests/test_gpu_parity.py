@@ -177,6 +177,27 @@ def test_persistent_and_level_schedules_agree(monkeypatch, precision, dims):
     assert np.array_equal(a, b) and list(ra.si_counts) == list(rb.si_counts)
 
 
+@pytest.mark.parametrize("tile", [8, 16, 32])
+@pytest.mark.parametrize("np_,na", [(2, 3), (3, 3), (5, 5)])
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+@pytest.mark.parametrize("dims", [2, 3])
+def test_packed_and_scalar_sweep_bodies_agree(monkeypatch, tile, np_, na, scheme, dims):
+    """In single precision the dataflow sweep runs the packed body (two
+    ordinates per lane in f32x2 instructions) and the one-launch-per-level
+    sweep the scalar body (one ordinate per lane).  Per-element rounding is
+    the same, so whole solves must agree bit for bit: with an odd ordinate
+    count (the last pair half empty) and with more ordinates per octant than
+    one task holds (25 = 16 + 9)."""
+    p = P.random_problem(43, dims, 21, 13, 6, groups=2, np_=np_, na=na, materials=3)
+    opts = P.make_options(scheme=scheme, theta=0.8, precision="fp32", fs_tol=1e-6, mg_tol=1e-6,
+                          tile=(tile, 0, 0))
+    a, ra = run(p, opts)
+    monkeypatch.setenv("DOMA_SWEEP_SCHEDULE", "levels")
+    b, rb = run(p, opts)
+    assert list(ra.si_counts) == list(rb.si_counts)
+    assert np.array_equal(a, b), rel_linf(a, b)
+
+
 def test_wait_timeout_is_reported_and_context_survives(monkeypatch):
     """A dependency wait that can never be satisfied gives up after a bounded
     number of polls; the host sees DOMA_DEVICE_WAIT_TIMEOUT and the CUDA

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as ol
+from doma_gb300 import problems as P
 from golden_cases import (case_names, eigen_case_names, load_case, load_eigen_case,
                           load_transient_case, quadrature_sets, transient_case_names)
 
@@ -40,6 +41,19 @@ def test_oracle_threads_agree():
     assert ok and list(si) == list(exp["si_counts"])
     rel = np.abs(phi - exp["phi"]).max() / np.abs(exp["phi"]).max()
     assert rel < 1e-13
+
+
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
+@pytest.mark.parametrize("dims", [2, 3])
+def test_oracle_single_thread_order_with_threads(scheme, dims):
+    """Ordinates in parallel, sums in the one-thread order: the same bits as a
+    single-thread run (and therefore as DOMA's single-thread run)."""
+    p = P.random_problem(41, dims, 9, 8, 6, groups=3, np_=3, na=2, materials=4, fission=True)
+    opts = P.make_options(scheme=scheme, theta=0.8, fs_tol=1e-9, mg_tol=1e-9)
+    a, ok_a, si_a, mg_a, _ = ol.oracle_solve(p, opts, threads=1)
+    b, ok_b, si_b, mg_b, _ = ol.oracle_solve(p, opts, threads=4, ordered=True)
+    assert np.array_equal(a, b)
+    assert (ok_a, list(si_a), mg_a) == (ok_b, list(si_b), mg_b)
 
 
 def test_oracle_rejects_bad_input():
