@@ -13,10 +13,8 @@ namespace doma {
 
 constexpr double kPi = 3.14159265358979323846;  // M_PI
 
-// Largest sweep CTA: 16 ordinates x 16 pencils (scalar bodies), or 8
-// ordinate pairs x 16 pencils (the packed single-precision body).
+// Largest sweep CTA: 16 ordinates x 16 pencils.
 constexpr int kMaxSweepThreads = 256;
-constexpr int kMaxSweepThreadsF32 = 128;
 
 // Error reporting (per thread, read through doma_last_error()).
 void set_error(const std::string & msg);
@@ -134,9 +132,8 @@ doma_status launch_sweep(int dims, int precision, int scheme, const Schedule & s
                          cudaStream_t stream, uint64_t * launches);
 int sweep_tile_x(int requested);  // supported block length along x: 8, 16 or 32
 // Threads of a sweep CTA for an ordinate group of gs: one per (ordinate,
-// pencil), or per (ordinate pair, pencil) for the packed single-precision body
-// (the persistent and batched kernels), in whole warps.
-int sweep_threads(int precision, int gs, bool packed);
+// pencil), in whole warps.
+int sweep_threads(int gs);
 size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx);
 doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem);
 // CTAs of the persistent sweep kernel that fit on the device at once.

@@ -314,7 +314,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   Schedule sc;  // persistent mode: only the launch shape is used
   sc.tx = tx;
   sc.persistent = true;
-  sc.threads = sweep_threads(DOMA_PREC_FP32, std::min(kGroup, d_oct), true);
+  sc.threads = sweep_threads(std::min(kGroup, d_oct));
   sc.smem = sweep_smem_bytes(dims, DOMA_PREC_FP32, (int)scheme, tx);
   st = sweep_prepare(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.smem);
   if (st != DOMA_OK) return st;

@@ -242,7 +242,7 @@ void build_schedule(doma_solver * s)
   sc.nbx = (s->nx + sc.tx - 1) / sc.tx;
   sc.nby = (s->ny + sc.ty - 1) / sc.ty;
   sc.nbz = (s->nz + sc.tz - 1) / sc.tz;
-  sc.threads = sweep_threads(s->opts.precision, sc.gs, true);
+  sc.threads = sweep_threads(sc.gs);
   sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx);
   const int levels = sc.nbx + sc.nby + sc.nbz - 2;
   std::vector<std::vector<Task>> by_level(levels);
@@ -1964,7 +1964,7 @@ struct doma_batch {
   std::vector<doma_solver *> solvers;
   doma_options opts{};
   int dims = 3;
-  int tx = 8, threads = kMaxSweepThreadsF32, grid = 0;
+  int tx = 8, threads = kMaxSweepThreads, grid = 0;
   size_t smem = 0;
   int num_tasks = 0, epi_blocks = 0;
   SweepArgs<float> * d_args = nullptr;

@@ -42,12 +42,6 @@
 
 #include "common.cuh"
 
-#ifndef DOMA_SWEEP_MIN_CTAS_PACKED_TW
-#define DOMA_SWEEP_MIN_CTAS_PACKED_TW 5
-#endif
-#ifndef DOMA_SWEEP_MIN_CTAS_PACKED_DD
-#define DOMA_SWEEP_MIN_CTAS_PACKED_DD 6
-#endif
 #ifndef DOMA_SWEEP_MIN_CTAS
 #define DOMA_SWEEP_MIN_CTAS 3
 #endif
@@ -270,131 +264,6 @@ __device__ __forceinline__ float twdd2_fast(float q, float st, float hx, float h
   return c;
 }
 
-// ---- packed pairs of single-precision values (f32x2) --------------------------
-// Blackwell executes add / sub / mul / fma on two FP32 values per instruction
-// (the .f32x2 forms).  Each element is rounded exactly as the scalar
-// instruction rounds it (round to nearest, denormals kept), so a lane that
-// solves two ordinates with packed instructions produces the same bits as two
-// lanes with the scalar intrinsics above.  A pair lives in one 64-bit
-// register: the low half is the first ordinate, the high half the second.
-using f2 = unsigned long long;
-
-__device__ __forceinline__ f2 pk(float a, float b)
-{
-  f2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ f2 pk(float2 v) { return pk(v.x, v.y); }
-__device__ __forceinline__ f2 dup(float a) { return pk(a, a); }
-__device__ __forceinline__ float2 upk(f2 v)
-{
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-  return r;
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b)
-{
-  f2 d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b)
-{
-  f2 d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b)
-{
-  f2 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c)
-{
-  f2 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-// exact negation of both halves (sign bits)
-__device__ __forceinline__ f2 neg2(f2 a) { return a ^ 0x8000000080000000ull; }
-__device__ __forceinline__ f2 rcp2(f2 a)
-{
-  const float2 v = upk(a);
-  return pk(rcp_approx(v.x), rcp_approx(v.y));
-}
-__device__ __forceinline__ f2 sel2(bool c, f2 a, f2 b) { return c ? a : b; }
-
-// dd3_fast on a pair of ordinates.
-__device__ __forceinline__ f2 dd3_fast2(f2 q, f2 st, f2 cx, f2 cy, f2 cz, f2 cyz, f2 & x, f2 & y,
-                                        f2 & z)
-{
-  const f2 num = fma2(cz, z, fma2(cy, y, fma2(cx, x, q)));
-  const f2 c = mul2(num, rcp2(add2(add2(cx, cyz), st)));
-  const f2 two = dup(2.0f);
-  x = fma2(two, c, neg2(x));
-  y = fma2(two, c, neg2(y));
-  z = fma2(two, c, neg2(z));
-  return c;
-}
-
-__device__ __forceinline__ f2 dd2_fast2(f2 q, f2 st, f2 cx, f2 cy, f2 & x, f2 & y)
-{
-  const f2 c = mul2(fma2(cy, y, fma2(cx, x, q)), rcp2(add2(add2(cx, cy), st)));
-  const f2 two = dup(2.0f);
-  x = fma2(two, c, neg2(x));
-  y = fma2(two, c, neg2(y));
-  return c;
-}
-
-// tw_rweight on a pair: the max, the saturation and the select per element.
-__device__ __forceinline__ f2 tw_rweight2(f2 n, f2 D, f2 flux)
-{
-  const f2 dx = mul2(D, flux);
-  const float2 dn = upk(sub2(dx, n));
-  const f2 den = pk(fmaxf(dn.x, 1e-30f), fmaxf(dn.y, 1e-30f));
-  const float2 t = upk(fma2(dx, rcp2(den), dup(-1.0f)));
-  const float2 r = upk(add2(dup(1.0f), pk(__saturatef(t.x), __saturatef(t.y))));
-  const float2 fl = upk(flux);
-  return pk(fl.x > 1e-8f ? r.x : 2.0f, fl.y > 1e-8f ? r.y : 2.0f);
-}
-
-// twdd3_fast on a pair; h2y = hy + hy and h2z = hz + hz are the caller's
-// (per-thread constants).
-__device__ __forceinline__ f2 twdd3_fast2(f2 q, f2 st, f2 hx, f2 hy, f2 hz, f2 h2y, f2 h2z, f2 th,
-                                          f2 om, f2 & x, f2 & y, f2 & z)
-{
-  const f2 X = mul2(hx, x), Y = mul2(hy, y), Z = mul2(hz, z);
-  const f2 B = fma2(th, add2(add2(X, Y), Z), mul2(th, q));
-  const f2 h2x = add2(hx, hx);
-  const f2 ra = tw_rweight2(fma2(om, X, B), add2(add2(st, h2y), h2z), x);
-  const f2 rb = tw_rweight2(fma2(om, Y, B), add2(add2(st, h2z), h2x), y);
-  const f2 rc = tw_rweight2(fma2(om, Z, B), add2(add2(st, h2y), h2x), z);
-  const f2 num = fma2(rc, Z, fma2(rb, Y, fma2(ra, X, q)));
-  const f2 den = fma2(hz, rc, fma2(hy, rb, fma2(hx, ra, st)));
-  const f2 c = mul2(num, rcp2(den));
-  x = fma2(ra, sub2(c, x), x);
-  y = fma2(rb, sub2(c, y), y);
-  z = fma2(rc, sub2(c, z), z);
-  return c;
-}
-
-__device__ __forceinline__ f2 twdd2_fast2(f2 q, f2 st, f2 hx, f2 hy, f2 txv, f2 th, f2 om, f2 & x,
-                                          f2 & y)
-{
-  const f2 X = mul2(hx, x), Y = mul2(hy, y);
-  const f2 B = fma2(th, add2(X, Y), mul2(th, q));
-  const f2 ra = tw_rweight2(fma2(om, X, B), add2(st, add2(hy, hy)), x);
-  const f2 rb = tw_rweight2(add2(fma2(om, Y, B), txv), add2(st, add2(hx, hx)), y);
-  const f2 num = fma2(rb, Y, fma2(ra, X, q));
-  const f2 den = fma2(hy, rb, fma2(hx, ra, st));
-  const f2 c = mul2(num, rcp2(den));
-  x = fma2(ra, sub2(c, x), x);
-  y = fma2(rb, sub2(c, y), y);
-  return c;
-}
-
 // ---- scheduling primitives -------------------------------------------------
 
 __device__ __forceinline__ void st_release(unsigned * p, unsigned v)
@@ -408,12 +277,6 @@ __device__ __forceinline__ void st_global_if(float * p, float v, bool c)
 {
   asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.f32 [%0], %1;\n\t}"
                ::"l"(p), "f"(v), "r"((unsigned)c));
-}
-
-__device__ __forceinline__ void st_global2_if(float * p, f2 v, bool c)
-{
-  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.b64 [%0], %1;\n\t}"
-               ::"l"(p), "l"(v), "r"((unsigned)c));
 }
 
 __device__ __forceinline__ void st_shared_if(float * p, float v, bool c)
@@ -726,11 +589,11 @@ struct TaskSmemF32 {
 
 // Coalesced, all-loads-first copy of `count` float4s: in each round every
 // load of a thread is issued before its first shared-memory store, so the
-// round trips overlap.  A full-size CTA (NT threads) needs one round.
-template <int COUNT, int NT = kMaxSweepThreads, typename L>
+// round trips overlap.  A full-size CTA (kMaxSweepThreads) needs one round.
+template <int COUNT, typename L>
 __device__ __forceinline__ void stage_f4(float4 * dst, L load)
 {
-  constexpr int IT = (COUNT + NT - 1) / NT;
+  constexpr int IT = (COUNT + kMaxSweepThreads - 1) / kMaxSweepThreads;
   for (int base = 0; base < COUNT; base += IT * (int)blockDim.x) {
     float4 v[IT];
 #pragma unroll
@@ -897,7 +760,13 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const float wgt = PAIRS ? wts[min(nl, kGroup - 1)] : 0.f;
     float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
+    // A warp whose two ordinates both lie past the group's last one has
+    // nothing to solve: it skips the walk (warp-uniform).  The batched launch
+    // sizes every CTA for a full group, so a problem with 4 or 9 ordinates
+    // per octant would otherwise spend 6 or 3 idle warps' issue slots here.
+    const bool warp_busy = 2 * (t >> 5) < gs;
     // 3D: fully unrolled; 2D (long skew) partly, which keeps it out of local memory
+    if (warp_busy)
 #pragma unroll (DIMS == 3 ? STEPS : 4)
     for (int s = 0; s < STEPS; ++s) {
       const int il = s - d;
@@ -972,312 +841,39 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   }
 }
 
-// ---- single precision, packed ordinate pairs --------------------------------------
-//
-// The same task as run_task_f32, with each lane solving two ordinates of one
-// pencil in f32x2 instructions: a warp holds two ordinate pairs (half-warps)
-// over the 16-pencil cross-section, a CTA of kMaxSweepThreadsF32 threads the
-// 8 pairs of a 16-ordinate group.  The per-step loads of the y / z faces and
-// the x coefficients are 8-byte pairs (the x coefficients are staged
-// cell-major, [TX][kGroup], for that), the outgoing faces are stored as pairs,
-// and the lane forms its pair's w psi sum during the walk -- the same pair sums
-// the scalar body forms, so the two bodies give the same bits.
-
-template <int DIMS, int TX>
-struct TaskSmemF32P {
-  static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
-  static constexpr int CELLS = TX * PY * PZ;
-  static constexpr int SKEW = PY + PZ - 2;
-  static constexpr int FPAD = SKEW * kGroup;
-  static constexpr int YF = PZ * TX * kGroup;
-  static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;
-  static constexpr int YREG = YF + 2 * FPAD;
-  static constexpr int ZREG = DIMS == 3 ? ZF + 2 * FPAD : 0;
-  static constexpr int CREG = 2 * (CELLS + 2 * SKEW);          // {q, sigma_t} per cell
-  static constexpr int HREG = kGroup * TX + 2 * FPAD;          // x coefficients [TX][kGroup]
-  static constexpr int RREG = TX + 2 * SKEW;                   // 1/dx [TX] (2D TW-DD)
-  static constexpr int RREG_PAD = RREG + (RREG & 1);           // keeps the next region 8-byte aligned
-  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG_PAD + kGroup + (kGroup / 2) * CELLS;
-  static constexpr size_t bytes = floats * sizeof(float);
-  static_assert(FPAD % 4 == 0 && YREG % 4 == 0, "face regions stay float4-aligned");
-  static_assert(CREG % 2 == 0 && HREG % 2 == 0, "pair regions stay 8-byte aligned");
-};
-
-template <int DIMS, int SCHEME, int TX>
-__device__ __forceinline__ void run_task_f32p(const SweepArgs<float> & A, const Task task,
-                                              unsigned char * smem_raw, bool dataflow, unsigned epoch)
-{
-  using SM = TaskSmemF32P<DIMS, TX>;
-  constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
-  constexpr unsigned FULL = 0xffffffffu;
-  constexpr bool TW = SCHEME == DOMA_SCHEME_TW_DD;
-  constexpr float HS = TW ? 0.5f : 1.0f;
-  constexpr int NT = kMaxSweepThreadsF32;
-  const int og = task.og;
-  const int o = task.oct;
-  const int of = task.grp * 8 + o;
-  const bool rx = (o & 4) != 0, ry = (o & 2) != 0, rz = (o & 1) != 0;
-  const int nx = A.nx, ny = A.ny, nz = DIMS == 3 ? A.nz : 1;
-  const size_t N = (size_t)nx * ny * nz;
-  const float * gq = A.q + (size_t)task.grp * N;
-  const float * gsig = A.sigt + (size_t)task.grp * N;
-  const int n0 = og * kGroup;
-  const int gs = min(kGroup, A.d_oct - n0);
-  const int i0 = task.bi * TX, j0 = task.bj * PY, k0 = task.bk * PZ;
-  const int vx = min(TX, nx - i0), vy = min(PY, ny - j0), vz = min(PZ, nz - k0);
-  const FacePlanes<float> F(A, of, og);
-  const size_t slot = F.plane;
-
-  const int t = threadIdx.x;
-  const int lane = t & 31;
-  const int p = lane & 15;
-  const int pr = (t >> 5) * 2 + (lane >> 4);   // ordinate pair: ordinates 2 pr, 2 pr + 1
-  const int na = 2 * pr;
-  const bool second = na + 1 < gs;             // the pair's second ordinate exists
-  const int jl = DIMS == 3 ? (p & 3) : p;
-  const int kl = DIMS == 3 ? (p >> 2) : 0;
-  const bool active = na < gs && jl < vy && kl < vz;
-  const int ob = A.oct_offset[o] + n0;
-  const int orda = ob + min(na, gs - 1), ordb = ob + min(na + 1, gs - 1);
-
-  constexpr int SKEW = SM::SKEW, FPAD = SM::FPAD;
-  float * const sbase = reinterpret_cast<float *>(smem_raw);
-  float * yin = sbase + FPAD;                                            // [PZ][TX][kGroup]
-  float * zin = sbase + SM::YREG + (DIMS == 3 ? FPAD : 0);               // [PY][TX][kGroup]
-  float2 * cell = reinterpret_cast<float2 *>(sbase + SM::YREG + SM::ZREG) + SKEW;  // {q, sigma_t}
-  float * hxs = sbase + SM::YREG + SM::ZREG + SM::CREG + FPAD;           // [TX][kGroup]
-  float * rlx = hxs - FPAD + SM::HREG + SKEW;                            // [TX] 1/dx
-  float * wts = rlx - SKEW + SM::RREG_PAD;                               // [kGroup] weights
-  float * P = wts + kGroup;                                              // [kGroup / 2][CELLS]
-
-  for (int e = t; e < FPAD; e += blockDim.x) {
-    yin[e - FPAD] = 0.f;
-    yin[SM::YF + e] = 0.f;
-    hxs[e - FPAD] = 0.f;
-    hxs[kGroup * TX + e] = 0.f;
-    if constexpr (DIMS == 3) {
-      zin[e - FPAD] = 0.f;
-      zin[SM::ZF + e] = 0.f;
-    }
-  }
-  for (int e = t; e < SKEW; e += blockDim.x) {
-    cell[e - SKEW] = make_float2(0.f, 1.f);
-    cell[CELLS + e] = make_float2(0.f, 1.f);
-    rlx[e - SKEW] = 0.f;
-    rlx[TX + e] = 0.f;
-  }
-
-  auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
-  auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
-  auto phys_k = [&](int kk) { return rz ? nz - 1 - (k0 + kk) : k0 + kk; };
-
-  // -- stage what does not depend on upstream blocks ----------------------------
-  {
-    constexpr int IT = (CELLS + NT - 1) / NT;
-    for (int base = 0; base < CELLS; base += IT * (int)blockDim.x) {
-      float2 v[IT];
-#pragma unroll
-      for (int u = 0; u < IT; ++u) {
-        const int e = base + t + u * (int)blockDim.x;
-        const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
-        v[u] = make_float2(0.f, 1.f);
-        if (e < CELLS && il < vx && jj < vy && kk < vz) {
-          const size_t c = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
-          v[u] = make_float2(gq[c], gsig[c]);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < IT; ++u) {
-        const int e = base + t + u * (int)blockDim.x;
-        if (e < CELLS) cell[e] = v[u];
-      }
-    }
-  }
-  // x coefficients: read along x (coalesced), stored cell-major so that a
-  // lane's two ordinates are adjacent
-  for (int e = t; e < kGroup * TX; e += blockDim.x) {
-    const int nn = e / TX, il = e % TX;
-    hxs[il * kGroup + nn] = (nn < gs && il < vx) ? fM(HS, A.cx[(size_t)(ob + nn) * nx + phys_i(il)]) : 0.f;
-  }
-  for (int e = t; e < kGroup; e += blockDim.x) wts[e] = e < gs ? (float)A.wgt[ob + e] : 0.f;
-  if (DIMS == 2 && TW)
-    for (int e = t; e < TX; e += blockDim.x) rlx[e] = e < vx ? __frcp_rn(A.wx[phys_i(e)]) : 0.f;
-  // per-thread constants of the pencil, per ordinate of the pair
-  const int jc = phys_j(min(jl, vy - 1));
-  const f2 cy2 = pk(fM(HS, A.cy[(size_t)orda * ny + jc]), fM(HS, A.cy[(size_t)ordb * ny + jc]));
-  f2 cz2 = dup(0.f);
-  if constexpr (DIMS == 3) {
-    const int kc = phys_k(min(kl, vz - 1));
-    cz2 = pk(fM(HS, A.cz[(size_t)orda * nz + kc]), fM(HS, A.cz[(size_t)ordb * nz + kc]));
-  }
-  const f2 cyz2 = add2(cy2, cz2);
-  const f2 h2y = add2(cy2, cy2), h2z = add2(cz2, cz2);
-  const float thf = (float)A.theta;
-  const f2 th2 = dup(thf), om2 = dup(fS(1.0f, thf));
-  f2 txy2 = dup(0.f);
-  if constexpr (DIMS == 2 && TW) {
-    const float ry_ = __frcp_rn(A.wy[jc]);
-    txy2 = pk(fM(fM(thf, A.axi_f[orda]), ry_), fM(fM(thf, A.axi_f[ordb]), ry_));
-  }
-
-  if (dataflow) wait_upstream<float, DIMS>(A, task, slot, epoch);
-
-  // -- incoming faces: every load issued before the first store ----------------------
-  {
-    constexpr int Y4 = SM::YF / 4, R4 = TX * kGroup / 4;
-    f2 xin2 = dup(0.f);
-    const size_t xslot = F.x(k0 + kl, j0 + jl) + na;
-    if (active && task.bi > 0) xin2 = pk(__ldcg(reinterpret_cast<const float2 *>(A.xf + xslot)));
-    stage_f4<Y4, NT>(reinterpret_cast<float4 *>(yin), [&](int e) {
-      const int kk = e / R4, r = e % R4;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (task.bj > 0 && kk < vz && r / (kGroup / 4) < vx)
-        v = __ldcg(reinterpret_cast<const float4 *>(A.yf + F.y(k0 + kk, i0)) + r);
-      return v;
-    });
-    if constexpr (DIMS == 3)
-      stage_f4<SM::ZF / 4, NT>(reinterpret_cast<float4 *>(zin), [&](int e) {
-        const int jj = e / R4, r = e % R4;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (task.bk > 0 && jj < vy && r / (kGroup / 4) < vx)
-          v = __ldcg(reinterpret_cast<const float4 *>(A.zf + F.z(j0 + jj, i0)) + r);
-        return v;
-      });
-    __syncthreads();
-
-    // -- wavefront: step s solves the cells with il + jl + kl == s ---------------------
-    const int d = jl + kl;
-    const int ebase = (kl * PY + jl) * TX;
-    const float * yin_l = yin + (kl * TX - d) * kGroup + na;
-    const float * zin_l = zin + (jl * TX - d) * kGroup + na;
-    const float2 * cell_l = cell + (ebase - d);
-    const float * hx_l = hxs - d * kGroup + na;
-    const float * rlx_l = rlx - d;
-    const bool ybound = active && jl == vy - 1;
-    const bool zbound = DIMS == 3 && active && kl == vz - 1;
-    float * yout_g = A.yf + F.y(k0 + kl, i0) + na;
-    float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + na : nullptr;
-    float * P_lane = P + pr * CELLS + ebase;
-    const f2 w2 = pk(wts[min(na, kGroup - 1)], wts[min(na + 1, kGroup - 1)]);
-    f2 x2 = xin2, ysh2 = dup(0.f), zsh2 = dup(0.f);
-    constexpr int STEPS = TX + PY + PZ - 2;
-    // a warp whose two pairs both lie past the group's last ordinate has
-    // nothing to solve (the CTA is sized for the largest group of a launch)
-    const bool warp_busy = 4 * (t >> 5) < gs;
-    if (warp_busy) {
-#pragma unroll (DIMS == 3 ? STEPS : 4)
-    for (int s = 0; s < STEPS; ++s) {
-      const int il = s - d;
-      const bool valid = active && (unsigned)il < (unsigned)vx;
-      const f2 yl = *reinterpret_cast<const f2 *>(yin_l + s * kGroup);
-      f2 y2 = jl == 0 ? yl : ysh2;
-      f2 z2 = dup(0.f);
-      if constexpr (DIMS == 3) {
-        const f2 zl = *reinterpret_cast<const f2 *>(zin_l + s * kGroup);
-        z2 = kl == 0 ? zl : zsh2;
-      }
-      const float2 qc = cell_l[s];
-      const f2 q2 = dup(qc.x), st2 = dup(qc.y);
-      const f2 hx2 = *reinterpret_cast<const f2 *>(hx_l + s * kGroup);
-      f2 xo2 = x2, psi2;
-      if constexpr (DIMS == 3) {
-        if constexpr (TW) psi2 = twdd3_fast2(q2, st2, hx2, cy2, cz2, h2y, h2z, th2, om2, xo2, y2, z2);
-        else psi2 = dd3_fast2(q2, st2, hx2, cy2, cz2, cyz2, xo2, y2, z2);
-      } else {
-        if constexpr (TW) psi2 = twdd2_fast2(q2, st2, hx2, cy2, mul2(txy2, dup(rlx_l[s])), th2, om2, xo2, y2);
-        else psi2 = dd2_fast2(q2, st2, hx2, cy2, xo2, y2);
-      }
-      x2 = sel2(valid, xo2, x2);
-      st_global2_if(yout_g + il * kGroup, y2, valid && ybound);
-      if constexpr (DIMS == 3) st_global2_if(zout_g + il * kGroup, z2, valid && zbound);
-      // the pair's w psi sum, as the scalar body forms it: fA(w_a psi_a, w_b psi_b)
-      const float2 wp = upk(mul2(w2, psi2));
-      st_shared_if(P_lane + il, fA(wp.x, second ? wp.y : 0.f), valid);
-      const float2 yv = upk(y2);
-      ysh2 = pk(__shfl_up_sync(FULL, yv.x, 1), __shfl_up_sync(FULL, yv.y, 1));
-      if constexpr (DIMS == 3) {
-        const float2 zv = upk(z2);
-        zsh2 = pk(__shfl_up_sync(FULL, zv.x, PY), __shfl_up_sync(FULL, zv.y, PY));
-      }
-    }
-    }
-    if (active) *reinterpret_cast<float2 *>(A.xf + xslot) = upk(x2);
-  }
-  __syncthreads();
-
-  if (dataflow && t == 0) st_release(done_flag(A, slot, task.bk, task.bj, task.bi), epoch);
-
-  // -- the slot's scalar-flux partial: Kahan over the ordinate pairs, fixed order -------
-  for (int e = t; e < CELLS; e += blockDim.x) {
-    const int il = e % TX, r = e / TX, jj = r % PY, kk = r / PY;
-    if (il < vx && jj < vy && kk < vz) {
-      float sum = 0.0f, comp = 0.0f;
-      const int npairs = (gs + 1) >> 1;
-      for (int nn = 0; nn < npairs; ++nn) {
-        const float v = P[nn * CELLS + e];
-        const float yv = fS(v, comp);
-        const float tv = fA(sum, yv);
-        comp = fS(fS(tv, sum), yv);
-        sum = tv;
-      }
-      const size_t cg = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
-      A.octphi[slot * N + cg] = (double)sum - (double)comp;
-    }
-  }
-}
-
-// PACKED selects the f32x2 body for single precision (the persistent and
-// batched kernels); the level-synchronous kernel keeps the scalar body, so the
-// two schedules cross-check the packed arithmetic bit for bit.
-template <typename T, int DIMS, int SCHEME, int TX, bool PACKED>
+template <typename T, int DIMS, int SCHEME, int TX>
 __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task,
                                          unsigned char * smem_raw, bool dataflow, unsigned epoch)
 {
   if constexpr (std::is_same<T, double>::value)
     run_task_exact<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
-  else if constexpr (PACKED)
-    run_task_f32p<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
   else
     run_task_f32<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
 }
 
-template <typename T, bool PACKED>
-constexpr int sweep_max_threads()
-{
-  return std::is_same<T, float>::value && PACKED ? kMaxSweepThreadsF32 : kMaxSweepThreads;
-}
-
 // Resident CTAs per SM the kernels are compiled for (caps the registers of
-// the single-precision bodies, whose unrolled wavefronts would otherwise take
-// every register they can).  Scalar body, measured on GB300 (64^3, 16
-// ordinates per octant): DD is fastest with 4 CTAs per SM (64 registers),
-// TW-DD, with more live values per cell, with 3 (80 registers).  The packed
-// body has half the threads per CTA and about twice the live values per
-// thread.
-template <typename T, int SCHEME, bool PACKED>
+// the single-precision body, whose unrolled wavefront would otherwise take
+// every register it can).  Measured on GB300 (64^3, 16 ordinates per
+// octant): DD is fastest with 4 CTAs per SM (64 registers), TW-DD, with more
+// live values per cell, with 3 (80 registers).
+template <typename T, int SCHEME>
 constexpr int sweep_min_ctas()
 {
-  if constexpr (std::is_same<T, double>::value) return 1;
-  else if constexpr (PACKED) return SCHEME == DOMA_SCHEME_DD ? DOMA_SWEEP_MIN_CTAS_PACKED_DD
-                                                            : DOMA_SWEEP_MIN_CTAS_PACKED_TW;
-  else return SCHEME == DOMA_SCHEME_DD ? 4 : DOMA_SWEEP_MIN_CTAS;
+  return std::is_same<T, double>::value ? 1 : SCHEME == DOMA_SCHEME_DD ? 4 : DOMA_SWEEP_MIN_CTAS;
 }
 
-// Shared memory of a task: for single precision the larger of the packed and
-// scalar layouts, so one size serves every kernel of a schedule.
 template <typename T, int DIMS, int TX>
 constexpr size_t task_smem_bytes()
 {
   if constexpr (std::is_same<T, double>::value) return TaskSmemExact<DIMS, TX>::bytes;
-  else return TaskSmemF32<DIMS, TX>::bytes > TaskSmemF32P<DIMS, TX>::bytes
-                  ? TaskSmemF32<DIMS, TX>::bytes : TaskSmemF32P<DIMS, TX>::bytes;
+  else return TaskSmemF32<DIMS, TX>::bytes;
 }
 
 // Persistent dataflow sweep: CTAs claim tasks in topological order from a
 // ticket counter; a claimed task waits only on tasks with smaller tickets,
 // which running CTAs already hold, so progress never depends on residency.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(sweep_max_threads<T, true>(), sweep_min_ctas<T, SCHEME, true>())
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
     sweep_persistent_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1293,7 +889,7 @@ __global__ void __launch_bounds__(sweep_max_threads<T, true>(), sweep_min_ctas<T
     // claim the following ticket now: its round trip overlaps this task (the
     // task's internal barriers order the write before the next read)
     if (threadIdx.x == claimer) s_next = atomicAdd(A.ticket, 1u);
-    run_task<T, DIMS, SCHEME, TX, true>(A, A.tasks[tk], smem_raw, true, epoch);
+    run_task<T, DIMS, SCHEME, TX>(A, A.tasks[tk], smem_raw, true, epoch);
   }
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1311,7 +907,7 @@ __global__ void __launch_bounds__(sweep_max_threads<T, true>(), sweep_min_ctas<T
 // every problem of a batch.  Tasks of problems that have converged publish
 // their done flag and return, so a batch keeps one static task list.
 template <typename T, int DIMS, int SCHEME>
-__global__ void __launch_bounds__(sweep_max_threads<T, true>(), sweep_min_ctas<T, SCHEME, true>())
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
     sweep_batch_kernel(const SweepArgs<T> * args, const BatchTask * tasks, int num_tasks,
                        unsigned * ticket, unsigned * exit_count, unsigned * epoch_ctr,
                        const BatchLoop * loops)
@@ -1340,9 +936,9 @@ __global__ void __launch_bounds__(sweep_max_threads<T, true>(), sweep_min_ctas<T
       continue;
     }
     // each problem has its own block length (uniform across the CTA)
-    if (A.tx <= 8) run_task<T, DIMS, SCHEME, 8, true>(A, bt.t, smem_raw, true, epoch);
-    else if (A.tx <= 16) run_task<T, DIMS, SCHEME, 16, true>(A, bt.t, smem_raw, true, epoch);
-    else run_task<T, DIMS, SCHEME, 32, true>(A, bt.t, smem_raw, true, epoch);
+    if (A.tx <= 8) run_task<T, DIMS, SCHEME, 8>(A, bt.t, smem_raw, true, epoch);
+    else if (A.tx <= 16) run_task<T, DIMS, SCHEME, 16>(A, bt.t, smem_raw, true, epoch);
+    else run_task<T, DIMS, SCHEME, 32>(A, bt.t, smem_raw, true, epoch);
   }
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1357,11 +953,11 @@ __global__ void __launch_bounds__(sweep_max_threads<T, true>(), sweep_min_ctas<T
 
 // One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(sweep_max_threads<T, false>(), sweep_min_ctas<T, SCHEME, false>())
+__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
     sweep_level_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  run_task<T, DIMS, SCHEME, TX, false>(A, A.tasks[A.task_offset + blockIdx.x], smem_raw, false, 0u);
+  run_task<T, DIMS, SCHEME, TX>(A, A.tasks[A.task_offset + blockIdx.x], smem_raw, false, 0u);
 }
 
 template <typename T, int DIMS, int SCHEME, int TX>
@@ -1374,14 +970,11 @@ doma_status launch_impl(const Schedule & s, const SweepArgs<T> & args, cudaStrea
   } else {
     SweepArgs<T> a = args;
     const int levels = (int)s.level_begin.size() - 1;
-    // the level kernel runs the scalar body in single precision
-    const int threads = std::is_same<T, float>::value ? sweep_threads(DOMA_PREC_FP32, s.gs, false)
-                                                      : s.threads;
     for (int L = 0; L < levels; ++L) {
       const int count = s.level_begin[L + 1] - s.level_begin[L];
       if (count == 0) continue;
       a.task_offset = s.level_begin[L];
-      sweep_level_kernel<T, DIMS, SCHEME, TX><<<count, threads, s.smem, stream>>>(a);
+      sweep_level_kernel<T, DIMS, SCHEME, TX><<<count, s.threads, s.smem, stream>>>(a);
       if (launches) ++*launches;
     }
   }
@@ -1421,10 +1014,9 @@ auto dispatch(int dims, int precision, int scheme, int tx, F && f)
 
 }  // namespace
 
-int sweep_threads(int precision, int gs, bool packed)
+int sweep_threads(int gs)
 {
-  const int per = precision == DOMA_PREC_FP32 && packed ? (gs + 1) / 2 : gs;
-  return ((16 * per + 31) / 32) * 32;
+  return ((16 * gs + 31) / 32) * 32;
 }
 
 int sweep_tile_x(int requested)
@@ -1486,6 +1078,7 @@ auto dispatch_batch(int dims, int scheme, F && f)
 
 size_t sweep_batch_smem_bytes(int dims)
 {
+  // the largest block length's layout serves all three
   return dims == 2 ? task_smem_bytes<float, 2, 32>() : task_smem_bytes<float, 3, 32>();
 }
 

@@ -181,13 +181,11 @@ def test_persistent_and_level_schedules_agree(monkeypatch, precision, dims):
 @pytest.mark.parametrize("np_,na", [(2, 3), (3, 3), (5, 5)])
 @pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
 @pytest.mark.parametrize("dims", [2, 3])
-def test_packed_and_scalar_sweep_bodies_agree(monkeypatch, tile, np_, na, scheme, dims):
-    """In single precision the dataflow sweep runs the packed body (two
-    ordinates per lane in f32x2 instructions) and the one-launch-per-level
-    sweep the scalar body (one ordinate per lane).  Per-element rounding is
-    the same, so whole solves must agree bit for bit: with an odd ordinate
-    count (the last pair half empty) and with more ordinates per octant than
-    one task holds (25 = 16 + 9)."""
+def test_schedules_agree_across_shapes(monkeypatch, tile, np_, na, scheme, dims):
+    """The dataflow sweep and the one-launch-per-level sweep give the same
+    bits in single precision for every block length and scheme, with an odd
+    number of ordinates per octant (the last warp half used) and with more
+    ordinates per octant than one task holds (25 = 16 + 9)."""
     p = P.random_problem(43, dims, 21, 13, 6, groups=2, np_=np_, na=na, materials=3)
     opts = P.make_options(scheme=scheme, theta=0.8, precision="fp32", fs_tol=1e-6, mg_tol=1e-6,
                           tile=(tile, 0, 0))
