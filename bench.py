@@ -734,11 +734,13 @@ def profile_main(argv) -> None:
                     help="host: host-driven solve loop (kernels profilable one by one)")
     ap.add_argument("--iteration", choices=["gauss_seidel", "multigroup"], default="gauss_seidel")
     ap.add_argument("--unet-forward", type=int, default=0)
+    ap.add_argument("--unet-backward", type=int, default=0,
+                    help="K training steps (forward, loss, backward, Adam) of the U-Net")
     ap.add_argument("--batch", type=int, default=1)
     ap.add_argument("--streaming", action="store_true",
                     help="the 100^3 duct problem (one group, 12 x 24 directions, DD)")
     a = ap.parse_args(argv)
-    if a.unet_forward > 0:
+    if a.unet_forward > 0 or a.unet_backward > 0:
         profile_unet_forward(a)
         return
     if a.schedule == "levels":
@@ -778,6 +780,10 @@ def profile_main(argv) -> None:
 
 
 def profile_unet_forward(a) -> None:
+    """K forward passes (--unet-forward K) or K training steps (--unet-backward
+    K: forward, mean-square loss against a random target, backward, Adam) of
+    the U-Net with the committed weights on an n^3 volume of --batch samples;
+    prints the CUDA-event time per pass or step."""
     import torch
 
     from doma_gb300.learned.net import UNet
@@ -790,17 +796,22 @@ def profile_unet_forward(a) -> None:
         g = torch.Generator(device="cuda").manual_seed(0)
         x = torch.randn((a.batch, a.n, a.n, a.n, 16), generator=g, device="cuda").to(torch.bfloat16)
         y = torch.empty((a.batch, a.n, a.n, a.n), dtype=torch.float32, device="cuda")
+        t = torch.randn((a.batch, a.n, a.n, a.n), generator=g, device="cuda")
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        count = a.unet_backward if a.unet_backward > 0 else a.unet_forward
         torch.cuda.synchronize()
         e0.record()
-        for _ in range(a.unet_forward):
-            net.forward(x, y)
+        for _ in range(count):
+            if a.unet_backward > 0:
+                net.backward(x, t)
+                net.adam(1e-6)
+            else:
+                net.forward(x, y)
         e1.record()
         torch.cuda.synchronize()
-        print(json.dumps({"workload": f"unet_forward_{a.n}cube_batch{a.batch}",
-                          "forwards": a.unet_forward,
-                          "ms_per_forward": e0.elapsed_time(e1) / a.unet_forward}))
-
+        kind = "training_step" if a.unet_backward > 0 else "forward"
+        print(json.dumps({"workload": f"unet_{kind}_{a.n}cube_batch{a.batch}", "count": count,
+                          f"ms_per_{kind}": e0.elapsed_time(e1) / count}))
 
 
 def main():

@@ -220,6 +220,10 @@ SIGNATURES = {
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 4,
     ),
+    "doma_unet_backward_weighted": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 4,
+    ),
     "doma_unet_last_loss": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "doma_unet_adam": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_float] * 4),
     "doma_conv3_forward": (

@@ -550,9 +550,12 @@ __global__ void head_forward_kernel(long long voxels, int c, const bf16 * x, con
 }
 
 // Head backward and loss: per block, double partials [c dw, db, loss].
+// With sample weights, voxel m belongs to sample m / per_sample and its term
+// of the loss (and of every gradient) is scaled by that sample's weight.
 __global__ void head_backward_kernel(long long voxels, int c, const bf16 * x, const float * w,
                                      const float * out, const float * target, bf16 * dx,
-                                     double * partial)
+                                     double * partial, const float * sample_weight,
+                                     long long per_sample)
 {
   extern __shared__ double dsh[];  // [blockDim][c + 2]
   const int W = c + 2;
@@ -562,7 +565,8 @@ __global__ void head_backward_kernel(long long voxels, int c, const bf16 * x, co
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < voxels;
        m += (long long)gridDim.x * blockDim.x) {
     const double r = (double)out[m] - (double)target[m];
-    const float gs = (float)(2.0 * r * inv);
+    const double sw = sample_weight ? (double)sample_weight[m / per_sample] : 1.0;
+    const float gs = (float)(2.0 * sw * r * inv);
     for (int k = 0; k < c; k += 8) {
       const Vec8 xv = load8(x + m * c + k);
       Vec8 d;
@@ -574,7 +578,7 @@ __global__ void head_backward_kernel(long long voxels, int c, const bf16 * x, co
       store8(dx + m * c + k, d);
     }
     acc[c] += gs;
-    acc[c + 1] += r * r;
+    acc[c + 1] += sw * r * r;
   }
   for (int k = 0; k < W; ++k) dsh[threadIdx.x * W + k] = acc[k];
   __syncthreads();
@@ -828,7 +832,8 @@ size_t head_backward_scratch(int c) { return (size_t)kReduceBlocks * (c + 2); }
 
 doma_status head_backward(size_t voxels, int c, const bf16 * x, const float * w, const float * out,
                           const float * target, bf16 * dx, float * dw, float * db,
-                          double * partial, double * loss, cudaStream_t st)
+                          double * partial, double * loss, cudaStream_t st,
+                          const float * sample_weight, size_t per_sample)
 {
   if (c > 32 || c % 8) {
     set_error("head_backward: the head takes at most 32 channels");
@@ -836,7 +841,8 @@ doma_status head_backward(size_t voxels, int c, const bf16 * x, const float * w,
   }
   const int threads = 128;
   head_backward_kernel<<<kReduceBlocks, threads, threads * (c + 2) * sizeof(double), st>>>(
-      (long long)voxels, c, x, w, out, target, dx, partial);
+      (long long)voxels, c, x, w, out, target, dx, partial, sample_weight,
+      (long long)std::max<size_t>(per_sample, 1));
   DOMA_CUDA_TRY(cudaGetLastError());
   head_finish_kernel<<<1, 64, 0, st>>>(partial, kReduceBlocks, c, (long long)voxels, dw, db, loss);
   DOMA_CUDA_TRY(cudaGetLastError());

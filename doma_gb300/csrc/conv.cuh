@@ -87,11 +87,14 @@ doma_status head_forward(size_t voxels, int c, const __nv_bfloat16 * x, const fl
 //   r = out - target; loss = sum r^2 / voxels (double, in *loss)
 //   dx[m][c] = (2 r[m] / voxels) w[c] * (x[m][c] > 0)   (x is the head input, a relu output)
 //   dw[c] = sum_m (2 r / voxels) x[m][c], db = sum_m 2 r / voxels
-// partial: scratch of head_backward_scratch(c) doubles.
+// partial: scratch of head_backward_scratch(c) doubles.  With sample_weight
+// (device, one per sample of per_sample voxels) every voxel's r is weighted by
+// its sample's weight: loss = sum w r^2 / voxels and the gradients follow.
 size_t head_backward_scratch(int c);
 doma_status head_backward(size_t voxels, int c, const __nv_bfloat16 * x, const float * w,
                           const float * out, const float * target, __nv_bfloat16 * dx, float * dw,
-                          float * db, double * partial, double * loss, cudaStream_t st);
+                          float * db, double * partial, double * loss, cudaStream_t st,
+                          const float * sample_weight = nullptr, size_t per_sample = 1);
 // FP32 master weights -> bf16 forward (w) and mirrored/transposed (wt) copies.
 doma_status publish_weights(const float * w32, int cin, int cout, __nv_bfloat16 * w,
                             __nv_bfloat16 * wt, cudaStream_t st);

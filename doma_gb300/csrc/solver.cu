@@ -2258,12 +2258,11 @@ doma_status doma_batch_set_stream(doma_batch * b, void * stream)
 // The batch's autotuner: a block length per class of problems.  A class is
 // (16-cell bucket of the longest mesh axis, ordinates per octant, groups).
 // For each length in {8, 16, 32} every solver is rescheduled to it and the
-// batched sweep is timed with all problems active (the uniform choice) and
-// with each class alone active (the others' tasks only publish their flags);
-// each class takes its fastest length.  The mixed assignment is then timed
-// against the best uniform length and kept only if it is faster.  The
-// results do not depend on the choice (every block length gives the same
-// bits).
+// batched sweep is timed over all problems (the uniform choice) and over each
+// class alone (a task list of that class's problems only); each class takes
+// its fastest length.  The mixed assignment is then timed against the best
+// uniform length and kept only if it is faster.  The results do not depend
+// on the choice (every block length gives the same bits).
 doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
 {
   if (!b) return bad("null batch");
@@ -2280,22 +2279,19 @@ doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
   cudaEvent_t e0, e1;
   DOMA_CUDA_TRY(cudaEventCreate(&e0));
   DOMA_CUDA_TRY(cudaEventCreate(&e1));
-  auto time_sweeps = [&](float * ms) -> doma_status {
-    DOMA_TRY(batch_sweep(b));  // warm-up
+  // one warm-up sweep, then two timed
+  auto time_list = [&](const BatchTask * tasks, int count, int grid, float * ms) -> doma_status {
+    auto one = [&]() {
+      return launch_sweep_batch(b->dims, b->opts.scheme, grid, b->threads, b->smem, b->d_args, tasks,
+                                count, &b->d_ctl->ticket, &b->d_ctl->exit_count, &b->d_ctl->epoch,
+                                b->d_loops, b->stream);
+    };
+    DOMA_TRY(one());
     DOMA_CUDA_TRY(cudaEventRecord(e0, b->stream));
-    for (int k = 0; k < 2; ++k) DOMA_TRY(batch_sweep(b));
+    for (int k = 0; k < 2; ++k) DOMA_TRY(one());
     DOMA_CUDA_TRY(cudaEventRecord(e1, b->stream));
     DOMA_CUDA_TRY(cudaEventSynchronize(e1));
     DOMA_CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
-    return DOMA_OK;
-  };
-  std::vector<BatchLoop> loops(P);
-  auto set_active = [&](const std::vector<size_t> * only) -> doma_status {
-    for (size_t p = 0; p < P; ++p) loops[p] = BatchLoop{only ? 0u : 1u, 0u, 0u, 0u, 0.0};
-    if (only)
-      for (size_t p : *only) loops[p].active = 1u;
-    DOMA_CUDA_TRY(cudaMemcpyAsync(b->d_loops, loops.data(), P * sizeof(BatchLoop),
-                                  cudaMemcpyHostToDevice, b->stream));
     return DOMA_OK;
   };
   auto apply = [&](const std::vector<int> & per_problem) -> doma_status {
@@ -2303,17 +2299,37 @@ doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
     DOMA_TRY(build_batch_schedule(b));
     return batch_init_sources(b);
   };
+  // a class's own tasks, merged level by level as build_batch_schedule merges them
+  BatchTask * d_class_tasks = nullptr;
+  std::vector<BatchTask> tasks;
+  const int fit = sweep_batch_resident_ctas(b->dims, b->opts.scheme, b->threads, b->smem);
+  if (fit <= 0) return bad("the batched sweep block does not fit on this device");
   for (int k = 0; k < 3; ++k) {
     DOMA_TRY(apply(std::vector<int>(P, txs[k])));
-    DOMA_TRY(set_active(nullptr));
-    DOMA_TRY(time_sweeps(&uniform_ms[k]));
+    DOMA_TRY(time_list(b->d_tasks, b->num_tasks, b->grid, &uniform_ms[k]));
+    if (!d_class_tasks) DOMA_TRY(balloc(b, &d_class_tasks, (size_t)b->num_tasks * 4));
     size_t c = 0;
     for (auto & kv : classes) {
-      DOMA_TRY(set_active(&kv.second));
-      DOMA_TRY(time_sweeps(&class_ms[c][k]));
+      tasks.clear();
+      int levels = 0;
+      for (size_t p : kv.second)
+        levels = std::max(levels, (int)b->solvers[p]->sched.level_begin.size() - 1);
+      for (int L = 0; L < levels; ++L)
+        for (size_t p : kv.second) {
+          const Schedule & sc = b->solvers[p]->sched;
+          if (L + 1 >= (int)sc.level_begin.size()) continue;
+          for (int t = sc.level_begin[L]; t < sc.level_begin[L + 1]; ++t)
+            tasks.push_back(BatchTask{sc.tasks[t], (int)p});
+        }
+      DOMA_CUDA_TRY(cudaMemcpyAsync(d_class_tasks, tasks.data(), tasks.size() * sizeof(BatchTask),
+                                    cudaMemcpyHostToDevice, b->stream));
+      DOMA_TRY(time_list(d_class_tasks, (int)tasks.size(), std::min(fit, (int)tasks.size()),
+                         &class_ms[c][k]));
       ++c;
     }
   }
+  DOMA_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  bfree(b, d_class_tasks);
   int best_uniform = 0;
   for (int k = 1; k < 3; ++k)
     if (uniform_ms[k] < uniform_ms[best_uniform]) best_uniform = k;
@@ -2329,9 +2345,8 @@ doma_status doma_batch_tune(doma_batch * b, uint32_t * tile_x)
     }
   }
   DOMA_TRY(apply(mixed));
-  DOMA_TRY(set_active(nullptr));
   float mixed_ms = 0.f;
-  DOMA_TRY(time_sweeps(&mixed_ms));
+  DOMA_TRY(time_list(b->d_tasks, b->num_tasks, b->grid, &mixed_ms));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (!(mixed_ms < uniform_ms[best_uniform])) {

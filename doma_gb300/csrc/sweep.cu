@@ -609,7 +609,7 @@ __device__ __forceinline__ void stage_f4(float4 * dst, L load)
   }
 }
 
-template <int DIMS, int SCHEME, int TX>
+template <int DIMS, int SCHEME, int TX, bool SKIP_IDLE = false>
 __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const Task task,
                                              unsigned char * smem_raw, bool dataflow, unsigned epoch)
 {
@@ -760,11 +760,13 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const float wgt = PAIRS ? wts[min(nl, kGroup - 1)] : 0.f;
     float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
-    // A warp whose two ordinates both lie past the group's last one has
-    // nothing to solve: it skips the walk (warp-uniform).  The batched launch
-    // sizes every CTA for a full group, so a problem with 4 or 9 ordinates
-    // per octant would otherwise spend 6 or 3 idle warps' issue slots here.
-    const bool warp_busy = 2 * (t >> 5) < gs;
+    // SKIP_IDLE (the batched kernel): a warp whose two ordinates both lie
+    // past the group's last one has nothing to solve and skips the walk
+    // (warp-uniform).  The batched launch sizes every CTA for a full group, so
+    // a problem with 4 or 9 ordinates per octant would otherwise spend 6 or 3
+    // idle warps' issue slots here.  A single problem's CTAs are sized to its
+    // group, and its kernel keeps the branch-free walk.
+    const bool warp_busy = !SKIP_IDLE || 2 * (t >> 5) < gs;
     // 3D: fully unrolled; 2D (long skew) partly, which keeps it out of local memory
     if (warp_busy)
 #pragma unroll (DIMS == 3 ? STEPS : 4)
@@ -841,14 +843,14 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   }
 }
 
-template <typename T, int DIMS, int SCHEME, int TX>
+template <typename T, int DIMS, int SCHEME, int TX, bool SKIP_IDLE = false>
 __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task,
                                          unsigned char * smem_raw, bool dataflow, unsigned epoch)
 {
   if constexpr (std::is_same<T, double>::value)
     run_task_exact<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
   else
-    run_task_f32<DIMS, SCHEME, TX>(A, task, smem_raw, dataflow, epoch);
+    run_task_f32<DIMS, SCHEME, TX, SKIP_IDLE>(A, task, smem_raw, dataflow, epoch);
 }
 
 // Resident CTAs per SM the kernels are compiled for (caps the registers of
@@ -936,9 +938,9 @@ __global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
       continue;
     }
     // each problem has its own block length (uniform across the CTA)
-    if (A.tx <= 8) run_task<T, DIMS, SCHEME, 8>(A, bt.t, smem_raw, true, epoch);
-    else if (A.tx <= 16) run_task<T, DIMS, SCHEME, 16>(A, bt.t, smem_raw, true, epoch);
-    else run_task<T, DIMS, SCHEME, 32>(A, bt.t, smem_raw, true, epoch);
+    if (A.tx <= 8) run_task<T, DIMS, SCHEME, 8, true>(A, bt.t, smem_raw, true, epoch);
+    else if (A.tx <= 16) run_task<T, DIMS, SCHEME, 16, true>(A, bt.t, smem_raw, true, epoch);
+    else run_task<T, DIMS, SCHEME, 32, true>(A, bt.t, smem_raw, true, epoch);
   }
   if (threadIdx.x == 0) {
     __threadfence();

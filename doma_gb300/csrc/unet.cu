@@ -187,12 +187,13 @@ doma_status forward_impl(doma_unet * n, const bf16 * x, cudaStream_t st)
                       n->params + n->head_b_off, w.out, st);
 }
 
-doma_status backward_impl(doma_unet * n, const bf16 * x, const float * target, cudaStream_t st)
+doma_status backward_impl(doma_unet * n, const bf16 * x, const float * target, cudaStream_t st,
+                          const float * sample_weight = nullptr)
 {
   UnetWork & w = n->work;
   DOMA_TRY(head_backward(w.voxels[0], kUnetBase, w.d0, n->params + n->head_w_off, w.out, target,
                          w.gA[0], n->grads + n->head_w_off, n->grads + n->head_b_off, w.hpartial,
-                         n->d_loss, st));
+                         n->d_loss, st, sample_weight, w.voxels[0] / (size_t)std::max(n->batch, 1)));
   // decoder levels 0, 1, 2: gA[l] holds the gradient of d_l's pre-activation
   for (int l = 0; l <= 2; ++l) {
     const int up = 8 + 2 * (2 - l), dec = up + 1;
@@ -403,6 +404,18 @@ doma_status doma_unet_backward(doma_unet * n, const void * input, const float * 
   const bf16 * x = static_cast<const bf16 *>(input);
   DOMA_TRY(forward_impl(n, x, n->stream));
   return backward_impl(n, x, target, n->stream);
+}
+
+doma_status doma_unet_backward_weighted(doma_unet * n, const void * input, const float * target,
+                                        const float * sample_weight, uint32_t batch, uint32_t nz,
+                                        uint32_t ny, uint32_t nx)
+{
+  if (!n || !input || !target || !sample_weight) return bad_net("null network or buffer");
+  DOMA_TRY(check_shape((int)batch, (int)nz, (int)ny, (int)nx));
+  DOMA_TRY(ensure_work(n, (int)batch, (int)nz, (int)ny, (int)nx));
+  const bf16 * x = static_cast<const bf16 *>(input);
+  DOMA_TRY(forward_impl(n, x, n->stream));
+  return backward_impl(n, x, target, n->stream, sample_weight);
 }
 
 doma_status doma_unet_last_loss(doma_unet * n, double * loss)

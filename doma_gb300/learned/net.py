@@ -76,11 +76,19 @@ class UNet:
                                              ctypes.c_void_p(out.data_ptr()), b, z, y, w),
                   "doma_unet_forward", self.lib)
 
-    def backward(self, x, target) -> None:
+    def backward(self, x, target, weight=None) -> None:
+        """Forward, mean-square loss and gradients; weight: optional [B] float32
+        cuda tensor scaling each sample's squared error."""
         b, z, y, w = self._shape(x)
-        abi.check(self.lib.doma_unet_backward(self._h, ctypes.c_void_p(x.data_ptr()),
-                                              ctypes.c_void_p(target.data_ptr()), b, z, y, w),
-                  "doma_unet_backward", self.lib)
+        if weight is None:
+            abi.check(self.lib.doma_unet_backward(self._h, ctypes.c_void_p(x.data_ptr()),
+                                                  ctypes.c_void_p(target.data_ptr()), b, z, y, w),
+                      "doma_unet_backward", self.lib)
+            return
+        weight = weight.contiguous()
+        abi.check(self.lib.doma_unet_backward_weighted(
+            self._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(target.data_ptr()),
+            ctypes.c_void_p(weight.data_ptr()), b, z, y, w), "doma_unet_backward_weighted", self.lib)
 
     def loss(self) -> float:
         v = ctypes.c_double()

@@ -47,10 +47,22 @@ def make_batch(ps: D.PairSet, gen: torch.Generator, batch: int):
     return x, t
 
 
+def sample_weights(t: torch.Tensor) -> torch.Tensor:
+    """Per-sample loss weights that make each sample's squared error relative
+    to its target's mean square (plus 1, so near-zero targets stay bounded),
+    normalized to mean 1 over the batch."""
+    w = 1.0 / (t.pow(2).flatten(1).mean(dim=1) + 1.0)
+    return (w / w.mean()).float().contiguous()
+
+
 def train(ps: D.PairSet, steps: int = 4000, batch: int = 16, lr: float = 1e-3,
-          seed: int = 0, log_every: int = 200, log=print, init=None) -> tuple[UNet, list]:
+          seed: int = 0, log_every: int = 200, log=print, init=None,
+          weighted: bool = False) -> tuple[UNet, list]:
     """Adam with a short warm-up and cosine decay; `init` (a weights file)
-    starts from trained weights instead of the seeded initialisation."""
+    starts from trained weights instead of the seeded initialisation.  With
+    `weighted`, every sample's squared error is divided by its target's mean
+    square (sample_weights), so the few very large normalized targets do not
+    dominate the loss."""
     torch.cuda.synchronize()
     net = UNet(seed=seed)
     if init is not None:
@@ -60,7 +72,7 @@ def train(ps: D.PairSet, steps: int = 4000, batch: int = 16, lr: float = 1e-3,
     t0 = time.perf_counter()
     for step in range(1, steps + 1):
         x, t = make_batch(ps, gen, batch)
-        net.backward(x, t)
+        net.backward(x, t, sample_weights(t) if weighted else None)
         # cosine decay to 1% with a short warm-up
         warm = min(1.0, step / 200.0)
         rate = lr * warm * (0.01 + 0.99 * 0.5 * (1.0 + math.cos(math.pi * step / steps)))
@@ -85,6 +97,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--random-rounds", type=int, default=16)
     ap.add_argument("--init", default=None, help="weights file to start from")
+    ap.add_argument("--weighted", action="store_true",
+                    help="relative per-sample loss (each sample's error over its target's size)")
     ap.add_argument("--out", default="accel_weights.npz")
     a = ap.parse_args()
     torch.cuda.set_device(0)
@@ -97,7 +111,8 @@ def main():
         R, Z = D.generate_random([probs[i] for i in ps.kept], rounds=a.random_rounds, seed=a.seed)
         ps = D.PairSet(torch.cat([ps.R, R], dim=1), torch.cat([ps.Z, Z], dim=1), ps.F, ps.n,
                        ps.iterations, ps.seconds, ps.kept)
-    net, _ = train(ps, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed, init=a.init)
+    net, _ = train(ps, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed, init=a.init,
+                   weighted=a.weighted)
     net.save(a.out)
     print(f"weights written to {a.out}")
 

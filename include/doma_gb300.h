@@ -356,6 +356,13 @@ doma_status doma_unet_forward(doma_unet *net, const void *input, float *output, 
  * loss for every parameter (read with doma_unet_get_grads). */
 doma_status doma_unet_backward(doma_unet *net, const void *input, const float *target,
                                uint32_t batch, uint32_t nz, uint32_t ny, uint32_t nx);
+/* The same with a weight per sample (device, batch floats): each sample's
+ * squared error, and so its share of every gradient, is scaled by its
+ * weight; the reported loss is the weighted mean.  Used to train on targets
+ * of very different sizes without the largest dominating. */
+doma_status doma_unet_backward_weighted(doma_unet *net, const void *input, const float *target,
+                                        const float *sample_weight, uint32_t batch, uint32_t nz,
+                                        uint32_t ny, uint32_t nx);
 doma_status doma_unet_last_loss(doma_unet *net, double *loss);
 /* One Adam step (bias-corrected) with the last gradients. */
 doma_status doma_unet_adam(doma_unet *net, float lr, float beta1, float beta2, float eps);
