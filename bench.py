@@ -375,9 +375,10 @@ def roofline_entry(ms: float, updates: float, d_oct: int, s_bytes: int, peak: fl
 
 
 # DRAM traffic of one sweep launch on the 100^3, 288-direction duct problem
-# (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture); None until
-# captured.
-STREAMING_SWEEP_DRAM_BYTES = None
+# (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture).  The
+# 192 MB of double partials (3 ordinate groups x 8 octants x 10^6 cells) no
+# longer fit in L2, so most of it is their write-back.
+STREAMING_SWEEP_DRAM_BYTES = 34_532_864 + 262_337_536
 
 
 def streaming_leg(args, stream, flush):

@@ -233,6 +233,12 @@ SIGNATURES = {
                                                       ctypes.c_void_p, ctypes.c_uint32,
                                                       ctypes.c_void_p],
     ),
+    "doma_conv3_wgrad": (
+        ctypes.c_int,
+        [ctypes.c_void_p] + [ctypes.c_uint32] * 5 + [ctypes.c_void_p, ctypes.c_uint32,
+                                                      ctypes.c_void_p, ctypes.c_uint32,
+                                                      ctypes.c_void_p],
+    ),
     "doma_conv_wait_error": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int)]),
 }
 

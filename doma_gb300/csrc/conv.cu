@@ -735,7 +735,7 @@ size_t conv3_wgrad_scratch(const ConvShape & s, int cin, int cout)
 }
 
 doma_status conv3_wgrad(const ConvShape & s, const bf16 * x, int cin, const bf16 * dz, int cout,
-                        float * partial, float * dw, cudaStream_t st)
+                        float * partial, float * dw, cudaStream_t st, int path)
 {
   if (!valid_channels(cin, true) || !valid_channels(cout, false)) {
     set_error("conv3_wgrad: unsupported channel counts");
@@ -744,6 +744,24 @@ doma_status conv3_wgrad(const ConvShape & s, const bf16 * x, int cin, const bf16
   int bmo, bni, tiles, splits;
   long long per;
   wgrad_plan(s, cin, cout, bmo, bni, tiles, splits, per);
+  static const bool mma_only = [] {
+    const char * e = std::getenv("DOMA_CONV_PATH");
+    return e && std::string(e) == "mma";
+  }();
+  const bool tc_ok = conv3_wgrad_tc_supported(s, cin, cout);
+  if (path == DOMA_CONV_TENSOR_MEMORY && !tc_ok) {
+    set_error("conv3_wgrad: shape not supported by the tensor-memory kernel");
+    return DOMA_BAD_INPUT;
+  }
+  if (tc_ok && (path == DOMA_CONV_TENSOR_MEMORY || (path == DOMA_CONV_AUTO && !mma_only))) {
+    // tensor cores: partials within the same scratch (at most the MMA plan's splits)
+    int tc_splits = 0;
+    DOMA_TRY(conv3_wgrad_tc(s, x, cin, dz, cout, partial, splits, &tc_splits, st));
+    const size_t count = (size_t)27 * cin * cout;
+    reduce_splits_kernel<<<blocks_for((long long)count), 256, 0, st>>>(partial, tc_splits, count, dw);
+    DOMA_CUDA_TRY(cudaGetLastError());
+    return DOMA_OK;
+  }
   WgradArgs a{x, dz, partial, s.nz, s.ny, s.nx, (long long)s.voxels(), cin, cout, per, cin / bni};
   doma_status r;
   if (bmo == 32) {

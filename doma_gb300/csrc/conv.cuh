@@ -49,15 +49,24 @@ doma_status conv3_forward_mma(const ConvShape & s, const __nv_bfloat16 * x, int 
                               const __nv_bfloat16 * w, const float * bias, int cout, bool relu,
                               __nv_bfloat16 * y, cudaStream_t st);
 doma_status conv3_tc_error(int * flag);
+// Weight-gradient partials on the tensor cores (conv_tc.cu): for shapes the
+// tensor-memory forward supports and cin in {16, 32, 64, 128, 256}, writes
+// FP32 partials [splits][27][cout][cin] (at most max_splits) and *splits_out.
+bool conv3_wgrad_tc_supported(const ConvShape & s, int cin, int cout);
+doma_status conv3_wgrad_tc(const ConvShape & s, const __nv_bfloat16 * x, int cin,
+                           const __nv_bfloat16 * dz, int cout, float * partial, int max_splits,
+                           int * splits_out, cudaStream_t st);
 doma_status conv3_tc_error_reset(cudaStream_t st);
 
 // Weight gradient: dw[tap][cout][cin] = sum over voxels m of
 // dz[m][cout] * x[m + offset(tap)][cin], reduced over voxel splits in a fixed
 // order (deterministic).  partial: scratch of conv3_wgrad_scratch() floats.
+// path: DOMA_CONV_AUTO (tensor cores where supported), DOMA_CONV_MMA or
+// DOMA_CONV_TENSOR_MEMORY; DOMA_CONV_PATH=mma in the environment forces MMA.
 size_t conv3_wgrad_scratch(const ConvShape & s, int cin, int cout);
 doma_status conv3_wgrad(const ConvShape & s, const __nv_bfloat16 * x, int cin,
                         const __nv_bfloat16 * dz, int cout, float * partial, float * dw,
-                        cudaStream_t st);
+                        cudaStream_t st, int path = DOMA_CONV_AUTO);
 
 // Elementwise and resampling pieces of the U-Net (all channels-last, bf16).
 // pool: 2x2x2 average; up: nearest-neighbour 2x; sumpool: adjoint of up.

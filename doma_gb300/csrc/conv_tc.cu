@@ -439,6 +439,228 @@ __global__ void conv_split_reduce_kernel(const float4 * __restrict__ p, int spli
   }
 }
 
+// ---- weight gradient on the tensor cores ------------------------------------------
+//
+// dw[tap][co][ci] = sum over voxels m of x[m + offset(tap)][ci] * dz[m][co].
+// One GEMM per tap with K = voxels.  The rows (M = 128) stack several taps of
+// one input-channel block: 128 / ci_blk taps of ci_blk channels (8 taps of 16
+// channels, 4 of 32, 2 of 64, or one of 128), so that even the 16- and
+// 32-channel layers fill a 128-row MMA.  N = cout.  Both operands come from
+// TMA boxes of the channels-last activations -- a box of SPAN channels over a
+// 128-voxel brick, the tap's shift applied to the brick's (x, y, z)
+// coordinates as in the forward kernel (zero fill outside the volume) -- so
+// the channels are the contiguous (MN) dimension and the voxels the K rows:
+// MN-major operands (instruction-descriptor bits 15 and 16).  In the
+// canonical MN-major swizzled layout an atom is 8 K rows of SPAN channels;
+// SBO steps 8 rows, LBO steps from one SPAN-channel block (one box) to the
+// next along M or N.  Each CTA covers one (tap group, channel block) over a
+// contiguous range of voxel bricks and writes its FP32 sums as partials
+// [split][tap][co][ci], which are added in split order afterwards
+// (deterministic).
+
+// Shared-memory descriptor of an MN-major swizzled tile.
+__device__ __forceinline__ uint64_t smem_desc_mn(uint32_t addr, uint32_t lbo, uint32_t sbo,
+                                                 uint32_t mode)
+{
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)mode << 61;
+  return d;
+}
+
+struct WgArgs {
+  float * partial;            // [splits][27][cout][cin]
+  long long bricks;           // 128-voxel bricks in the volume
+  int bx, by, bz, bb;         // voxel brick (bx*by*bz*bb = 128)
+  int tx, ty, tz;             // bricks per axis
+  int cin, cout;
+  int ci_blk;                 // input channels of one block (16, 32, 64 or 128)
+  int tpg;                    // taps per group: 128 / ci_blk
+  int groups;                 // tap groups: ceil(27 / tpg)
+  int splits;
+};
+
+constexpr uint32_t swizzle_mode(int span_bytes)
+{
+  return span_bytes == 128 ? 2u : (span_bytes == 64 ? 4u : 6u);
+}
+
+template <int SPAN_A, int N>
+__global__ void __launch_bounds__(kThreads, 1)
+    conv3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap tmX,
+                          const __grid_constant__ CUtensorMap tmD, const WgArgs a)
+{
+  constexpr int SPAN_B = N < 64 ? N : 64;            // dz channels per box
+  constexpr int NBA = 128 / SPAN_A, NBB = N / SPAN_B;
+  constexpr int A_BOX = 128 * SPAN_A * 2, B_BOX = 128 * SPAN_B * 2;
+  constexpr int A_BYTES = NBA * A_BOX, B_BYTES = NBB * B_BOX, STAGE = A_BYTES + B_BYTES;
+  constexpr int STAGES = std::max(2, std::min(4, (200 * 1024) / STAGE));
+  constexpr uint32_t SBO_A = 8 * SPAN_A * 2, SBO_B = 8 * SPAN_B * 2;
+  constexpr uint32_t MODE_A = swizzle_mode(SPAN_A * 2), MODE_B = swizzle_mode(SPAN_B * 2);
+  constexpr uint32_t IDESC = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
+  static_assert(A_BYTES == 128 * 128 * 2, "A stage: 128 rows x 128 voxels");
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t * smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+  uint64_t * full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE);
+  uint64_t * empty = full + STAGES;
+  uint64_t * tmem_full = empty + STAGES;
+  uint32_t * tmem_slot = reinterpret_cast<uint32_t *>(tmem_full + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0 && lane == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(tmem_full, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __shared__ int s_issued, s_consumed;
+  if (threadIdx.x == 0) s_issued = s_consumed = 0;
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(tmem_slot)),
+                 "r"((uint32_t)N));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int g = (int)blockIdx.x % a.groups;          // tap group
+  const int cb = (int)blockIdx.x / a.groups;         // input-channel block
+  const int split = (int)blockIdx.y;
+  const long long k0 = (long long)split * a.bricks / a.splits;
+  const int kn = (int)((long long)(split + 1) * a.bricks / a.splits - k0);
+  const int bpt = a.ci_blk / SPAN_A;                 // A boxes per tap
+  // A boxes that carry a tap (the last group may have fewer than tpg taps)
+  const int taps_here = min(a.tpg, 27 - g * a.tpg);
+  const int boxes_a = taps_here * bpt;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(&tmX) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(&tmD) : "memory");
+      int j = 0;
+      for (; j < kn; ++j) {
+        const int s = j % STAGES;
+        const uint32_t use = (uint32_t)(j / STAGES);
+        if (j >= STAGES && !mbar_wait(empty + s, (use & 1u) ^ 1u)) break;
+        long long t = k0 + j;
+        const int x0 = (int)(t % a.tx) * a.bx;
+        t /= a.tx;
+        const int y0 = (int)(t % a.ty) * a.by;
+        t /= a.ty;
+        const int z0 = (int)(t % a.tz) * a.bz;
+        const int b0 = (int)(t / a.tz) * a.bb;
+        uint8_t * As = smem + s * STAGE;
+        uint8_t * Bs = As + A_BYTES;
+        mbar_expect_tx(full + s, (uint32_t)(boxes_a * A_BOX + B_BYTES));
+        for (int b = 0; b < boxes_a; ++b) {
+          const int tap = g * a.tpg + b / bpt;
+          const int c0 = cb * a.ci_blk + (b % bpt) * SPAN_A;
+          const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+          tma_load_5d(As + b * A_BOX, &tmX, full + s, c0, x0 + dx, y0 + dy, z0 + dz, b0);
+        }
+        for (int b = 0; b < NBB; ++b)
+          tma_load_5d(Bs + b * B_BOX, &tmD, full + s, b * SPAN_B, x0, y0, z0, b0);
+      }
+      s_issued = j;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int j = 0;
+      for (; j < kn; ++j) {
+        const int s = j % STAGES;
+        const uint32_t use = (uint32_t)(j / STAGES);
+        if (!mbar_wait(full + s, use & 1u)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a_addr = saddr(smem + s * STAGE);
+        const uint32_t b_addr = a_addr + A_BYTES;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {   // 16 voxels (two 8-row atoms) per MMA
+          const uint64_t ad = smem_desc_mn(a_addr + k * 2 * SBO_A, A_BOX, SBO_A, MODE_A);
+          const uint64_t bd = smem_desc_mn(b_addr + k * 2 * SBO_B, B_BOX, SBO_B, MODE_B);
+          umma_bf16(tmem, ad, bd, IDESC, (j | k) != 0 ? 1u : 0u);
+        }
+        umma_commit(empty + s);
+      }
+      s_consumed = j;
+      umma_commit(tmem_full);  // also after a failed wait, so the epilogue is released
+    }
+  } else {
+    // epilogue: warps 2..5 cover TMEM lane quarters 2, 3, 0, 1; row = (tap slot, channel)
+    const int q = warp & 3;
+    int ok = 0;
+    if (lane == 0) ok = mbar_wait(tmem_full, 0) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0) && kn > 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int row = q * 32 + lane;
+    const int tap = g * a.tpg + row / a.ci_blk;
+    const int ci = cb * a.ci_blk + row % a.ci_blk;
+    float * out = a.partial + ((long long)split * 27 + tap) * a.cout * (long long)a.cin + ci;
+#pragma unroll 1
+    for (int c0 = 0; ok && c0 < N; c0 += 32) {
+      uint32_t v[32];
+      tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+      if (tap < 27) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) out[(long long)(c0 + j) * a.cin] = __uint_as_float(v[j]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  // Teardown after a failed wait: let this CTA's own copies and MMAs in
+  // flight land (bounded) before its shared and tensor memory go away.
+  if (threadIdx.x == 0)
+    for (int i = s_consumed; i < s_issued; ++i)
+      mbar_wait(full + i % STAGES, (uint32_t)(i / STAGES) & 1u);
+  if (threadIdx.x == 32) mbar_wait(tmem_full, 0);
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)N));
+  }
+}
+
+template <int SPAN_A, int N>
+doma_status launch_wgrad_tc(const CUtensorMap & mx, const CUtensorMap & md, const WgArgs & a,
+                            cudaStream_t st)
+{
+  constexpr int SPAN_B = N < 64 ? N : 64;
+  constexpr int STAGE = 128 * 128 * 2 + (N / SPAN_B) * 128 * SPAN_B * 2;
+  constexpr int STAGES = std::max(2, std::min(4, (200 * 1024) / STAGE));
+  constexpr int smem = STAGES * STAGE + 1024 + (2 * STAGES + 2) * 8;
+  static bool configured = false;
+  if (!configured) {
+    DOMA_CUDA_TRY(cudaFuncSetAttribute(conv3_wgrad_tc_kernel<SPAN_A, N>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = true;
+  }
+  conv3_wgrad_tc_kernel<SPAN_A, N><<<dim3((unsigned)(a.groups * (a.cin / a.ci_blk)),
+                                          (unsigned)a.splits), kThreads, smem, st>>>(mx, md, a);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+template <int SPAN_A>
+doma_status dispatch_wgrad_n(const CUtensorMap & mx, const CUtensorMap & md, const WgArgs & a,
+                             cudaStream_t st)
+{
+  switch (a.cout) {
+    case 32: return launch_wgrad_tc<SPAN_A, 32>(mx, md, a, st);
+    case 64: return launch_wgrad_tc<SPAN_A, 64>(mx, md, a, st);
+    case 128: return launch_wgrad_tc<SPAN_A, 128>(mx, md, a, st);
+    default: return launch_wgrad_tc<SPAN_A, 256>(mx, md, a, st);
+  }
+}
+
 int sm_count()
 {
   static int n = 0;
@@ -575,6 +797,81 @@ doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const
                                                      reinterpret_cast<uint2 *>(y));
     DOMA_CUDA_TRY(cudaGetLastError());
   }
+  return DOMA_OK;
+}
+
+bool conv3_wgrad_tc_supported(const ConvShape & s, int cin, int cout)
+{
+  if (!(cin == 16 || cin == 32 || cin == 64 || cin == 128 || cin == 256)) return false;
+  return conv3_tc_supported(s, cin, cout);
+}
+
+doma_status conv3_wgrad_tc(const ConvShape & s, const bf16 * x, int cin, const bf16 * dz, int cout,
+                           float * partial, int max_splits, int * splits_out, cudaStream_t st)
+{
+  if (!conv3_wgrad_tc_supported(s, cin, cout)) {
+    set_error("conv3_wgrad_tc: shape not supported by the tensor-memory kernel");
+    return DOMA_BAD_INPUT;
+  }
+  WgArgs a{};
+  a.partial = partial;
+  a.bx = std::min(s.nx, 128);
+  a.by = std::min(s.ny, 128 / a.bx);
+  a.bz = std::min(s.nz, 128 / (a.bx * a.by));
+  a.bb = 128 / (a.bx * a.by * a.bz);
+  a.tx = s.nx / a.bx;
+  a.ty = s.ny / a.by;
+  a.tz = s.nz / a.bz;
+  a.bricks = (long long)(s.voxels() / 128);
+  a.cin = cin;
+  a.cout = cout;
+  a.ci_blk = std::min(cin, 128);
+  a.tpg = 128 / a.ci_blk;
+  a.groups = (27 + a.tpg - 1) / a.tpg;
+  const int ctas = a.groups * (cin / a.ci_blk);
+  // enough CTAs for two per SM, at least two bricks per split
+  long long want = (2LL * sm_count() + ctas - 1) / ctas;
+  want = std::min<long long>(want, std::max<long long>(1, a.bricks / 2));
+  a.splits = (int)std::max<long long>(1, std::min<long long>(want, std::max(1, max_splits)));
+  const int span_a = std::min(a.ci_blk, 64), span_b = std::min(cout, 64);
+  CUtensorMap mx, md;
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  {
+    const cuuint64_t gdim[5] = {(cuuint64_t)cin, (cuuint64_t)s.nx, (cuuint64_t)s.ny,
+                                (cuuint64_t)s.nz, (cuuint64_t)s.batch};
+    const cuuint64_t row = (cuuint64_t)cin * 2;
+    const cuuint64_t gstr[4] = {row, row * s.nx, row * s.nx * s.ny, row * s.nx * s.ny * s.nz};
+    const cuuint32_t box[5] = {(cuuint32_t)span_a, (cuuint32_t)a.bx, (cuuint32_t)a.by,
+                               (cuuint32_t)a.bz, (cuuint32_t)a.bb};
+    const CUresult r = encoder()(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x),
+                                 gdim, gstr, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                 swizzle_for(span_a), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      set_error("cuTensorMapEncodeTiled (wgrad activations) failed: " + std::to_string((int)r));
+      return DOMA_CUDA_ERROR;
+    }
+  }
+  {
+    const cuuint64_t gdim[5] = {(cuuint64_t)cout, (cuuint64_t)s.nx, (cuuint64_t)s.ny,
+                                (cuuint64_t)s.nz, (cuuint64_t)s.batch};
+    const cuuint64_t row = (cuuint64_t)cout * 2;
+    const cuuint64_t gstr[4] = {row, row * s.nx, row * s.nx * s.ny, row * s.nx * s.ny * s.nz};
+    const cuuint32_t box[5] = {(cuuint32_t)span_b, (cuuint32_t)a.bx, (cuuint32_t)a.by,
+                               (cuuint32_t)a.bz, (cuuint32_t)a.bb};
+    const CUresult r = encoder()(&md, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(dz),
+                                 gdim, gstr, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                 swizzle_for(span_b), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      set_error("cuTensorMapEncodeTiled (wgrad output gradient) failed: " + std::to_string((int)r));
+      return DOMA_CUDA_ERROR;
+    }
+  }
+  if (span_a == 64) DOMA_TRY(dispatch_wgrad_n<64>(mx, md, a, st));
+  else if (span_a == 32) DOMA_TRY(dispatch_wgrad_n<32>(mx, md, a, st));
+  else DOMA_TRY(dispatch_wgrad_n<16>(mx, md, a, st));
+  if (splits_out) *splits_out = a.splits;
   return DOMA_OK;
 }
 

@@ -42,6 +42,9 @@
 
 #include "common.cuh"
 
+#ifndef DOMA_SWEEP_MIN_CTAS_DD
+#define DOMA_SWEEP_MIN_CTAS_DD 4
+#endif
 #ifndef DOMA_SWEEP_MIN_CTAS
 #define DOMA_SWEEP_MIN_CTAS 3
 #endif
@@ -861,7 +864,9 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 template <typename T, int SCHEME>
 constexpr int sweep_min_ctas()
 {
-  return std::is_same<T, double>::value ? 1 : SCHEME == DOMA_SCHEME_DD ? 4 : DOMA_SWEEP_MIN_CTAS;
+  return std::is_same<T, double>::value ? 1
+         : SCHEME == DOMA_SCHEME_DD     ? DOMA_SWEEP_MIN_CTAS_DD
+                                        : DOMA_SWEEP_MIN_CTAS;
 }
 
 template <typename T, int DIMS, int TX>

@@ -461,6 +461,29 @@ doma_status doma_conv3_forward(const void * x, uint32_t batch, uint32_t nz, uint
   return r;
 }
 
+doma_status doma_conv3_wgrad(const void * x, uint32_t batch, uint32_t nz, uint32_t ny, uint32_t nx,
+                             uint32_t cin, const void * dz, uint32_t cout, float * dw,
+                             uint32_t path, void * stream)
+{
+  if (!x || !dz || !dw) return bad_net("null tensor");
+  const ConvShape s{(int)batch, (int)nz, (int)ny, (int)nx};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (path == DOMA_CONV_TENSOR_MEMORY || path == DOMA_CONV_AUTO) DOMA_TRY(conv3_tc_error_reset(st));
+  // the split partials, stream-ordered here (the U-Net keeps them in its workspace)
+  void * p = nullptr;
+  const size_t floats = conv3_wgrad_scratch(s, (int)cin, (int)cout);
+  DOMA_CUDA_TRY(cudaMallocAsync(&p, std::max<size_t>(floats, 1) * sizeof(float), st));
+  const doma_status r = conv3_wgrad(s, static_cast<const bf16 *>(x), (int)cin,
+                                    static_cast<const bf16 *>(dz), (int)cout,
+                                    static_cast<float *>(p), dw, st, (int)path);
+  const cudaError_t e = cudaFreeAsync(p, st);
+  if (r == DOMA_OK && e != cudaSuccess) {
+    set_error(std::string("cudaFreeAsync: ") + cudaGetErrorString(e));
+    return DOMA_CUDA_ERROR;
+  }
+  return r;
+}
+
 doma_status doma_conv_wait_error(int * flag)
 {
   if (!flag) return bad_net("null flag");

@@ -383,6 +383,15 @@ doma_status doma_conv3_forward(const void *x, uint32_t batch, uint32_t nz, uint3
                                uint32_t nx, uint32_t cin, const void *w, const float *bias,
                                uint32_t cout, uint32_t relu, void *y, uint32_t path, void *stream);
 doma_status doma_conv_wait_error(int *flag);
+/* The weight gradient of one such convolution: dw[27][cout][cin] (FP32,
+ * device) = sum over voxels of x[voxel + tap offset][cin] * dz[voxel][cout],
+ * x [batch][nz][ny][nx][cin] and dz [...][cout] bf16 channels-last, reduced
+ * in a fixed order.  path as above: the tensor-memory kernel stacks taps
+ * along the MMA's 128 rows; DOMA_CONV_MMA is the warp-MMA kernel.  Scratch
+ * for the partial sums is allocated on `stream` and freed there. */
+doma_status doma_conv3_wgrad(const void *x, uint32_t batch, uint32_t nz, uint32_t ny, uint32_t nx,
+                             uint32_t cin, const void *dz, uint32_t cout, float *dw,
+                             uint32_t path, void *stream);
 
 /* Learned corrections inside a multigroup solve (3D, DD, extents multiples
  * of 8).  After `first` iterations, and then every `interval` iterations,

@@ -86,3 +86,57 @@ def test_split_reduction_is_deterministic():
 def test_conv_path_constants_are_exported():
     from doma_gb300 import abi
     assert (abi.DOMA_CONV_AUTO, abi.DOMA_CONV_MMA, abi.DOMA_CONV_TENSOR_MEMORY) == (0, 1, 2)
+
+
+WGRAD_CASES = CASES + [
+    (1, 64, 64, 64, 32, 32),    # the 64^3 level: 4 taps of 32 channels per MMA
+    (1, 8, 8, 8, 256, 256),     # two 128-channel blocks, one tap per MMA
+]
+
+
+def run_wgrad(case, path, seed=0):
+    import torch
+    from doma_gb300 import abi
+    b, z, y, x, cin, cout = case
+    rng = np.random.default_rng(seed)
+    xs = rng.normal(0, 1, (b, z, y, x, cin)).astype(np.float32)
+    gs = rng.normal(0, 1, (b, z, y, x, cout)).astype(np.float32)
+    dev = torch.device("cuda:0")
+    xd = torch.from_numpy(xs).to(dev).to(torch.bfloat16).contiguous()
+    gd = torch.from_numpy(gs).to(dev).to(torch.bfloat16).contiguous()
+    dw = torch.full((27, cout, cin), float("nan"), device=dev)
+    lib = abi.load_library()
+    st = lib.doma_conv3_wgrad(ctypes.c_void_p(xd.data_ptr()), b, z, y, x, cin,
+                              ctypes.c_void_p(gd.data_ptr()), cout,
+                              ctypes.c_void_p(dw.data_ptr()), path, None)
+    abi.check(st, "doma_conv3_wgrad", lib)
+    torch.cuda.synchronize()
+    flag = ctypes.c_int(-1)
+    abi.check(lib.doma_conv_wait_error(ctypes.byref(flag)), "doma_conv_wait_error", lib)
+    assert flag.value == 0
+    return dw.cpu().numpy().astype(np.float64), xs, gs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", WGRAD_CASES)
+def test_tensor_memory_wgrad_matches_the_oracle(case):
+    """The tensor-core weight gradient (taps stacked along the MMA rows,
+    MN-major operands straight from TMA) against the FP64 oracle on the same
+    bf16 inputs, and against the warp-MMA kernel."""
+    from doma_gb300 import abi
+    got, xs, gs = run_wgrad(case, abi.DOMA_CONV_TENSOR_MEMORY, seed=5)
+    want = U.conv_wgrad(U.round_bf16(xs), U.round_bf16(gs))
+    assert np.all(np.isfinite(got))
+    err = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err < 1e-4, err
+    mma, _, _ = run_wgrad(case, abi.DOMA_CONV_MMA, seed=5)
+    assert np.linalg.norm(mma - want) / np.linalg.norm(want) < 1e-4
+
+
+@pytest.mark.gpu
+def test_tensor_memory_wgrad_is_deterministic():
+    from doma_gb300 import abi
+    case = (1, 16, 16, 16, 64, 64)
+    a, _, _ = run_wgrad(case, abi.DOMA_CONV_TENSOR_MEMORY, seed=9)
+    b, _, _ = run_wgrad(case, abi.DOMA_CONV_TENSOR_MEMORY, seed=9)
+    assert np.array_equal(a, b)
