@@ -506,32 +506,48 @@ __global__ void relu_mask_kernel(size_t vecs, bf16 * g, const bf16 * y)
 
 // Bias gradient: block b sums voxels b, b + B, ... of each channel; the
 // block partials are then added in block order.
+// Per-block partial column sums of g [voxels][c] (bf16): each thread owns one
+// 8-channel group of a fixed set of voxels and reads it as one 16-byte vector;
+// the block then adds its voxel lanes per channel in lane order (fixed, so
+// deterministic).
 __global__ void bias_grad_kernel(long long voxels, int c, const bf16 * g, float * partial)
 {
-  extern __shared__ float sh[];
-  const int lanes_per = blockDim.x / c;  // voxel lanes per channel (blockDim multiple of c)
-  const int ch = threadIdx.x % c, lane = threadIdx.x / c;
-  float s = 0.0f;
-  if (lane < lanes_per)
-    for (long long m = (long long)blockIdx.x * lanes_per + lane; m < voxels;
-         m += (long long)gridDim.x * lanes_per)
-      s += __bfloat162float(g[m * c + ch]);
-  sh[threadIdx.x] = s;
+  extern __shared__ float sh[];  // [lanes][c]
+  const int groups = c / 8;
+  const int lanes = blockDim.x / groups;   // blockDim is a multiple of c / 8
+  const int cg = threadIdx.x % groups, lane = threadIdx.x / groups;
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (lane < lanes) {
+#pragma unroll 4
+    for (long long m = (long long)blockIdx.x * lanes + lane; m < voxels;
+         m += (long long)gridDim.x * lanes) {
+      const Vec8 v = load8(g + m * c + cg * 8);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] += v.v[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sh[lane * c + cg * 8 + q] = acc[q];
+  }
   __syncthreads();
-  if (threadIdx.x < c) {
+  for (int ch = threadIdx.x; ch < c; ch += blockDim.x) {
     float t = 0.0f;
-    for (int l = 0; l < lanes_per; ++l) t += sh[l * c + threadIdx.x];
-    partial[(size_t)blockIdx.x * c + threadIdx.x] = t;
+    for (int l = 0; l < lanes; ++l) t += sh[l * c + ch];
+    partial[(size_t)blockIdx.x * c + ch] = t;
   }
 }
 
+// out[ch] = sum over blocks of partial[b][ch]: one warp per channel, each lane
+// adding every 32nd block in order, then a fixed shuffle tree (deterministic).
 __global__ void sum_blocks_kernel(const float * partial, int blocks, int c, float * out)
 {
-  for (int ch = threadIdx.x; ch < c; ch += blockDim.x) {
-    float t = 0.0f;
-    for (int b = 0; b < blocks; ++b) t += partial[(size_t)b * c + ch];
-    out[ch] = t;
-  }
+  const int ch = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (ch >= c) return;
+  float t = 0.0f;
+  for (int b = lane; b < blocks; b += 32) t += partial[(size_t)b * c + ch];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[ch] = t;
 }
 
 __global__ void head_forward_kernel(long long voxels, int c, const bf16 * x, const float * w,
@@ -731,6 +747,7 @@ size_t conv3_wgrad_scratch(const ConvShape & s, int cin, int cout)
   int bmo, bni, tiles, splits;
   long long per;
   wgrad_plan(s, cin, cout, bmo, bni, tiles, splits, per);
+  splits = std::max(splits, conv3_wgrad_tc_splits(s, cin, cout));
   return (size_t)splits * 27 * cin * cout;
 }
 
@@ -756,7 +773,8 @@ doma_status conv3_wgrad(const ConvShape & s, const bf16 * x, int cin, const bf16
   if (tc_ok && (path == DOMA_CONV_TENSOR_MEMORY || (path == DOMA_CONV_AUTO && !mma_only))) {
     // tensor cores: partials within the same scratch (at most the MMA plan's splits)
     int tc_splits = 0;
-    DOMA_TRY(conv3_wgrad_tc(s, x, cin, dz, cout, partial, splits, &tc_splits, st));
+    const int room = std::max(splits, conv3_wgrad_tc_splits(s, cin, cout));  // conv3_wgrad_scratch
+    DOMA_TRY(conv3_wgrad_tc(s, x, cin, dz, cout, partial, room, &tc_splits, st));
     const size_t count = (size_t)27 * cin * cout;
     reduce_splits_kernel<<<blocks_for((long long)count), 256, 0, st>>>(partial, tc_splits, count, dw);
     DOMA_CUDA_TRY(cudaGetLastError());
@@ -829,10 +847,15 @@ doma_status bias_grad(size_t voxels, int c, const bf16 * g, float * partial, flo
                       cudaStream_t st)
 {
   const int threads = 256;  // a multiple of every channel count <= 256
-  bias_grad_kernel<<<kReduceBlocks, threads, threads * sizeof(float), st>>>((long long)voxels, c, g,
+  if (c % 8 || threads % (c / 8)) {
+    set_error("bias_grad: the channel count must be a multiple of 8 with c / 8 dividing 256");
+    return DOMA_BAD_INPUT;
+  }
+  // shared memory: [threads / (c / 8) voxel lanes][c] floats = threads * 8 floats
+  bias_grad_kernel<<<kReduceBlocks, threads, threads * 8 * sizeof(float), st>>>((long long)voxels, c, g,
                                                                            partial);
   DOMA_CUDA_TRY(cudaGetLastError());
-  sum_blocks_kernel<<<1, 256, 0, st>>>(partial, kReduceBlocks, c, db);
+  sum_blocks_kernel<<<(c + 7) / 8, 256, 0, st>>>(partial, kReduceBlocks, c, db);
   DOMA_CUDA_TRY(cudaGetLastError());
   return DOMA_OK;
 }

@@ -53,6 +53,7 @@ doma_status conv3_tc_error(int * flag);
 // tensor-memory forward supports and cin in {16, 32, 64, 128, 256}, writes
 // FP32 partials [splits][27][cout][cin] (at most max_splits) and *splits_out.
 bool conv3_wgrad_tc_supported(const ConvShape & s, int cin, int cout);
+int conv3_wgrad_tc_splits(const ConvShape & s, int cin, int cout);  // 0 if unsupported
 doma_status conv3_wgrad_tc(const ConvShape & s, const __nv_bfloat16 * x, int cin,
                            const __nv_bfloat16 * dz, int cout, float * partial, int max_splits,
                            int * splits_out, cudaStream_t st);

@@ -23,6 +23,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <mutex>
 
 #include "conv.cuh"
@@ -487,8 +489,15 @@ constexpr uint32_t swizzle_mode(int span_bytes)
   return span_bytes == 128 ? 2u : (span_bytes == 64 ? 4u : 6u);
 }
 
+// Two pipeline stages per CTA; with N <= 64 two CTAs share an SM (their
+// prologues and epilogues overlap each other's main loops), wider N take one.
+constexpr int kWgStages = 2;
+constexpr int wg_stage_bytes(int n) { return 128 * 128 * 2 + 128 * n * 2; }
+constexpr int wg_smem_bytes(int n) { return kWgStages * wg_stage_bytes(n) + 1024 + (2 * kWgStages + 2) * 8; }
+constexpr int wg_ctas_per_sm(int n) { return n <= 64 ? 2 : 1; }
+
 template <int SPAN_A, int N>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, wg_ctas_per_sm(N))
     conv3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap tmX,
                           const __grid_constant__ CUtensorMap tmD, const WgArgs a)
 {
@@ -496,11 +505,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   constexpr int NBA = 128 / SPAN_A, NBB = N / SPAN_B;
   constexpr int A_BOX = 128 * SPAN_A * 2, B_BOX = 128 * SPAN_B * 2;
   constexpr int A_BYTES = NBA * A_BOX, B_BYTES = NBB * B_BOX, STAGE = A_BYTES + B_BYTES;
-  constexpr int STAGES = std::max(2, std::min(4, (200 * 1024) / STAGE));
+  constexpr int STAGES = kWgStages;
   constexpr uint32_t SBO_A = 8 * SPAN_A * 2, SBO_B = 8 * SPAN_B * 2;
   constexpr uint32_t MODE_A = swizzle_mode(SPAN_A * 2), MODE_B = swizzle_mode(SPAN_B * 2);
   constexpr uint32_t IDESC = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
   static_assert(A_BYTES == 128 * 128 * 2, "A stage: 128 rows x 128 voxels");
+  static_assert(STAGE == wg_stage_bytes(N), "stage layout");
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t * smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
@@ -633,10 +643,7 @@ template <int SPAN_A, int N>
 doma_status launch_wgrad_tc(const CUtensorMap & mx, const CUtensorMap & md, const WgArgs & a,
                             cudaStream_t st)
 {
-  constexpr int SPAN_B = N < 64 ? N : 64;
-  constexpr int STAGE = 128 * 128 * 2 + (N / SPAN_B) * 128 * SPAN_B * 2;
-  constexpr int STAGES = std::max(2, std::min(4, (200 * 1024) / STAGE));
-  constexpr int smem = STAGES * STAGE + 1024 + (2 * STAGES + 2) * 8;
+  constexpr int smem = wg_smem_bytes(N);
   static bool configured = false;
   if (!configured) {
     DOMA_CUDA_TRY(cudaFuncSetAttribute(conv3_wgrad_tc_kernel<SPAN_A, N>,
@@ -659,6 +666,264 @@ doma_status dispatch_wgrad_n(const CUtensorMap & mx, const CUtensorMap & md, con
     case 128: return launch_wgrad_tc<SPAN_A, 128>(mx, md, a, st);
     default: return launch_wgrad_tc<SPAN_A, 256>(mx, md, a, st);
   }
+}
+
+// ---- halo-tile forward convolution (16- and 32-channel inputs) ------------------
+//
+// For inputs of at most 32 channels the tile's A operand is staged once per
+// tile instead of once per tap: the CTA loads the output brick's halo --
+// (8 + 2) x (16 + 2) x 3 voxels around an 8 x 16 x 1 brick -- as one TMA box
+// per 8-channel group, unswizzled, so each plane is [z][y][x] x 16 bytes.  In
+// the canonical K-major layout without swizzle a core matrix is 8 rows x 16
+// bytes: here 8 consecutive x of one y row.  The 128 rows of the brick are 16
+// such core matrices one halo row (10 voxels, 160 B = SBO) apart, the K
+// dimension steps from one 8-channel plane to the next (LBO = plane stride),
+// and tap (dz, dy, dx) starts ((dz+1) 180 + (dy+1) 10 + (dx+1)) x 16 bytes into
+// the halo.  So 27 taps read 540 staged rows per 8 channels, against
+// 27 x 128 = 3,456 for one shifted box per tap.  The weights of all 27 taps
+// (27 x cout x cin, at most 108 KB) stay resident: the CTA is persistent over
+// output bricks, the halo stages are triple-buffered, and the accumulator is
+// double-buffered in tensor memory so a brick's epilogue overlaps the next
+// brick's MMAs.  Each brick accumulates tap by tap in the same order as
+// conv3_tc_kernel (one channel chunk), so the sums are the same.
+
+constexpr int kHaloPlane = 8704;    // 10 x 18 x 3 x 16 B = 8640, padded to 128 B
+constexpr int kHaloStages = 3;
+
+__device__ __forceinline__ void tma_load_3d(void * dst, const CUtensorMap * map, uint64_t * bar,
+                                            int c0, int c1, int c2)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5}], [%2];" ::"r"(saddr(dst)),
+      "l"(map), "r"(saddr(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t * bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+
+struct HaloArgs {
+  const float * bias;
+  bf16 * y;
+  int nz, ny, nx;
+  int tiles_x, tiles_y;       // nx / 8, ny / 16
+  long long tiles;            // batch * nz * tiles_y * tiles_x
+};
+
+template <int KC, int N>
+constexpr int halo_smem_bytes()
+{
+  return 27 * N * KC * 2 + kHaloStages * (KC / 8) * kHaloPlane + 1024 + 16 * 8;
+}
+
+template <int KC, int N, bool RELU>
+__global__ void __launch_bounds__(kThreads, 1)
+    conv3_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
+                      const HaloArgs a)
+{
+  constexpr int PLANES = KC / 8;
+  constexpr int A_STAGE = PLANES * kHaloPlane;
+  constexpr int B_TAP = N * KC * 2;
+  constexpr int B_BYTES = 27 * B_TAP;
+  constexpr uint32_t MODE_B = KC == 32 ? 4u : 6u;      // 64- or 32-byte swizzle rows
+  constexpr uint32_t SBO_B = 8 * KC * 2;
+  constexpr uint32_t IDESC = idesc_bf16(128, N);
+  constexpr uint32_t TMEM_COLS = 2 * N;
+  static_assert(B_BYTES % 1024 == 0, "the halo stages start 1024-byte aligned");
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t * smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+  uint8_t * Bsm = smem;
+  uint8_t * Asm = smem + B_BYTES;
+  uint64_t * bars = reinterpret_cast<uint64_t *>(Asm + kHaloStages * A_STAGE);
+  uint64_t * b_full = bars;
+  uint64_t * full = bars + 1;
+  uint64_t * empty = full + kHaloStages;
+  uint64_t * tfull = empty + kHaloStages;             // [2]
+  uint64_t * tempty = tfull + 2;                      // [2]
+  uint32_t * tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0 && lane == 0) {
+    mbar_init(b_full, 1);
+    for (int s = 0; s < kHaloStages; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull + b, 1);
+      mbar_init(tempty + b, 128);   // every epilogue thread arrives
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __shared__ int s_issued, s_consumed, s_committed;
+  if (threadIdx.x == 0) s_issued = s_consumed = s_committed = 0;
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  // this CTA's bricks: blockIdx.x, blockIdx.x + gridDim.x, ...
+  const int my = (int)((a.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(&tmX) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(&tmW) : "memory");
+      mbar_expect_tx(b_full, (uint32_t)B_BYTES);
+      tma_load_3d(Bsm, &tmW, b_full, 0, 0, 0);
+      int i = 0;
+      for (; i < my; ++i) {
+        const int s = i % kHaloStages;
+        const uint32_t use = (uint32_t)(i / kHaloStages);
+        if (i >= kHaloStages && !mbar_wait(empty + s, (use & 1u) ^ 1u)) break;
+        long long t = blockIdx.x + (long long)i * gridDim.x;
+        const int x0 = (int)(t % a.tiles_x) * 8;
+        t /= a.tiles_x;
+        const int y0 = (int)(t % a.tiles_y) * 16;
+        t /= a.tiles_y;
+        const int z0 = (int)(t % a.nz);
+        const int b0 = (int)(t / a.nz);
+        uint8_t * As = Asm + s * A_STAGE;
+        mbar_expect_tx(full + s, (uint32_t)(PLANES * 8640));
+        for (int p = 0; p < PLANES; ++p)
+          tma_load_5d(As + p * kHaloPlane, &tmX, full + s, p * 8, x0 - 1, y0 - 1, z0 - 1, b0);
+      }
+      s_issued = i;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int i = 0;
+      bool ok = mbar_wait(b_full, 0);
+      for (; ok && i < my; ++i) {
+        const int s = i % kHaloStages, buf = i & 1;
+        const uint32_t use = (uint32_t)(i / kHaloStages);
+        if (!mbar_wait(full + s, use & 1u)) break;
+        if (i >= 2 && !mbar_wait(tempty + buf, (uint32_t)((i >> 1) - 1) & 1u)) {
+          s_consumed = i;   // stage s landed but is not used
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a_addr = saddr(Asm + s * A_STAGE);
+        const uint32_t b_addr = saddr(Bsm);
+        const uint32_t d = tmem + (uint32_t)(buf * N);
+        for (int tap = 0; tap < 27; ++tap) {
+          const uint32_t off = (uint32_t)(((tap / 9) * 180 + ((tap / 3) % 3) * 10 + tap % 3) * 16);
+#pragma unroll
+          for (int k = 0; k < KC / 16; ++k) {
+            const uint64_t ad = smem_desc_mn(a_addr + off + k * 2 * kHaloPlane, kHaloPlane, 160, 0u);
+            const uint64_t bd = smem_desc(b_addr + tap * B_TAP + k * 32, SBO_B, MODE_B);
+            umma_bf16(d, ad, bd, IDESC, (tap | k) != 0 ? 1u : 0u);
+          }
+        }
+        umma_commit(empty + s);
+        umma_commit(tfull + buf);
+        s_committed = i + 1;
+      }
+      if (ok) s_consumed = i;
+    }
+  } else {
+    // epilogue: warps 2..5 cover TMEM lane quarters 2, 3, 0, 1
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    for (int i = 0; i < my; ++i) {
+      const int buf = i & 1;
+      int ok = 0;
+      if (lane == 0) ok = mbar_wait(tfull + buf, (uint32_t)(i >> 1) & 1u) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      long long t = blockIdx.x + (long long)i * gridDim.x;
+      const int x0 = (int)(t % a.tiles_x) * 8;
+      t /= a.tiles_x;
+      const int y0 = (int)(t % a.tiles_y) * 16;
+      t /= a.tiles_y;
+      const int z0 = (int)(t % a.nz);
+      const long long b0 = t / a.nz;
+      const long long vox = ((b0 * a.nz + z0) * a.ny + (y0 + row / 8)) * a.nx + (x0 + row % 8);
+      bf16 * out = a.y + vox * N;
+#pragma unroll 1
+      for (int c0 = 0; c0 < N; c0 += 32) {
+        uint32_t v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * N + c0), v);
+        uint4 pk[4];
+        uint32_t * pw = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+          if (a.bias) {
+            f0 += __ldg(a.bias + c0 + 2 * j);
+            f1 += __ldg(a.bias + c0 + 2 * j + 1);
+          }
+          if (RELU) {
+            f0 = fmaxf(f0, 0.0f);
+            f1 = fmaxf(f1, 0.0f);
+          }
+          const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+          pw[j] = *reinterpret_cast<const uint32_t *>(&h);
+        }
+        uint4 * dst = reinterpret_cast<uint4 *>(out + c0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dst[j] = pk[j];
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(tempty + buf);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  // Teardown after a failed wait: let this CTA's own copies and MMAs in
+  // flight land (bounded) before its shared and tensor memory go away.
+  if (threadIdx.x == 0) {
+    mbar_wait(b_full, 0);
+    for (int i = s_consumed; i < s_issued; ++i)
+      mbar_wait(full + i % kHaloStages, (uint32_t)(i / kHaloStages) & 1u);
+  }
+  if (threadIdx.x == 32 && s_committed > 0) {
+    const int last = s_committed - 1;
+    mbar_wait(tfull + (last & 1), (uint32_t)(last >> 1) & 1u);
+  }
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+int sm_count();
+
+template <int KC, int N, bool RELU>
+doma_status launch_halo(const CUtensorMap & mx, const CUtensorMap & mw, const HaloArgs & a,
+                        cudaStream_t st)
+{
+  constexpr int smem = halo_smem_bytes<KC, N>();
+  static bool configured = false;
+  if (!configured) {
+    DOMA_CUDA_TRY(cudaFuncSetAttribute(conv3_halo_kernel<KC, N, RELU>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = true;
+  }
+  const unsigned grid = (unsigned)std::min<long long>(a.tiles, (long long)sm_count());
+  conv3_halo_kernel<KC, N, RELU><<<grid, kThreads, smem, st>>>(mx, mw, a);
+  DOMA_CUDA_TRY(cudaGetLastError());
+  return DOMA_OK;
+}
+
+template <int KC, int N>
+doma_status launch_halo_act(const CUtensorMap & mx, const CUtensorMap & mw, const HaloArgs & a,
+                            bool relu, cudaStream_t st)
+{
+  return relu ? launch_halo<KC, N, true>(mx, mw, a, st) : launch_halo<KC, N, false>(mx, mw, a, st);
 }
 
 int sm_count()
@@ -729,11 +994,74 @@ bool conv3_tc_supported(const ConvShape & s, int cin, int cout)
   return encoder() != nullptr;
 }
 
+bool conv3_halo_supported(const ConvShape & s, int cin, int cout)
+{
+  return (cin == 16 || cin == 32) && (cout == 32 || cout == 64) && s.nx % 8 == 0 &&
+         s.ny % 16 == 0 && s.nz >= 1 && s.batch >= 1 && encoder() != nullptr;
+}
+
+// The halo-tile kernel for one convolution (conv3_halo_supported shapes).
+doma_status conv3_forward_halo(const ConvShape & s, const bf16 * x, int cin, const bf16 * w,
+                               const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st)
+{
+  HaloArgs a{};
+  a.bias = bias;
+  a.y = y;
+  a.nz = s.nz;
+  a.ny = s.ny;
+  a.nx = s.nx;
+  a.tiles_x = s.nx / 8;
+  a.tiles_y = s.ny / 16;
+  a.tiles = (long long)s.batch * s.nz * a.tiles_y * a.tiles_x;
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUtensorMap mx, mw;
+  {
+    const cuuint64_t gdim[5] = {(cuuint64_t)cin, (cuuint64_t)s.nx, (cuuint64_t)s.ny,
+                                (cuuint64_t)s.nz, (cuuint64_t)s.batch};
+    const cuuint64_t row = (cuuint64_t)cin * 2;
+    const cuuint64_t gstr[4] = {row, row * s.nx, row * s.nx * s.ny, row * s.nx * s.ny * s.nz};
+    const cuuint32_t box[5] = {8, 10, 18, 3, 1};   // one 8-channel plane of the brick's halo
+    const CUresult r = encoder()(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x),
+                                 gdim, gstr, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      set_error("cuTensorMapEncodeTiled (halo) failed: " + std::to_string((int)r));
+      return DOMA_CUDA_ERROR;
+    }
+  }
+  {
+    const cuuint64_t gdim[3] = {(cuuint64_t)cin, (cuuint64_t)cout, 27};
+    const cuuint64_t gstr[2] = {(cuuint64_t)cin * 2, (cuuint64_t)cin * cout * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)cin, (cuuint32_t)cout, 27};   // every tap's weights
+    const CUresult r = encoder()(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(w),
+                                 gdim, gstr, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                 swizzle_for(cin), CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      set_error("cuTensorMapEncodeTiled (halo weights) failed: " + std::to_string((int)r));
+      return DOMA_CUDA_ERROR;
+    }
+  }
+  if (cin == 32) {
+    if (cout == 32) return launch_halo_act<32, 32>(mx, mw, a, relu, st);
+    return launch_halo_act<32, 64>(mx, mw, a, relu, st);
+  }
+  if (cout == 32) return launch_halo_act<16, 32>(mx, mw, a, relu, st);
+  return launch_halo_act<16, 64>(mx, mw, a, relu, st);
+}
+
 doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const bf16 * w,
                              const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st,
                              ConvScratch scratch)
 {
   if (!scratch.p) scratch.floats = 0;
+  static const bool halo_off = [] {
+    const char * e = std::getenv("DOMA_CONV_HALO");
+    return e && std::string(e) == "0";
+  }();
+  if (!halo_off && conv3_halo_supported(s, cin, cout))
+    return conv3_forward_halo(s, x, cin, w, bias, cout, relu, y, st);
   if (!conv3_tc_supported(s, cin, cout)) {
     set_error("conv3_forward_tc: shape not supported by the tensor-memory kernel");
     return DOMA_BAD_INPUT;
@@ -806,6 +1134,21 @@ bool conv3_wgrad_tc_supported(const ConvShape & s, int cin, int cout)
   return conv3_tc_supported(s, cin, cout);
 }
 
+int conv3_wgrad_tc_splits(const ConvShape & s, int cin, int cout)
+{
+  if (!conv3_wgrad_tc_supported(s, cin, cout)) return 0;
+  const int ci_blk = std::min(cin, 128);
+  const int tpg = 128 / ci_blk;
+  const int ctas = ((27 + tpg - 1) / tpg) * (cin / ci_blk);
+  const long long bricks = (long long)(s.voxels() / 128);
+  // whole waves: as many splits as fill the resident CTA slots once, at
+  // least two bricks per split
+  const long long slots = (long long)sm_count() * wg_ctas_per_sm(cout);
+  long long want = std::max<long long>(1, slots / ctas);
+  want = std::min<long long>(want, std::max<long long>(1, bricks / 2));
+  return (int)want;
+}
+
 doma_status conv3_wgrad_tc(const ConvShape & s, const bf16 * x, int cin, const bf16 * dz, int cout,
                            float * partial, int max_splits, int * splits_out, cudaStream_t st)
 {
@@ -828,11 +1171,7 @@ doma_status conv3_wgrad_tc(const ConvShape & s, const bf16 * x, int cin, const b
   a.ci_blk = std::min(cin, 128);
   a.tpg = 128 / a.ci_blk;
   a.groups = (27 + a.tpg - 1) / a.tpg;
-  const int ctas = a.groups * (cin / a.ci_blk);
-  // enough CTAs for two per SM, at least two bricks per split
-  long long want = (2LL * sm_count() + ctas - 1) / ctas;
-  want = std::min<long long>(want, std::max<long long>(1, a.bricks / 2));
-  a.splits = (int)std::max<long long>(1, std::min<long long>(want, std::max(1, max_splits)));
+  a.splits = std::max(1, std::min(conv3_wgrad_tc_splits(s, cin, cout), std::max(1, max_splits)));
   const int span_a = std::min(a.ci_blk, 64), span_b = std::min(cout, 64);
   CUtensorMap mx, md;
   const cuuint32_t estr[5] = {1, 1, 1, 1, 1};

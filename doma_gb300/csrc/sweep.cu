@@ -43,7 +43,7 @@
 #include "common.cuh"
 
 #ifndef DOMA_SWEEP_MIN_CTAS_DD
-#define DOMA_SWEEP_MIN_CTAS_DD 4
+#define DOMA_SWEEP_MIN_CTAS_DD 6
 #endif
 #ifndef DOMA_SWEEP_MIN_CTAS
 #define DOMA_SWEEP_MIN_CTAS 3
