@@ -1000,6 +1000,22 @@ bool conv3_halo_supported(const ConvShape & s, int cin, int cout)
          s.ny % 16 == 0 && s.nz >= 1 && s.batch >= 1 && encoder() != nullptr;
 }
 
+// Where the halo kernel is the faster one.  Its planes are 16-byte rows (8
+// channels of a voxel), which TMA moves row by row with 32-byte sectors: for
+// 16-channel inputs that still beats 27 shifted boxes (24 vs 52 us for the
+// 64^3 input layer on GB300), for 32-channel inputs it does not (58 vs 53 us),
+// so those keep the per-tap kernel.  DOMA_CONV_HALO=1 forces it wherever it
+// applies (tests), 0 turns it off.
+bool conv3_halo_preferred(const ConvShape & s, int cin, int cout)
+{
+  static const int mode = [] {
+    const char * e = std::getenv("DOMA_CONV_HALO");
+    return e ? std::atoi(e) : -1;
+  }();
+  if (mode == 0 || !conv3_halo_supported(s, cin, cout)) return false;
+  return mode == 1 || cin == 16;
+}
+
 // The halo-tile kernel for one convolution (conv3_halo_supported shapes).
 doma_status conv3_forward_halo(const ConvShape & s, const bf16 * x, int cin, const bf16 * w,
                                const float * bias, int cout, bool relu, bf16 * y, cudaStream_t st)
@@ -1056,11 +1072,7 @@ doma_status conv3_forward_tc(const ConvShape & s, const bf16 * x, int cin, const
                              ConvScratch scratch)
 {
   if (!scratch.p) scratch.floats = 0;
-  static const bool halo_off = [] {
-    const char * e = std::getenv("DOMA_CONV_HALO");
-    return e && std::string(e) == "0";
-  }();
-  if (!halo_off && conv3_halo_supported(s, cin, cout))
+  if (conv3_halo_preferred(s, cin, cout))
     return conv3_forward_halo(s, x, cin, w, bias, cout, relu, y, st);
   if (!conv3_tc_supported(s, cin, cout)) {
     set_error("conv3_forward_tc: shape not supported by the tensor-memory kernel");

@@ -140,3 +140,18 @@ def test_tensor_memory_wgrad_is_deterministic():
     a, _, _ = run_wgrad(case, abi.DOMA_CONV_TENSOR_MEMORY, seed=9)
     b, _, _ = run_wgrad(case, abi.DOMA_CONV_TENSOR_MEMORY, seed=9)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_halo_kernel_on_every_shape_it_supports():
+    """The halo-tile kernel runs by default for 16-channel inputs only; with
+    DOMA_CONV_HALO=1 (read once per process, hence the child process) it takes
+    every shape it supports, 32-channel inputs included, and must pass the
+    same oracle comparisons."""
+    import os
+    import subprocess
+    env = dict(os.environ, DOMA_CONV_HALO="1")
+    r = subprocess.run([sys.executable, "-m", "pytest", __file__, "-q", "-m", "gpu",
+                        "-p", "no:cacheprovider", "-k", "tensor_memory_conv_matches_the_oracle"],
+                       env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
