@@ -35,8 +35,19 @@ const char * get_error();
     if (_s != DOMA_OK) return _s;         \
   } while (0)
 
-// Ordinates of one octant handled by one sweep task (two per warp).
-constexpr int kGroup = 16;
+// Ordinates of one octant handled by one sweep task (two per warp), at most
+// kGroupMax.  FP32 DD runs groups of 8: twice the tasks per sweep, each half
+// as long, which shortens the dataflow's critical path (measured on GB300:
+// 100^3 with 36 ordinates per octant 1.73 -> 1.38 ms per sweep, 64^3 with 16
+// ordinates 229 -> 221 us).  FP32 TW-DD, whose cell solve keeps more values
+// live, was slower with 8 (271 -> 278 us at 64^3) and keeps 16, as does the
+// FP64 exact mode.  Every kernel of one (precision, scheme) uses the same
+// size, so single, batched and allocation-free sweeps give the same bits.
+constexpr int kGroupMax = 16;
+__host__ __device__ constexpr int ordinate_group(int precision, int scheme)
+{
+  return precision == DOMA_PREC_FP32 && scheme == DOMA_SCHEME_DD ? 8 : kGroupMax;
+}
 
 // One sweep task: energy group (multigroup mode; 0 otherwise), octant,
 // ordinate group and block coordinates in the octant's sweep frame
@@ -66,7 +77,7 @@ struct SweepArgs {
   int nx, ny, nz;
   int d_oct;           // ordinates per octant
   int d_total;         // ordinates over all octants (exact mode row length)
-  int ngroups;         // ordinate groups per octant (ceil(d_oct / kGroup))
+  int ngroups;         // ordinate groups per octant (ceil(d_oct / ordinate_group))
   int nbx, nby, nbz;   // blocks per axis
   int tx;              // block length along x of this schedule (the batched kernel dispatches on it)
   int num_tasks;
@@ -92,8 +103,9 @@ struct SweepArgs {
   // per-cell sweep inputs: [groups in flight][N] (one group in Gauss-Seidel mode)
   const T * q;
   const T * sigt;
-  // face planes (sweep frame, per (group in flight, octant)):
-  // x [G*8][nz][ny][d_oct], y [G*8][nz][nx][d_oct], z [G*8][ny][nx][d_oct]
+  // face planes (sweep frame, per (group in flight, octant, ordinate group),
+  // ordinate_group slots per face): x [G*8][ngroups][nz][ny][slots], y
+  // [G*8][ngroups][nz][nx][slots], z [G*8][ngroups][ny][nx][slots]
   T * xf;
   T * yf;
   T * zf;
@@ -146,7 +158,7 @@ doma_status launch_sweep_batch(int dims, int scheme, int grid, int threads, size
                                const SweepArgs<float> * args, const BatchTask * tasks,
                                int num_tasks, unsigned * ticket, unsigned * exit_count,
                                unsigned * epoch, const BatchLoop * loops, cudaStream_t stream);
-size_t sweep_batch_smem_bytes(int dims);
+size_t sweep_batch_smem_bytes(int dims, int scheme);
 int sweep_batch_resident_ctas(int dims, int scheme, int threads, size_t smem);
 
 // Host quadrature (quadrature.cpp): np, na <= kMaxQuadPolar; allocates nothing.

@@ -196,7 +196,8 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   const int D = quadrature_fixed(p->num_polar, p->num_azimuthal, (unsigned)dims, counts);
   if (D <= 0) return fail("bad quadrature order");
   const int d_oct = (int)(p->num_polar * p->num_azimuthal);
-  const int ngroups = (d_oct + kGroup - 1) / kGroup;
+  const int kg = ordinate_group(DOMA_PREC_FP32, (int)scheme);
+  const int ngroups = (d_oct + kg - 1) / kg;
   unsigned oct_mask = 0;
   int offs[8];
   for (int o = 0, acc = 0; o < 8; ++o) {
@@ -241,7 +242,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   const size_t o_cy = cv.take(sizeof(float) * (size_t)D * ny);
   const size_t o_cz = cv.take(sizeof(float) * (size_t)D * nz);
   const size_t o_wf = cv.take(sizeof(float) * (size_t)(nx + ny + nz));
-  const size_t slots = (size_t)ngroups * kGroup;  // face slots per face (padded ordinate groups)
+  const size_t slots = (size_t)ngroups * kg;  // face slots per face (padded ordinate groups)
   const size_t o_xf = cv.take(sizeof(float) * 8 * (size_t)nz * ny * slots);
   const size_t o_yf = cv.take(sizeof(float) * 8 * (size_t)nz * nx * slots);
   const size_t o_zf = cv.take(sizeof(float) * 8 * (size_t)ny * nx * slots);
@@ -314,7 +315,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   Schedule sc;  // persistent mode: only the launch shape is used
   sc.tx = tx;
   sc.persistent = true;
-  sc.threads = sweep_threads(std::min(kGroup, d_oct));
+  sc.threads = sweep_threads(std::min(kg, d_oct));
   sc.smem = sweep_smem_bytes(dims, DOMA_PREC_FP32, (int)scheme, tx);
   st = sweep_prepare(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.smem);
   if (st != DOMA_OK) return st;

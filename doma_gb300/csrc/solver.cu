@@ -222,7 +222,8 @@ doma_status validate(const doma_problem * p, const doma_options * o)
 }
 
 // Block shape: tx cells along x (8, 16 or 32) by the kernel's fixed 16-pencil
-// cross-section; ordinates split into groups of at most kGroup per task.
+// cross-section; ordinates split into groups of at most ordinate_group(precision,
+// scheme) per task.
 void pick_tile(doma_solver * s, const doma_options * o)
 {
   // measured on GB300 (64^3, 16 ordinates per octant): DD is fastest with
@@ -232,8 +233,9 @@ void pick_tile(doma_solver * s, const doma_options * o)
   s->sched.tx = sweep_tile_x(want);
   s->sched.ty = s->dims == 3 ? 4 : 16;
   s->sched.tz = s->dims == 3 ? 4 : 1;
-  s->sched.ngroups = (s->d_oct + kGroup - 1) / kGroup;
-  s->sched.gs = std::min(kGroup, s->d_oct);
+  const int kg = ordinate_group((int)o->precision, (int)o->scheme);
+  s->sched.ngroups = (s->d_oct + kg - 1) / kg;
+  s->sched.gs = std::min(kg, s->d_oct);
 }
 
 void build_schedule(doma_solver * s)
@@ -394,9 +396,10 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   DOMA_TRY(dalloc(s, &qb, 2 * gif * N * ts));
   s->d_q = qb;
   s->d_sigt = qb + gif * N * ts;
-  // face planes: kGroup slots per face for each ordinate group (the last
-  // group padded), so a task's faces along a row are contiguous
-  const size_t Do = (size_t)((s->d_oct + kGroup - 1) / kGroup) * kGroup;
+  // face planes: ordinate_group slots per face for each ordinate group (the
+  // last group padded), so a task's faces along a row are contiguous
+  const int kg = ordinate_group((int)s->opts.precision, (int)s->opts.scheme);
+  const size_t Do = (size_t)((s->d_oct + kg - 1) / kg) * kg;
   unsigned char * fb = nullptr;
   const size_t xf = gif * 8 * (size_t)s->nz * s->ny * Do, yf = gif * 8 * (size_t)s->nz * s->nx * Do,
                zf = gif * 8 * (size_t)s->ny * s->nx * Do;
@@ -407,7 +410,7 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   if (exact)
     DOMA_TRY(dalloc(s, &s->d_wpsi, gif * N * (size_t)s->D));
   else
-    DOMA_TRY(dalloc(s, &s->d_octphi, gif * 8 * (size_t)((s->d_oct + kGroup - 1) / kGroup) * N));
+    DOMA_TRY(dalloc(s, &s->d_octphi, gif * 8 * (size_t)((s->d_oct + kg - 1) / kg) * N));
   if (s->mgi) DOMA_TRY(dalloc(s, &s->d_dscratch, (size_t)s->G * N));
 
   pick_tile(s, o);
@@ -2062,7 +2065,8 @@ doma_status reschedule(doma_solver * s, int tx)
 doma_status build_batch_schedule(doma_batch * b)
 {
   const size_t P = b->solvers.size();
-  b->smem = sweep_batch_smem_bytes(b->dims);
+  b->smem = sweep_batch_smem_bytes(b->dims, (int)b->opts.scheme);
+  b->threads = sweep_threads(ordinate_group(DOMA_PREC_FP32, (int)b->opts.scheme));
   std::vector<BatchTask> tasks;
   int max_levels = 0;
   for (auto * s : b->solvers) max_levels = std::max(max_levels, (int)s->sched.level_begin.size() - 1);

@@ -45,6 +45,9 @@
 #ifndef DOMA_SWEEP_MIN_CTAS_DD
 #define DOMA_SWEEP_MIN_CTAS_DD 6
 #endif
+#ifndef DOMA_SWEEP_MIN_CTAS_FP64
+#define DOMA_SWEEP_MIN_CTAS_FP64 1
+#endif
 #ifndef DOMA_SWEEP_MIN_CTAS
 #define DOMA_SWEEP_MIN_CTAS 3
 #endif
@@ -331,23 +334,23 @@ __device__ bool wait_for(const unsigned * flag, unsigned epoch, unsigned limit, 
 // lane - PY, both computed on the previous step, so faces move between
 // lanes with __shfl_up_sync and the warps advance with no block barrier.
 //
-// Face planes (sweep frame, ordinate-group major, kGroup slots per face so
-// that one task's faces along a row are contiguous):
-//   x [G*8][ngroups][nz][ny][kGroup], y [G*8][ngroups][nz][nx][kGroup],
-//   z [G*8][ngroups][ny][nx][kGroup].
+// Face planes (sweep frame, ordinate-group major, KG = ordinate_group(precision,
+// scheme) slots per face so that one task's faces along a row are contiguous):
+//   x [G*8][ngroups][nz][ny][KG], y [G*8][ngroups][nz][nx][KG],
+//   z [G*8][ngroups][ny][nx][KG].
 
 template <int DIMS> struct Pencils;
 template <> struct Pencils<3> { static constexpr int PY = 4, PZ = 4; };
 template <> struct Pencils<2> { static constexpr int PY = 16, PZ = 1; };
 
-template <typename T>
+template <typename T, int KG>
 struct FacePlanes {
   const SweepArgs<T> & A;
   size_t plane;  // (group in flight, octant, ordinate group)
   __device__ FacePlanes(const SweepArgs<T> & a, int of, int og) : A(a), plane((size_t)of * a.ngroups + og) {}
-  __device__ size_t x(int k, int j) const { return ((plane * A.nz + k) * A.ny + j) * kGroup; }
-  __device__ size_t y(int k, int i) const { return ((plane * A.nz + k) * A.nx + i) * kGroup; }
-  __device__ size_t z(int j, int i) const { return ((plane * A.ny + j) * A.nx + i) * kGroup; }
+  __device__ size_t x(int k, int j) const { return ((plane * A.nz + k) * A.ny + j) * KG; }
+  __device__ size_t y(int k, int i) const { return ((plane * A.nz + k) * A.nx + i) * KG; }
+  __device__ size_t z(int j, int i) const { return ((plane * A.ny + j) * A.nx + i) * KG; }
 };
 
 // Done flag of block (bk, bj, bi) of a (group, octant, ordinate group) slot.
@@ -380,9 +383,10 @@ template <int DIMS, int TX>
 struct TaskSmemExact {
   static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
   static constexpr int CELLS = TX * PY * PZ;
-  static constexpr int YF = PZ * TX * kGroup;                  // y faces [PZ][TX][kGroup]
-  static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
-  static constexpr int NT = 2 * YF + 2 * ZF + 2 * CELLS + TX + PY + PZ + kGroup * (TX + PY + PZ);
+  static constexpr int KG = kGroupMax;                      // ordinate_group(DOMA_PREC_FP64, *)
+  static constexpr int YF = PZ * TX * KG;                  // y faces [PZ][TX][KG]
+  static constexpr int ZF = DIMS == 3 ? PY * TX * KG : 0;  // z faces [PY][TX][KG]
+  static constexpr int NT = 2 * YF + 2 * ZF + 2 * CELLS + TX + PY + PZ + KG * (TX + PY + PZ);
   static constexpr size_t bytes = NT * sizeof(double);
 };
 
@@ -392,7 +396,8 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
 {
   using T = double;
   using SM = TaskSmemExact<DIMS, TX>;
-  constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
+  constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS, KG = SM::KG;
+  static_assert(KG == ordinate_group(DOMA_PREC_FP64, SCHEME), "one ordinate-group size per mode");
   constexpr unsigned FULL = 0xffffffffu;
   const int og = task.og;
   const int o = task.oct;                 // octant: sweep directions
@@ -403,11 +408,11 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
   const T * gq = A.q + (size_t)task.grp * N;
   const T * gsig = A.sigt + (size_t)task.grp * N;
   const int Do = A.d_oct;
-  const int n0 = og * kGroup;
-  const int gs = min(kGroup, Do - n0);
+  const int n0 = og * KG;
+  const int gs = min(KG, Do - n0);
   const int i0 = task.bi * TX, j0 = task.bj * PY, k0 = task.bk * PZ;
   const int vx = min(TX, nx - i0), vy = min(PY, ny - j0), vz = min(PZ, nz - k0);
-  const FacePlanes<T> F(A, of, og);
+  const FacePlanes<T, KG> F(A, of, og);
 
   const int t = threadIdx.x;
   const int lane = t & 31;
@@ -428,9 +433,9 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
   T * lxs = ss + CELLS;
   T * lys = lxs + TX;
   T * lzs = lys + PY;
-  T * cxs = lzs + PZ;                 // [kGroup][TX]
-  T * cys = cxs + kGroup * TX;        // [kGroup][PY]
-  T * czs = cys + kGroup * PY;        // [kGroup][PZ]
+  T * cxs = lzs + PZ;                 // [KG][TX]
+  T * cys = cxs + KG * TX;        // [KG][PY]
+  T * czs = cys + KG * PY;        // [KG][PZ]
 
   auto phys_i = [&](int il) { return rx ? nx - 1 - (i0 + il) : i0 + il; };
   auto phys_j = [&](int jj) { return ry ? ny - 1 - (j0 + jj) : j0 + jj; };
@@ -449,16 +454,16 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
   for (int e = t; e < PY; e += blockDim.x) lys[e] = e < vy ? A.wy[phys_j(e)] : (T)1;
   if (DIMS == 3)
     for (int e = t; e < PZ; e += blockDim.x) lzs[e] = e < vz ? A.wz[phys_k(e)] : (T)1;
-  for (int e = t; e < kGroup * TX; e += blockDim.x) {
+  for (int e = t; e < KG * TX; e += blockDim.x) {
     const int nn = e / TX, il = e % TX;
     cxs[e] = (nn < gs && il < vx) ? A.cx[(size_t)(ob + nn) * nx + phys_i(il)] : (T)0;
   }
-  for (int e = t; e < kGroup * PY; e += blockDim.x) {
+  for (int e = t; e < KG * PY; e += blockDim.x) {
     const int nn = e / PY, jj = e % PY;
     cys[e] = (nn < gs && jj < vy) ? A.cy[(size_t)(ob + nn) * ny + phys_j(jj)] : (T)0;
   }
   if (DIMS == 3)
-    for (int e = t; e < kGroup * PZ; e += blockDim.x) {
+    for (int e = t; e < KG * PZ; e += blockDim.x) {
       const int nn = e / PZ, kk = e % PZ;
       czs[e] = (nn < gs && kk < vz) ? A.cz[(size_t)(ob + nn) * nz + phys_k(kk)] : (T)0;
     }
@@ -471,14 +476,14 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
 
   // -- incoming faces (written by other CTAs: read through L2) -----------------------
   for (int e = t; e < SM::YF; e += blockDim.x) {
-    const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
+    const int nn = e % KG, r = e / KG, il = r % TX, kk = r / TX;
     T v = (T)0;
     if (task.bj > 0 && nn < gs && il < vx && kk < vz) v = __ldcg(A.yf + F.y(k0 + kk, i0 + il) + nn);
     yin[e] = v;
   }
   if (DIMS == 3)
     for (int e = t; e < SM::ZF; e += blockDim.x) {
-      const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
+      const int nn = e % KG, r = e / KG, il = r % TX, jj = r / TX;
       T v = (T)0;
       if (task.bk > 0 && nn < gs && il < vx && jj < vy) v = __ldcg(A.zf + F.z(j0 + jj, i0 + il) + nn);
       zin[e] = v;
@@ -490,8 +495,8 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
 
   // -- wavefront: step s solves the cells with il + jl + kl == s, warp-synchronously --
   const int ebase = (kl * PY + jl) * TX;          // cell index of il = 0
-  const int ybase = kl * TX * kGroup + nl;        // y-face slot of il = 0
-  const int zbase = jl * TX * kGroup + nl;        // z-face slot of il = 0
+  const int ybase = kl * TX * KG + nl;        // y-face slot of il = 0
+  const int zbase = jl * TX * KG + nl;        // z-face slot of il = 0
   const int cxbase = nl * TX;
   const T cy_t = cys[nl * PY + jl];
   const T cz_t = DIMS == 3 ? czs[nl * PZ + kl] : (T)0;
@@ -505,9 +510,9 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
     const int il = s - jl - kl;
     const bool valid = active && (unsigned)il < (unsigned)vx;
     if (valid) {
-      T y = jl == 0 ? yin[ybase + il * kGroup] : ysh;
+      T y = jl == 0 ? yin[ybase + il * KG] : ysh;
       T z = (T)0;
-      if (DIMS == 3) z = kl == 0 ? zin[zbase + il * kGroup] : zsh;
+      if (DIMS == 3) z = kl == 0 ? zin[zbase + il * KG] : zsh;
       const int e = ebase + il;
       const T q = qs[e], st = ss[e];
       T psi;
@@ -530,8 +535,8 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
       A.wpsi[((size_t)task.grp * N + cg) * A.d_total + ord] = dM(wgt, psi);
       yo = y;
       zo = z;
-      if (jl == vy - 1) yout[ybase + il * kGroup] = y;
-      if (DIMS == 3 && kl == vz - 1) zout[zbase + il * kGroup] = z;
+      if (jl == vy - 1) yout[ybase + il * KG] = y;
+      if (DIMS == 3 && kl == vz - 1) zout[zbase + il * KG] = z;
     }
     ysh = __shfl_up_sync(FULL, yo, 1);
     if (DIMS == 3) zsh = __shfl_up_sync(FULL, zo, PY);
@@ -541,12 +546,12 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
   // -- outgoing faces -----------------------------------------------------------------
   if (active) A.xf[xslot] = xin;
   for (int e = t; e < SM::YF; e += blockDim.x) {
-    const int nn = e % kGroup, r = e / kGroup, il = r % TX, kk = r / TX;
+    const int nn = e % KG, r = e / KG, il = r % TX, kk = r / TX;
     if (nn < gs && il < vx && kk < vz) A.yf[F.y(k0 + kk, i0 + il) + nn] = yout[e];
   }
   if (DIMS == 3)
     for (int e = t; e < SM::ZF; e += blockDim.x) {
-      const int nn = e % kGroup, r = e / kGroup, il = r % TX, jj = r / TX;
+      const int nn = e % KG, r = e / KG, il = r % TX, jj = r / TX;
       if (nn < gs && il < vx && jj < vy) A.zf[F.z(j0 + jj, i0 + il) + nn] = zout[e];
     }
 
@@ -561,7 +566,7 @@ __device__ __forceinline__ void run_task_exact(const SweepArgs<double> & A, cons
 
 // ---- single precision -----------------------------------------------------------
 
-template <int DIMS, int TX>
+template <int DIMS, int TX, int KG>
 struct TaskSmemF32 {
   static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
   static constexpr int CELLS = TX * PY * PZ;
@@ -570,21 +575,21 @@ struct TaskSmemF32 {
   // plus s times the stride (a constant offset in the unrolled walk) with no
   // clamp; reads outside its pencil land in finite data it discards.
   static constexpr int SKEW = PY + PZ - 2;
-  static constexpr int FPAD = SKEW * kGroup;                   // face pad (floats), each side
-  static constexpr int YF = PZ * TX * kGroup;                  // y faces [PZ][TX][kGroup]
-  static constexpr int ZF = DIMS == 3 ? PY * TX * kGroup : 0;  // z faces [PY][TX][kGroup]
+  static constexpr int FPAD = SKEW * KG;                   // face pad (floats), each side
+  static constexpr int YF = PZ * TX * KG;                  // y faces [PZ][TX][KG]
+  static constexpr int ZF = DIMS == 3 ? PY * TX * KG : 0;  // z faces [PY][TX][KG]
   static constexpr int YREG = YF + 2 * FPAD;
   static constexpr int ZREG = DIMS == 3 ? ZF + 2 * FPAD : 0;
   static constexpr int CREG = 2 * (CELLS + 2 * SKEW);          // {q, sigma_t} per cell
-  static constexpr int HREG = kGroup * TX + 2 * SKEW;          // x coefficients [kGroup][TX]
+  static constexpr int HREG = KG * TX + 2 * SKEW;          // x coefficients [KG][TX]
   static constexpr int RREG = TX + 2 * SKEW;                   // 1/dx [TX] (2D TW-DD)
-  // The walk stores psi per ordinate and cell ([kGroup][CELLS]; weighted and
+  // The walk stores psi per ordinate and cell ([KG][CELLS]; weighted and
   // summed after the walk) -- or, for long blocks whose array would cost a CTA
-  // per SM, w psi summed over ordinate pairs across half-warps ([kGroup / 2][CELLS]).
+  // per SM, w psi summed over ordinate pairs across half-warps ([KG / 2][CELLS]).
   static constexpr bool PAIRS = CELLS >= 512;
-  static constexpr int PROWS = PAIRS ? kGroup / 2 : kGroup;
-  // floats: the padded regions, the ordinate weights [kGroup], then those sums
-  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + kGroup + PROWS * CELLS;
+  static constexpr int PROWS = PAIRS ? KG / 2 : KG;
+  // floats: the padded regions, the ordinate weights [KG], then those sums
+  static constexpr size_t floats = YREG + ZREG + CREG + HREG + RREG + KG + PROWS * CELLS;
   static constexpr size_t bytes = floats * sizeof(float);
   static_assert(FPAD % 4 == 0 && YREG % 4 == 0, "face regions stay float4-aligned");
   static_assert(CREG % 2 == 0 && (YREG + ZREG) % 2 == 0, "cell region stays float2-aligned");
@@ -616,7 +621,8 @@ template <int DIMS, int SCHEME, int TX, bool SKIP_IDLE = false>
 __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const Task task,
                                              unsigned char * smem_raw, bool dataflow, unsigned epoch)
 {
-  using SM = TaskSmemF32<DIMS, TX>;
+  constexpr int KG = ordinate_group(DOMA_PREC_FP32, SCHEME);
+  using SM = TaskSmemF32<DIMS, TX, KG>;
   constexpr int PY = SM::PY, PZ = SM::PZ, CELLS = SM::CELLS;
   constexpr unsigned FULL = 0xffffffffu;
   constexpr bool TW = SCHEME == DOMA_SCHEME_TW_DD;
@@ -630,11 +636,11 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
   const size_t N = (size_t)nx * ny * nz;
   const float * gq = A.q + (size_t)task.grp * N;
   const float * gsig = A.sigt + (size_t)task.grp * N;
-  const int n0 = og * kGroup;
-  const int gs = min(kGroup, A.d_oct - n0);
+  const int n0 = og * KG;
+  const int gs = min(KG, A.d_oct - n0);
   const int i0 = task.bi * TX, j0 = task.bj * PY, k0 = task.bk * PZ;
   const int vx = min(TX, nx - i0), vy = min(PY, ny - j0), vz = min(PZ, nz - k0);
-  const FacePlanes<float> F(A, of, og);
+  const FacePlanes<float, KG> F(A, of, og);
   const size_t slot = F.plane;
 
   const int t = threadIdx.x;
@@ -649,13 +655,13 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
 
   constexpr int SKEW = SM::SKEW, FPAD = SM::FPAD;
   float * const sbase = reinterpret_cast<float *>(smem_raw);
-  float * yin = sbase + FPAD;                                            // [PZ][TX][kGroup]
-  float * zin = sbase + SM::YREG + (DIMS == 3 ? FPAD : 0);               // [PY][TX][kGroup]
+  float * yin = sbase + FPAD;                                            // [PZ][TX][KG]
+  float * zin = sbase + SM::YREG + (DIMS == 3 ? FPAD : 0);               // [PY][TX][KG]
   float2 * cell = reinterpret_cast<float2 *>(sbase + SM::YREG + SM::ZREG) + SKEW;  // {q, sigma_t}
-  float * hxs = sbase + SM::YREG + SM::ZREG + SM::CREG + SKEW;           // [kGroup][TX]
+  float * hxs = sbase + SM::YREG + SM::ZREG + SM::CREG + SKEW;           // [KG][TX]
   float * rlx = hxs - SKEW + SM::HREG + SKEW;                            // [TX] 1/dx
-  float * wts = rlx - SKEW + SM::RREG;                                   // [kGroup] weights
-  float * P = wts + kGroup;                                              // [PROWS][CELLS]
+  float * wts = rlx - SKEW + SM::RREG;                                   // [KG] weights
+  float * P = wts + KG;                                              // [PROWS][CELLS]
   constexpr bool PAIRS = SM::PAIRS;
 
   // the pads: finite values for the reads of steps outside a lane's pencil
@@ -671,7 +677,7 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     cell[e - SKEW] = make_float2(0.f, 1.f);
     cell[CELLS + e] = make_float2(0.f, 1.f);
     hxs[e - SKEW] = 0.f;
-    hxs[kGroup * TX + e] = 0.f;
+    hxs[KG * TX + e] = 0.f;
     rlx[e - SKEW] = 0.f;
     rlx[TX + e] = 0.f;
   }
@@ -702,11 +708,11 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
       }
     }
   }
-  for (int e = t; e < kGroup * TX; e += blockDim.x) {
+  for (int e = t; e < KG * TX; e += blockDim.x) {
     const int nn = e / TX, il = e % TX;
     hxs[e] = (nn < gs && il < vx) ? fM(HS, A.cx[(size_t)(ob + nn) * nx + phys_i(il)]) : 0.f;
   }
-  for (int e = t; e < kGroup; e += blockDim.x) wts[e] = e < gs ? (float)A.wgt[ob + e] : 0.f;
+  for (int e = t; e < KG; e += blockDim.x) wts[e] = e < gs ? (float)A.wgt[ob + e] : 0.f;
   if (DIMS == 2 && TW)
     for (int e = t; e < TX; e += blockDim.x) rlx[e] = e < vx ? __frcp_rn(A.wx[phys_i(e)]) : 0.f;
   // per-thread constants of the pencil (clamped indices for inactive lanes)
@@ -721,14 +727,14 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
 
   // -- incoming faces: every load issued before the first store ----------------------
   {
-    constexpr int Y4 = SM::YF / 4, R4 = TX * kGroup / 4;   // float4s per block / per row
+    constexpr int Y4 = SM::YF / 4, R4 = TX * KG / 4;   // float4s per block / per row
     float xin_v = 0.f;
     const size_t xslot = F.x(k0 + kl, j0 + jl) + nl;
     if (active && task.bi > 0) xin_v = __ldcg(A.xf + xslot);
     stage_f4<Y4>(reinterpret_cast<float4 *>(yin), [&](int e) {
       const int kk = e / R4, r = e % R4;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (task.bj > 0 && kk < vz && r / (kGroup / 4) < vx)
+      if (task.bj > 0 && kk < vz && r / (KG / 4) < vx)
         v = __ldcg(reinterpret_cast<const float4 *>(A.yf + F.y(k0 + kk, i0)) + r);
       return v;
     });
@@ -736,7 +742,7 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
       stage_f4<SM::ZF / 4>(reinterpret_cast<float4 *>(zin), [&](int e) {
         const int jj = e / R4, r = e % R4;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (task.bk > 0 && jj < vy && r / (kGroup / 4) < vx)
+        if (task.bk > 0 && jj < vy && r / (KG / 4) < vx)
           v = __ldcg(reinterpret_cast<const float4 *>(A.zf + F.z(j0 + jj, i0)) + r);
         return v;
       });
@@ -750,8 +756,8 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const int d = jl + kl;
     const int ebase = (kl * PY + jl) * TX;
     // per-lane bases shifted by -d: step s reads element s of the lane's row
-    const float * yin_l = yin + (kl * TX - d) * kGroup + nl;
-    const float * zin_l = zin + (jl * TX - d) * kGroup + nl;
+    const float * yin_l = yin + (kl * TX - d) * KG + nl;
+    const float * zin_l = zin + (jl * TX - d) * KG + nl;
     const float2 * cell_l = cell + (ebase - d);
     const float * hx_l = hxs + (nl * TX - d);
     const float * rlx_l = rlx - d;
@@ -760,7 +766,7 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
     float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl : nullptr;
     float * P_lane = P + (PAIRS ? nl >> 1 : nl) * CELLS + ebase;
-    const float wgt = PAIRS ? wts[min(nl, kGroup - 1)] : 0.f;
+    const float wgt = PAIRS ? wts[min(nl, KG - 1)] : 0.f;
     float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
     // SKIP_IDLE (the batched kernel): a warp whose two ordinates both lie
@@ -777,11 +783,11 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
       const int il = s - d;
       const bool valid = active && (unsigned)il < (unsigned)vx;
       // unconditional loads (the padded rows are always in range), then a select
-      const float yl = yin_l[s * kGroup];
+      const float yl = yin_l[s * KG];
       float y = jl == 0 ? yl : ysh;
       float z = 0.f;
       if constexpr (DIMS == 3) {
-        const float zl = zin_l[s * kGroup];
+        const float zl = zin_l[s * KG];
         z = kl == 0 ? zl : zsh;
       }
       const float2 qc = cell_l[s];
@@ -795,8 +801,8 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
         else psi = dd2_fast(qc.x, qc.y, hx, cy_t, xo, y);
       }
       x = valid ? xo : x;
-      st_global_if(yout_g + il * kGroup, y, valid && ybound);
-      if constexpr (DIMS == 3) st_global_if(zout_g + il * kGroup, z, valid && zbound);
+      st_global_if(yout_g + il * KG, y, valid && ybound);
+      if constexpr (DIMS == 3) st_global_if(zout_g + il * KG, z, valid && zbound);
       if constexpr (PAIRS) {
         // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
         const float wp = valid ? fM(wgt, psi) : 0.f;
@@ -859,21 +865,22 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 // Resident CTAs per SM the kernels are compiled for (caps the registers of
 // the single-precision body, whose unrolled wavefront would otherwise take
 // every register it can).  Measured on GB300 (64^3, 16 ordinates per
-// octant): DD is fastest with 4 CTAs per SM (64 registers), TW-DD, with more
-// live values per cell, with 3 (80 registers).
+// octant): DD is fastest at the budget of 6 full-size CTAs per SM (40
+// registers; its 8-ordinate CTAs have 128 threads, so 12 of them fit), TW-DD,
+// with more live values per cell, at 3 (80 registers).
 template <typename T, int SCHEME>
 constexpr int sweep_min_ctas()
 {
-  return std::is_same<T, double>::value ? 1
+  return std::is_same<T, double>::value ? DOMA_SWEEP_MIN_CTAS_FP64
          : SCHEME == DOMA_SCHEME_DD     ? DOMA_SWEEP_MIN_CTAS_DD
                                         : DOMA_SWEEP_MIN_CTAS;
 }
 
-template <typename T, int DIMS, int TX>
+template <typename T, int DIMS, int SCHEME, int TX>
 constexpr size_t task_smem_bytes()
 {
   if constexpr (std::is_same<T, double>::value) return TaskSmemExact<DIMS, TX>::bytes;
-  else return TaskSmemF32<DIMS, TX>::bytes;
+  else return TaskSmemF32<DIMS, TX, ordinate_group(DOMA_PREC_FP32, SCHEME)>::bytes;
 }
 
 // Persistent dataflow sweep: CTAs claim tasks in topological order from a
@@ -1033,9 +1040,9 @@ int sweep_tile_x(int requested)
 
 size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx)
 {
-  return dispatch(dims, precision, scheme, tx, [](auto tag_t, auto dims_c, auto, auto tx_c) {
+  return dispatch(dims, precision, scheme, tx, [](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
     using T = typename decltype(tag_t)::type;
-    return task_smem_bytes<T, decltype(dims_c)::value, decltype(tx_c)::value>();
+    return task_smem_bytes<T, decltype(dims_c)::value, decltype(sch_c)::value, decltype(tx_c)::value>();
   });
 }
 
@@ -1083,10 +1090,12 @@ auto dispatch_batch(int dims, int scheme, F && f)
   return by_scheme(std::integral_constant<int, 3>{});
 }
 
-size_t sweep_batch_smem_bytes(int dims)
+size_t sweep_batch_smem_bytes(int dims, int scheme)
 {
   // the largest block length's layout serves all three
-  return dims == 2 ? task_smem_bytes<float, 2, 32>() : task_smem_bytes<float, 3, 32>();
+  return dispatch_batch(dims, scheme, [](auto dims_c, auto sch_c) {
+    return task_smem_bytes<float, decltype(dims_c)::value, decltype(sch_c)::value, 32>();
+  });
 }
 
 doma_status launch_sweep_batch(int dims, int scheme, int grid, int threads, size_t smem,

@@ -85,13 +85,15 @@ def test_fp64_matches_oracle_random(seed, scheme, dims):
 @pytest.mark.parametrize("tile", [(8, 0, 0), (16, 0, 0), (32, 0, 0)])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 @pytest.mark.parametrize("dims", [2, 3])
-def test_block_shape_does_not_change_results(tile, precision, dims):
+@pytest.mark.parametrize("scheme", ["tw_dd", "dd"])
+def test_block_shape_does_not_change_results(tile, precision, dims, scheme):
     """Every block length, with ragged edge blocks in every axis and a
-    partial ordinate group (9 ordinates per octant), gives the same bits."""
+    partial ordinate group (9 ordinates per octant: one partial group of 16,
+    or in FP32 DD a full group of 8 and a partial one), gives the same bits."""
     p = P.random_problem(31, dims, 37, 19, 7, groups=2, np_=3, na=3, materials=3)
-    base = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-9, mg_tol=1e-9)
+    base = P.make_options(scheme=scheme, precision=precision, fs_tol=1e-9, mg_tol=1e-9)
     ref_phi, _ = run(p, base)
-    opts = P.make_options(scheme="tw_dd", precision=precision, fs_tol=1e-9, mg_tol=1e-9,
+    opts = P.make_options(scheme=scheme, precision=precision, fs_tol=1e-9, mg_tol=1e-9,
                           tile=tile)
     phi, _ = run(p, opts)
     assert np.array_equal(phi, ref_phi)
