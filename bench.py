@@ -376,9 +376,9 @@ def roofline_entry(ms: float, updates: float, d_oct: int, s_bytes: int, peak: fl
 
 # DRAM traffic of one sweep launch on the 100^3, 288-direction duct problem
 # (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture).  The
-# 192 MB of double partials (3 ordinate groups x 8 octants x 10^6 cells) no
-# longer fit in L2, so most of it is their write-back.
-STREAMING_SWEEP_DRAM_BYTES = 34_532_864 + 262_337_536
+# 320 MB of double partials (5 ordinate groups of 8 x 8 octants x 10^6 cells)
+# do not fit in L2, so most of it is their write-back.
+STREAMING_SWEEP_DRAM_BYTES = 36_372_224 + 437_900_032
 
 
 def streaming_leg(args, stream, flush):

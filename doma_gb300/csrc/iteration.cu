@@ -17,6 +17,7 @@
 
 #include "common.cuh"
 #include "iteration.cuh"
+#include "loop_control.cuh"
 
 namespace doma {
 namespace {
@@ -83,18 +84,6 @@ __device__ __forceinline__ bool finish_norms(double a, double b, double * partia
     return true;
   }
   return false;
-}
-
-// DOMA's relative norm (src/TransportSolver3D.cpp:562): sqrt(diff)/sqrt(total),
-// or 0 when total <= 1e-8.  IEEE sqrt and division, the same bits as the host.
-__device__ __forceinline__ double norm_ratio(double diff, double tot)
-{
-  return tot > 1e-8 ? __ddiv_rn(__dsqrt_rn(diff), __dsqrt_rn(tot)) : 0.0;
-}
-
-__device__ __forceinline__ bool finite2(double a, double b)
-{
-  return isfinite(a) && isfinite(b);
 }
 
 // updateMultigroupSource for group g (fixed source: external, in-scatter and
@@ -360,26 +349,7 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
   }
   if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
     // sourceIteration's loop test (src/TransportSolver3D.cpp:481), on the device
-    LoopCtl * C = L.ctl;
-    const double res = norm_ratio(norms[0], norms[1]);
-    const unsigned it = ++C->si_it;
-    ++C->sweeps;
-    if (L.si_hist && C->hist_len < L.hist_cap) L.si_hist[C->hist_len] = res;
-    ++C->hist_len;
-    C->si_res = res;
-    const bool ok = finite2(norms[0], norms[1]) && C->error == 0;
-    const bool more = ok && it < L.fs_max_it && L.fs_tol < res;
-    if (!more) {
-      if (C->pairs < L.pair_cap) {
-        L.pair_counts[C->pairs] = it;
-        L.pair_res[C->pairs] = res;
-      }
-      ++C->pairs;
-      if (C->error != 0) C->failed = DOMA_DEVICE_WAIT_TIMEOUT;
-      else if (!ok) C->failed = DOMA_NUMERIC_ERROR;
-      else if (!(it < L.fs_max_it)) C->failed = DOMA_NOT_CONVERGED;
-    }
-    cudaGraphSetConditional(L.si_handle, more ? 1u : 0u);
+    si_loop_control(L, norms);
   }
 }
 
@@ -499,26 +469,7 @@ __global__ void __launch_bounds__(kBlock) mgi_epilogue_kernel(const IterArgs A, 
        c += (size_t)gridDim.x * blockDim.x)
     mgi_cell(A, c, q, dscratch, diff, tot);
   if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
-    LoopCtl * C = L.ctl;
-    const double res = norm_ratio(norms[0], norms[1]);
-    const unsigned it = ++C->si_it;
-    ++C->sweeps;
-    if (L.si_hist && C->hist_len < L.hist_cap) L.si_hist[C->hist_len] = res;
-    ++C->hist_len;
-    C->si_res = res;
-    const bool ok = finite2(norms[0], norms[1]) && C->error == 0;
-    const bool more = ok && it < L.fs_max_it && L.fs_tol < res;
-    if (!more) {
-      if (C->pairs < L.pair_cap) {
-        L.pair_counts[C->pairs] = it;
-        L.pair_res[C->pairs] = res;
-      }
-      ++C->pairs;
-      if (C->error != 0) C->failed = DOMA_DEVICE_WAIT_TIMEOUT;
-      else if (!ok) C->failed = DOMA_NUMERIC_ERROR;
-      else if (!(it < L.fs_max_it)) C->failed = DOMA_NOT_CONVERGED;
-    }
-    cudaGraphSetConditional(L.si_handle, more ? 1u : 0u);
+    si_loop_control(L, norms);
   }
 }
 

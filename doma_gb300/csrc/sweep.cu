@@ -43,7 +43,10 @@
 #include "common.cuh"
 
 #ifndef DOMA_SWEEP_MIN_CTAS_DD
-#define DOMA_SWEEP_MIN_CTAS_DD 6
+#define DOMA_SWEEP_MIN_CTAS_DD 12
+#endif
+#ifndef DOMA_SWEEP_BATCH_MIN_CTAS_DD
+#define DOMA_SWEEP_BATCH_MIN_CTAS_DD 8
 #endif
 #ifndef DOMA_SWEEP_MIN_CTAS_FP64
 #define DOMA_SWEEP_MIN_CTAS_FP64 1
@@ -862,18 +865,35 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
     run_task_f32<DIMS, SCHEME, TX, SKIP_IDLE>(A, task, smem_raw, dataflow, epoch);
 }
 
-// Resident CTAs per SM the kernels are compiled for (caps the registers of
-// the single-precision body, whose unrolled wavefront would otherwise take
-// every register it can).  Measured on GB300 (64^3, 16 ordinates per
-// octant): DD is fastest at the budget of 6 full-size CTAs per SM (40
-// registers; its 8-ordinate CTAs have 128 threads, so 12 of them fit), TW-DD,
-// with more live values per cell, at 3 (80 registers).
+// Threads of a full sweep CTA (16 pencils x the ordinate-group size) and the
+// resident CTAs per SM the kernels are compiled for, which cap the registers
+// of the single-precision body (its unrolled wavefront would otherwise take
+// every register it can).  Measured on GB300: FP32 DD (128-thread CTAs) at
+// 12 per SM, 40 registers (64^3 and the 100^3 duct; 8 per SM, 64 registers,
+// is faster at 64^3 and slower on the duct); FP32 TW-DD (256 threads), with
+// more live values per cell, at 3, 80 registers; FP64 at 1 (2 and 3 per SM
+// were 19 % and 38 % slower: the FP64 pipe is the limit).
+template <typename T, int SCHEME>
+constexpr int sweep_cta_threads()
+{
+  return 16 * ordinate_group(std::is_same<T, double>::value ? DOMA_PREC_FP64 : DOMA_PREC_FP32, SCHEME);
+}
+
 template <typename T, int SCHEME>
 constexpr int sweep_min_ctas()
 {
   return std::is_same<T, double>::value ? DOMA_SWEEP_MIN_CTAS_FP64
          : SCHEME == DOMA_SCHEME_DD     ? DOMA_SWEEP_MIN_CTAS_DD
                                         : DOMA_SWEEP_MIN_CTAS;
+}
+
+// The batched kernel holds every block length's body; at 40 registers its DD
+// form spills, and 8 CTAs per SM (64 registers) solved the 256-problem mix
+// 2.4 % faster than 12.
+template <typename T, int SCHEME>
+constexpr int sweep_batch_min_ctas()
+{
+  return SCHEME == DOMA_SCHEME_DD ? DOMA_SWEEP_BATCH_MIN_CTAS_DD : sweep_min_ctas<T, SCHEME>();
 }
 
 template <typename T, int DIMS, int SCHEME, int TX>
@@ -887,7 +907,7 @@ constexpr size_t task_smem_bytes()
 // ticket counter; a claimed task waits only on tasks with smaller tickets,
 // which running CTAs already hold, so progress never depends on residency.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
+__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_min_ctas<T, SCHEME>())
     sweep_persistent_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -921,7 +941,7 @@ __global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
 // every problem of a batch.  Tasks of problems that have converged publish
 // their done flag and return, so a batch keeps one static task list.
 template <typename T, int DIMS, int SCHEME>
-__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
+__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_batch_min_ctas<T, SCHEME>())
     sweep_batch_kernel(const SweepArgs<T> * args, const BatchTask * tasks, int num_tasks,
                        unsigned * ticket, unsigned * exit_count, unsigned * epoch_ctr,
                        const BatchLoop * loops)
@@ -967,7 +987,7 @@ __global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
 
 // One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
 template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(kMaxSweepThreads, sweep_min_ctas<T, SCHEME>())
+__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_min_ctas<T, SCHEME>())
     sweep_level_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
