@@ -49,6 +49,32 @@ __host__ __device__ constexpr int ordinate_group(int precision, int scheme)
   return precision == DOMA_PREC_FP32 && scheme == DOMA_SCHEME_DD ? 8 : kGroupMax;
 }
 
+#ifdef __CUDACC__
+// FP32 mode's scalar-flux partial of one (group, octant, ordinate group) slot
+// is the slot's Kahan sum kept as the unevaluated float pair hi + lo (hi =
+// the sum, lo = minus its compensation).  The epilogues add a cell's slots in
+// slot order in double-float arithmetic (a float pair carrying about 48
+// significant bits): Knuth's TwoSum of the high parts, the low parts added,
+// and Dekker's FastTwoSum to renormalise -- the "sloppy" double-float
+// addition of Hida, Li and Bailey's quad-double library.  It runs on the FP32
+// pipes, which GB300 issues 64 times as fast as FP64 adds, where a cell's 8
+// to 40 FP64 adds made the epilogues FP64-bound.  Every kernel that reads the
+// partials uses this accumulator, so they all give the same bits.
+struct PartialSum {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add(float2 p)
+  {
+    const float s = __fadd_rn(h, p.x);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(p.x, bb));
+    const float t = __fadd_rn(e, __fadd_rn(l, p.y));
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+  }
+  __device__ __forceinline__ double value() const { return __dadd_rn((double)h, (double)l); }
+};
+#endif
+
 // One sweep task: energy group (multigroup mode; 0 otherwise), octant,
 // ordinate group and block coordinates in the octant's sweep frame
 // (i' = i for +mu, nx-1-i for -mu, likewise for y and z).
@@ -110,7 +136,7 @@ struct SweepArgs {
   T * yf;
   T * zf;
   double * wpsi;     // exact mode: [groups in flight][N][d_total] weighted angular flux
-  double * octphi;   // fp32 mode: [G*8*ngroups][N] scalar-flux partials per (group, octant, ordinate group)
+  float2 * octphi;   // fp32 mode: [G*8*ngroups][N] scalar-flux partials (hi, lo) per (group, octant, ordinate group)
   double theta;
   // persistent-mode scheduling state (device memory, kept between sweeps)
   unsigned * ticket;      // next task to claim (reset by the last CTA to leave)

@@ -331,20 +331,20 @@ __global__ void __launch_bounds__(kBlock) si_epilogue_kernel(const IterArgs A, i
     }
   } else {
     // two of the thread's cells per pass: their slot sums are independent
-    // chains of FP64 adds, interleaved; the cells still finish in order
+    // chains, interleaved; the cells still finish in order
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N; c += 2 * stride) {
       const size_t c2 = c + stride;
       const bool two = c2 < N;
-      double da = 0.0, db = 0.0;
+      PartialSum sa, sb;
       for (int o = 0; o < 8; ++o)
         if (A.oct_mask & (1 << o))
           for (int og = 0; og < A.ngroups; ++og) {
-            const double * part = A.octphi + ((size_t)o * A.ngroups + og) * N;
-            da = dA(da, part[c]);
-            if (two) db = dA(db, part[c2]);
+            const float2 * part = A.octphi + ((size_t)o * A.ngroups + og) * N;
+            sa.add(part[c]);
+            if (two) sb.add(part[c2]);
           }
-      finish(c, da);
-      if (two) finish(c2, db);
+      finish(c, sa.value());
+      if (two) finish(c2, sb.value());
     }
   }
   if (finish_norms(diff, tot, A.partials, A.ticket, norms) && L.graph) {
@@ -431,10 +431,12 @@ __device__ __forceinline__ void mgi_cell(const IterArgs & A, size_t c, T * q, do
       const double * w = A.wpsi + ((size_t)g * N + c) * (size_t)A.D;
       for (int k = 0; k < A.D; ++k) d = dA(d, w[k]);
     } else {
+      PartialSum ps;
       for (int o = 0; o < 8; ++o)
         if (A.oct_mask & (1 << o))
           for (int og = 0; og < A.ngroups; ++og)
-            d = dA(d, A.octphi[((size_t)g * per_group + (size_t)o * A.ngroups + og) * N + c]);
+            ps.add(A.octphi[((size_t)g * per_group + (size_t)o * A.ngroups + og) * N + c]);
+      d = ps.value();
     }
     double * ph = A.phi + (size_t)g * N + c;
     const double t = dA(*ph, d);

@@ -32,7 +32,7 @@ struct IterArgs {
   double * phi = nullptr;             // [G][N]
   double * prev = nullptr;            // [G][N]
   const double * wpsi = nullptr;      // exact: [groups in flight][N][D]
-  const double * octphi = nullptr;    // fp32: [8 * ngroups][N]
+  const float2 * octphi = nullptr;    // fp32: [8 * ngroups][N] partials (hi, lo), see PartialSum
   double * partials = nullptr;        // [grid][2]
   unsigned * ticket = nullptr;        // last-block ticket (kept at 0 between launches)
   // Multigroup mode, the iteration after a learned correction Delta ([G][N]):

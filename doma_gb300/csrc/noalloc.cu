@@ -132,16 +132,16 @@ __global__ void noalloc_tables(const double * quad, int D, const double * w, int
 
 // phi = sum of the (octant, ordinate group) partials, in slot order: the
 // same order as the solver's source-iteration epilogue.
-__global__ void noalloc_reduce(const double * octphi, size_t N, unsigned oct_mask, int ngroups,
+__global__ void noalloc_reduce(const float2 * octphi, size_t N, unsigned oct_mask, int ngroups,
                                double * phi)
 {
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < N;
        c += (size_t)gridDim.x * blockDim.x) {
-    double d = 0.0;
+    PartialSum ps;
     for (int o = 0; o < 8; ++o)
       if (oct_mask & (1u << o))
-        for (int g = 0; g < ngroups; ++g) d = __dadd_rn(d, octphi[((size_t)o * ngroups + g) * N + c]);
-    phi[c] = __dadd_rn(0.0, d);
+        for (int g = 0; g < ngroups; ++g) ps.add(octphi[((size_t)o * ngroups + g) * N + c]);
+    phi[c] = __dadd_rn(0.0, ps.value());
   }
 }
 
@@ -246,7 +246,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   const size_t o_xf = cv.take(sizeof(float) * 8 * (size_t)nz * ny * slots);
   const size_t o_yf = cv.take(sizeof(float) * 8 * (size_t)nz * nx * slots);
   const size_t o_zf = cv.take(sizeof(float) * 8 * (size_t)ny * nx * slots);
-  const size_t o_oct = cv.take(sizeof(double) * 8 * (size_t)ngroups * N);
+  const size_t o_oct = cv.take(sizeof(float2) * 8 * (size_t)ngroups * N);
   if (cv.off > (size_t)DOMA_NOALLOC_SCRATCH_BYTES)
     return fail("the no-alloc sweep needs " + std::to_string(cv.off) + " bytes of scratch; it has " +
                 std::to_string((size_t)DOMA_NOALLOC_SCRATCH_BYTES));
@@ -301,7 +301,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   a.yf = reinterpret_cast<float *>(base + o_yf);
   a.zf = reinterpret_cast<float *>(base + o_zf);
   a.wpsi = nullptr;
-  a.octphi = reinterpret_cast<double *>(base + o_oct);
+  a.octphi = reinterpret_cast<float2 *>(base + o_oct);
   a.theta = theta;
   NoallocCtl * ctl = reinterpret_cast<NoallocCtl *>(base + o_ctl);
   a.ticket = &ctl->ticket;

@@ -77,7 +77,7 @@ struct doma_solver {
   void *d_q = nullptr, *d_sigt = nullptr;
   void *d_xf = nullptr, *d_yf = nullptr, *d_zf = nullptr;
   double * d_wpsi = nullptr;
-  double * d_octphi = nullptr;
+  float2 * d_octphi = nullptr;
   void *d_wx = nullptr, *d_wy = nullptr, *d_wz = nullptr;   // widths, sweep precision
   void *d_cx = nullptr, *d_cy = nullptr, *d_cz = nullptr;   // 2|cosine|/width tables
   double * d_partials = nullptr;

@@ -850,7 +850,7 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
         sum = tv;
       }
       const size_t cg = ((size_t)phys_k(kk) * ny + phys_j(jj)) * nx + phys_i(il);
-      A.octphi[slot * N + cg] = (double)sum - (double)comp;
+      A.octphi[slot * N + cg] = make_float2(sum, -comp);   // sum - comp, unevaluated
     }
   }
 }
