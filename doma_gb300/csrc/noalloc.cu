@@ -317,9 +317,11 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   sc.persistent = true;
   sc.threads = sweep_threads(std::min(kg, d_oct));
   sc.smem = sweep_smem_bytes(dims, DOMA_PREC_FP32, (int)scheme, tx);
-  st = sweep_prepare(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.smem);
+  sc.many = sweep_many_ctas(DOMA_PREC_FP32, (int)scheme, ngroups);
+  st = sweep_prepare(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.smem, sc.many);
   if (st != DOMA_OK) return st;
-  const int fit = sweep_resident_ctas(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.threads, sc.smem);
+  const int fit = sweep_resident_ctas(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.threads, sc.smem,
+                                      sc.many);
   if (fit <= 0) return fail("the sweep block does not fit on this device");
   sc.grid = std::max(1, std::min<int>(fit, (int)num_tasks));
   st = launch_sweep(dims, DOMA_PREC_FP32, (int)scheme, sc, nullptr, &a, s, nullptr);

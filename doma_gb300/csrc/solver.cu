@@ -246,6 +246,13 @@ void build_schedule(doma_solver * s)
   sc.nbz = (s->nz + sc.tz - 1) / sc.tz;
   sc.threads = sweep_threads(sc.gs);
   sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx);
+  sc.many = sweep_many_ctas(s->opts.precision, s->opts.scheme, sc.ngroups);
+  {
+    // DOMA_SWEEP_MANY=0/1 picks the FP32 DD body by hand (the tests run both)
+    const char * env = std::getenv("DOMA_SWEEP_MANY");
+    if (env && s->opts.precision == DOMA_PREC_FP32 && s->opts.scheme == DOMA_SCHEME_DD)
+      sc.many = std::string(env) == "1";
+  }
   const int levels = sc.nbx + sc.nby + sc.nbz - 2;
   std::vector<std::vector<Task>> by_level(levels);
   for (int g = 0; g < s->gif; ++g)
@@ -416,13 +423,13 @@ doma_status create_impl(const doma_problem * p, const doma_options * o, doma_sol
   pick_tile(s, o);
   build_schedule(s);
   if (s->sched.smem > 227 * 1024) return bad("sweep block needs too much shared memory");
-  DOMA_TRY(sweep_prepare(s->dims, o->precision, o->scheme, s->sched.tx, s->sched.smem));
+  DOMA_TRY(sweep_prepare(s->dims, o->precision, o->scheme, s->sched.tx, s->sched.smem, s->sched.many));
   DOMA_TRY(upload(s, &s->d_tasks, s->sched.tasks.data(), s->sched.tasks.size()));
   {
     const char * env = std::getenv("DOMA_SWEEP_SCHEDULE");
     s->sched.persistent = !(env && std::string(env) == "levels");
     const int fit = sweep_resident_ctas(s->dims, o->precision, o->scheme, s->sched.tx,
-                                        s->sched.threads, s->sched.smem);
+                                        s->sched.threads, s->sched.smem, s->sched.many);
     if (fit <= 0) return bad("the sweep block does not fit on this device");
     s->sched.grid = std::max(1, std::min<int>(fit, (int)s->sched.tasks.size()));
     // one flag per (octant slot, block): indexed by octant 0..7 even when
@@ -2040,7 +2047,8 @@ doma_status reschedule(doma_solver * s, int tx)
   s->opts.tile_x = (uint32_t)tx;
   pick_tile(s, &s->opts);
   build_schedule(s);
-  DOMA_TRY(sweep_prepare(s->dims, s->opts.precision, s->opts.scheme, s->sched.tx, s->sched.smem));
+  DOMA_TRY(sweep_prepare(s->dims, s->opts.precision, s->opts.scheme, s->sched.tx, s->sched.smem,
+                         s->sched.many));
   sfree(s, s->d_tasks);
   sfree(s, s->d_done);
   DOMA_TRY(upload(s, &s->d_tasks, s->sched.tasks.data(), s->sched.tasks.size()));
@@ -2048,7 +2056,7 @@ doma_status reschedule(doma_solver * s, int tx)
   DOMA_TRY(dalloc(s, &s->d_done, flags));
   DOMA_CUDA_TRY(cudaMemset(s->d_done, 0, flags * sizeof(unsigned)));
   const int fit = sweep_resident_ctas(s->dims, s->opts.precision, s->opts.scheme, s->sched.tx,
-                                      s->sched.threads, s->sched.smem);
+                                      s->sched.threads, s->sched.smem, s->sched.many);
   s->sched.grid = std::max(1, std::min<int>(fit, (int)s->sched.tasks.size()));
   for (auto * a : {&s->a32}) {
     a->nbx = s->sched.nbx; a->nby = s->sched.nby; a->nbz = s->sched.nbz;

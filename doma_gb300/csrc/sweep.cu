@@ -43,7 +43,10 @@
 #include "common.cuh"
 
 #ifndef DOMA_SWEEP_MIN_CTAS_DD
-#define DOMA_SWEEP_MIN_CTAS_DD 12
+#define DOMA_SWEEP_MIN_CTAS_DD 8
+#endif
+#ifndef DOMA_SWEEP_MIN_CTAS_DD_MANY
+#define DOMA_SWEEP_MIN_CTAS_DD_MANY 12
 #endif
 #ifndef DOMA_SWEEP_BATCH_MIN_CTAS_DD
 #define DOMA_SWEEP_BATCH_MIN_CTAS_DD 8
@@ -868,22 +871,28 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 // Threads of a full sweep CTA (16 pencils x the ordinate-group size) and the
 // resident CTAs per SM the kernels are compiled for, which cap the registers
 // of the single-precision body (its unrolled wavefront would otherwise take
-// every register it can).  Measured on GB300: FP32 DD (128-thread CTAs) at
-// 12 per SM, 40 registers (64^3 and the 100^3 duct; 8 per SM, 64 registers,
-// is faster at 64^3 and slower on the duct); FP32 TW-DD (256 threads), with
-// more live values per cell, at 3, 80 registers; FP64 at 1 (2 and 3 per SM
-// were 19 % and 38 % slower: the FP64 pipe is the limit).
+// every register it can).  Measured on GB300:
+//   * FP32 DD (128-thread CTAs) has two bodies.  At 8 CTAs per SM (64
+//     registers) the 48^3 and 64^3 sweeps with 16 ordinates per octant (two
+//     ordinate groups) take 115 and 196 us, against 143 and 219 us at 12 per
+//     SM (40 registers).  The 100^3 duct with 36 ordinates per octant (five
+//     groups: more independent tasks per wavefront level) is the other way
+//     round, 1542 against 1369 us.  MANY selects the 12-CTA body; solvers take
+//     it from three ordinate groups per octant up (sweep_many_ctas).
+//   * FP32 TW-DD (256 threads), with more live values per cell: 3, 80 registers.
+//   * FP64: 1 (2 and 3 per SM were 19 % and 38 % slower; the FP64 pipe is the limit).
+// Both DD bodies run the same instructions on the same values: the same bits.
 template <typename T, int SCHEME>
 constexpr int sweep_cta_threads()
 {
   return 16 * ordinate_group(std::is_same<T, double>::value ? DOMA_PREC_FP64 : DOMA_PREC_FP32, SCHEME);
 }
 
-template <typename T, int SCHEME>
+template <typename T, int SCHEME, bool MANY = false>
 constexpr int sweep_min_ctas()
 {
   return std::is_same<T, double>::value ? DOMA_SWEEP_MIN_CTAS_FP64
-         : SCHEME == DOMA_SCHEME_DD     ? DOMA_SWEEP_MIN_CTAS_DD
+         : SCHEME == DOMA_SCHEME_DD     ? (MANY ? DOMA_SWEEP_MIN_CTAS_DD_MANY : DOMA_SWEEP_MIN_CTAS_DD)
                                         : DOMA_SWEEP_MIN_CTAS;
 }
 
@@ -896,6 +905,13 @@ constexpr int sweep_batch_min_ctas()
   return SCHEME == DOMA_SCHEME_DD ? DOMA_SWEEP_BATCH_MIN_CTAS_DD : sweep_min_ctas<T, SCHEME>();
 }
 
+// Only FP32 DD has a second body.
+template <typename T, int SCHEME>
+constexpr bool has_many_body()
+{
+  return !std::is_same<T, double>::value && SCHEME == DOMA_SCHEME_DD;
+}
+
 template <typename T, int DIMS, int SCHEME, int TX>
 constexpr size_t task_smem_bytes()
 {
@@ -906,8 +922,8 @@ constexpr size_t task_smem_bytes()
 // Persistent dataflow sweep: CTAs claim tasks in topological order from a
 // ticket counter; a claimed task waits only on tasks with smaller tickets,
 // which running CTAs already hold, so progress never depends on residency.
-template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_min_ctas<T, SCHEME>())
+template <typename T, int DIMS, int SCHEME, int TX, bool MANY>
+__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_min_ctas<T, SCHEME, MANY>())
     sweep_persistent_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -986,20 +1002,20 @@ __global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_batch_mi
 }
 
 // One launch per level (level = bi + bj + bk): ordering by kernel boundaries.
-template <typename T, int DIMS, int SCHEME, int TX>
-__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_min_ctas<T, SCHEME>())
+template <typename T, int DIMS, int SCHEME, int TX, bool MANY>
+__global__ void __launch_bounds__(sweep_cta_threads<T, SCHEME>(), sweep_min_ctas<T, SCHEME, MANY>())
     sweep_level_kernel(const SweepArgs<T> A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   run_task<T, DIMS, SCHEME, TX>(A, A.tasks[A.task_offset + blockIdx.x], smem_raw, false, 0u);
 }
 
-template <typename T, int DIMS, int SCHEME, int TX>
+template <typename T, int DIMS, int SCHEME, int TX, bool MANY>
 doma_status launch_impl(const Schedule & s, const SweepArgs<T> & args, cudaStream_t stream,
                         uint64_t * launches)
 {
   if (s.persistent) {
-    sweep_persistent_kernel<T, DIMS, SCHEME, TX><<<s.grid, s.threads, s.smem, stream>>>(args);
+    sweep_persistent_kernel<T, DIMS, SCHEME, TX, MANY><<<s.grid, s.threads, s.smem, stream>>>(args);
     if (launches) ++*launches;
   } else {
     SweepArgs<T> a = args;
@@ -1008,7 +1024,7 @@ doma_status launch_impl(const Schedule & s, const SweepArgs<T> & args, cudaStrea
       const int count = s.level_begin[L + 1] - s.level_begin[L];
       if (count == 0) continue;
       a.task_offset = s.level_begin[L];
-      sweep_level_kernel<T, DIMS, SCHEME, TX><<<count, s.threads, s.smem, stream>>>(a);
+      sweep_level_kernel<T, DIMS, SCHEME, TX, MANY><<<count, s.threads, s.smem, stream>>>(a);
       if (launches) ++*launches;
     }
   }
@@ -1046,6 +1062,16 @@ auto dispatch(int dims, int precision, int scheme, int tx, F && f)
   return by_dims(TypeTag<float>{});
 }
 
+// Calls g with std::true_type for the 12-CTA FP32 DD body when `many` asks for
+// it, else with std::false_type (the only body of the other modes).
+template <typename T, int S, typename G>
+auto with_many(bool many, G && g)
+{
+  if constexpr (has_many_body<T, S>())
+    if (many) return g(std::true_type{});
+  return g(std::false_type{});
+}
+
 }  // namespace
 
 int sweep_threads(int gs)
@@ -1066,30 +1092,40 @@ size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx)
   });
 }
 
-doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem)
+bool sweep_many_ctas(int precision, int scheme, int ngroups)
+{
+  return precision == DOMA_PREC_FP32 && scheme == DOMA_SCHEME_DD && ngroups >= 3;
+}
+
+doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem, bool many)
 {
   cudaError_t e = dispatch(dims, precision, scheme, tx, [&](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
     using T = typename decltype(tag_t)::type;
     constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
-    cudaError_t r = cudaFuncSetAttribute(sweep_persistent_kernel<T, D, S, X>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (r != cudaSuccess) return r;
-    return cudaFuncSetAttribute(sweep_level_kernel<T, D, S, X>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return with_many<T, S>(many, [&](auto many_c) {
+      constexpr bool MN = decltype(many_c)::value;
+      cudaError_t r = cudaFuncSetAttribute(sweep_persistent_kernel<T, D, S, X, MN>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (r != cudaSuccess) return r;
+      return cudaFuncSetAttribute(sweep_level_kernel<T, D, S, X, MN>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
   });
   DOMA_CUDA_TRY(e);
   return DOMA_OK;
 }
 
-int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem)
+int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem, bool many)
 {
   return dispatch(dims, precision, scheme, tx, [&](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
     using T = typename decltype(tag_t)::type;
     constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T, D, S, X>,
-                                                      threads, smem) != cudaSuccess)
-      return 0;
+    const cudaError_t r = with_many<T, S>(many, [&](auto many_c) {
+      return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, sweep_persistent_kernel<T, D, S, X, decltype(many_c)::value>, threads, smem);
+    });
+    if (r != cudaSuccess) return 0;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1161,10 +1197,13 @@ doma_status launch_sweep(int dims, int precision, int scheme, const Schedule & s
   return dispatch(dims, precision, scheme, s.tx, [&](auto tag_t, auto dims_c, auto sch_c, auto tx_c) {
     using T = typename decltype(tag_t)::type;
     constexpr int D = decltype(dims_c)::value, S = decltype(sch_c)::value, X = decltype(tx_c)::value;
-    if constexpr (std::is_same<T, double>::value)
-      return launch_impl<T, D, S, X>(s, *a64, stream, launches);
-    else
-      return launch_impl<T, D, S, X>(s, *a32, stream, launches);
+    return with_many<T, S>(s.many, [&](auto many_c) {
+      constexpr bool MN = decltype(many_c)::value;
+      if constexpr (std::is_same<T, double>::value)
+        return launch_impl<T, D, S, X, MN>(s, *a64, stream, launches);
+      else
+        return launch_impl<T, D, S, X, MN>(s, *a32, stream, launches);
+    });
   });
 }
 
