@@ -158,7 +158,7 @@ struct Schedule {
   int nbx = 0, nby = 0, nbz = 0;
   int threads = 0;
   size_t smem = 0;
-  bool many = false;       // FP32 DD: the 12-CTA-per-SM body (sweep_many_ctas)
+  bool many = false;       // FP32: the body for many tasks per level (sweep_many_ctas)
   bool persistent = true;  // dataflow kernel (true) or one launch per level
   int grid = 0;            // persistent grid (CTAs)
   std::vector<Task> tasks;
@@ -174,11 +174,12 @@ int sweep_tile_x(int requested);  // supported block length along x: 8, 16 or 32
 // pencil), in whole warps.
 int sweep_threads(int gs);
 size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx);
-// FP32 DD compiles two bodies with the same arithmetic: 8 CTAs per SM (64
-// registers) and 12 (40 registers).  A schedule with three or more ordinate
-// groups per octant has enough independent tasks per wavefront level to use
-// the 12-CTA body; fewer groups favour the longer-lived registers.
-bool sweep_many_ctas(int precision, int scheme, int ngroups);
+// The FP32 modes compile two bodies with the same arithmetic: DD for 8 and 12
+// CTAs per SM (64 and 40 registers), TW-DD for 2 and 3 (128 and 80).  A
+// schedule with three or more (ordinate group, group in flight) slots per
+// octant has enough independent tasks per wavefront level for the body with
+// more CTAs; fewer favour the longer-lived registers.
+bool sweep_many_ctas(int precision, int ngroups, int groups_in_flight);
 doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem, bool many);
 // CTAs of the persistent sweep kernel that fit on the device at once.
 int sweep_resident_ctas(int dims, int precision, int scheme, int tx, int threads, size_t smem,

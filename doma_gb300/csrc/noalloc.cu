@@ -317,7 +317,7 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   sc.persistent = true;
   sc.threads = sweep_threads(std::min(kg, d_oct));
   sc.smem = sweep_smem_bytes(dims, DOMA_PREC_FP32, (int)scheme, tx);
-  sc.many = sweep_many_ctas(DOMA_PREC_FP32, (int)scheme, ngroups);
+  sc.many = sweep_many_ctas(DOMA_PREC_FP32, ngroups, 1);
   st = sweep_prepare(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.smem, sc.many);
   if (st != DOMA_OK) return st;
   const int fit = sweep_resident_ctas(dims, DOMA_PREC_FP32, (int)scheme, tx, sc.threads, sc.smem,

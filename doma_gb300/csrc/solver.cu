@@ -246,12 +246,11 @@ void build_schedule(doma_solver * s)
   sc.nbz = (s->nz + sc.tz - 1) / sc.tz;
   sc.threads = sweep_threads(sc.gs);
   sc.smem = sweep_smem_bytes(s->dims, s->opts.precision, s->opts.scheme, sc.tx);
-  sc.many = sweep_many_ctas(s->opts.precision, s->opts.scheme, sc.ngroups);
+  sc.many = sweep_many_ctas(s->opts.precision, sc.ngroups, s->gif);
   {
-    // DOMA_SWEEP_MANY=0/1 picks the FP32 DD body by hand (the tests run both)
+    // DOMA_SWEEP_MANY=0/1 picks the FP32 body by hand (the tests run both)
     const char * env = std::getenv("DOMA_SWEEP_MANY");
-    if (env && s->opts.precision == DOMA_PREC_FP32 && s->opts.scheme == DOMA_SCHEME_DD)
-      sc.many = std::string(env) == "1";
+    if (env && s->opts.precision == DOMA_PREC_FP32) sc.many = std::string(env) == "1";
   }
   const int levels = sc.nbx + sc.nby + sc.nbz - 2;
   std::vector<std::vector<Task>> by_level(levels);

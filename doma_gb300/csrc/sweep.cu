@@ -55,7 +55,10 @@
 #define DOMA_SWEEP_MIN_CTAS_FP64 1
 #endif
 #ifndef DOMA_SWEEP_MIN_CTAS
-#define DOMA_SWEEP_MIN_CTAS 3
+#define DOMA_SWEEP_MIN_CTAS 2
+#endif
+#ifndef DOMA_SWEEP_MIN_CTAS_MANY
+#define DOMA_SWEEP_MIN_CTAS_MANY 3
 #endif
 
 namespace doma {
@@ -877,11 +880,16 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 //     ordinate groups) take 115 and 196 us, against 143 and 219 us at 12 per
 //     SM (40 registers).  The 100^3 duct with 36 ordinates per octant (five
 //     groups: more independent tasks per wavefront level) is the other way
-//     round, 1542 against 1369 us.  MANY selects the 12-CTA body; solvers take
-//     it from three ordinate groups per octant up (sweep_many_ctas).
-//   * FP32 TW-DD (256 threads), with more live values per cell: 3, 80 registers.
+//     round, 1542 against 1369 us, and so is the multigroup solve with eight
+//     groups in flight (415 against 374 ms).
+//   * FP32 TW-DD (256-thread CTAs), with more live values per cell: 2 per SM
+//     (128 registers) for one group in flight, 265 against 270 us at 3 (80
+//     registers, which spill 12 bytes); 3 per SM with many tasks per level.
 //   * FP64: 1 (2 and 3 per SM were 19 % and 38 % slower; the FP64 pipe is the limit).
-// Both DD bodies run the same instructions on the same values: the same bits.
+// MANY selects the body for many tasks per wavefront level; solvers take it
+// from three (ordinate group, group in flight) slots per octant up
+// (sweep_many_ctas).  Both bodies of a scheme run the same instructions on the
+// same values: the same bits.
 template <typename T, int SCHEME>
 constexpr int sweep_cta_threads()
 {
@@ -893,7 +901,7 @@ constexpr int sweep_min_ctas()
 {
   return std::is_same<T, double>::value ? DOMA_SWEEP_MIN_CTAS_FP64
          : SCHEME == DOMA_SCHEME_DD     ? (MANY ? DOMA_SWEEP_MIN_CTAS_DD_MANY : DOMA_SWEEP_MIN_CTAS_DD)
-                                        : DOMA_SWEEP_MIN_CTAS;
+                                        : (MANY ? DOMA_SWEEP_MIN_CTAS_MANY : DOMA_SWEEP_MIN_CTAS);
 }
 
 // The batched kernel holds every block length's body; at 40 registers its DD
@@ -902,14 +910,14 @@ constexpr int sweep_min_ctas()
 template <typename T, int SCHEME>
 constexpr int sweep_batch_min_ctas()
 {
-  return SCHEME == DOMA_SCHEME_DD ? DOMA_SWEEP_BATCH_MIN_CTAS_DD : sweep_min_ctas<T, SCHEME>();
+  return SCHEME == DOMA_SCHEME_DD ? DOMA_SWEEP_BATCH_MIN_CTAS_DD : sweep_min_ctas<T, SCHEME, true>();
 }
 
-// Only FP32 DD has a second body.
+// Only the FP32 modes have a second body.
 template <typename T, int SCHEME>
 constexpr bool has_many_body()
 {
-  return !std::is_same<T, double>::value && SCHEME == DOMA_SCHEME_DD;
+  return !std::is_same<T, double>::value;
 }
 
 template <typename T, int DIMS, int SCHEME, int TX>
@@ -1062,8 +1070,8 @@ auto dispatch(int dims, int precision, int scheme, int tx, F && f)
   return by_dims(TypeTag<float>{});
 }
 
-// Calls g with std::true_type for the 12-CTA FP32 DD body when `many` asks for
-// it, else with std::false_type (the only body of the other modes).
+// Calls g with std::true_type for an FP32 mode's many-task body when `many`
+// asks for it, else with std::false_type (the only body of the FP64 mode).
 template <typename T, int S, typename G>
 auto with_many(bool many, G && g)
 {
@@ -1092,9 +1100,9 @@ size_t sweep_smem_bytes(int dims, int precision, int scheme, int tx)
   });
 }
 
-bool sweep_many_ctas(int precision, int scheme, int ngroups)
+bool sweep_many_ctas(int precision, int ngroups, int groups_in_flight)
 {
-  return precision == DOMA_PREC_FP32 && scheme == DOMA_SCHEME_DD && ngroups >= 3;
+  return precision == DOMA_PREC_FP32 && ngroups * groups_in_flight >= 3;
 }
 
 doma_status sweep_prepare(int dims, int precision, int scheme, int tx, size_t smem, bool many)

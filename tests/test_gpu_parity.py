@@ -99,13 +99,15 @@ def test_block_shape_does_not_change_results(tile, precision, dims, scheme):
     assert np.array_equal(phi, ref_phi)
 
 
+@pytest.mark.parametrize("scheme", ["dd", "tw_dd"])
 @pytest.mark.parametrize("dims", [2, 3])
-def test_both_dd_register_bodies_give_the_same_bits(monkeypatch, dims):
-    """FP32 DD is compiled twice, for 8 and for 12 CTAs per SM (64 and 40
-    registers); the solver picks one by its ordinate groups per octant.  Both
-    run the same arithmetic, so a solve gives the same bits and counts."""
+def test_both_register_bodies_give_the_same_bits(monkeypatch, dims, scheme):
+    """Each FP32 scheme is compiled twice, for fewer and for more CTAs per SM
+    (DD 8 and 12, TW-DD 2 and 3); the solver picks one by the tasks a
+    wavefront level holds.  Both run the same arithmetic, so a solve gives the
+    same bits and counts."""
     p = P.random_problem(17, dims, 21, 12, 8, groups=2, np_=3, na=3, materials=3)
-    opts = P.make_options(scheme="dd", precision="fp32", fs_tol=1e-6, mg_tol=1e-6)
+    opts = P.make_options(scheme=scheme, precision="fp32", fs_tol=1e-6, mg_tol=1e-6)
     out = []
     for many in ("0", "1"):
         monkeypatch.setenv("DOMA_SWEEP_MANY", many)
