@@ -163,7 +163,7 @@ class ClockSampler:
 # dram__bytes_write.sum from one ncu capture of sweep_persistent_kernel, FP32
 # TW-DD, 64^3, 128 directions).  Far below the algorithmic bytes: the sweep's
 # working set stays in L2.
-SWEEP_DRAM_BYTES_PER_LAUNCH = 2_484_736 + 320_768
+SWEEP_DRAM_BYTES_PER_LAUNCH = 2_484_224 + 279_040
 # the same kernel with all 8 groups in flight: mean of two captured launches
 # (dram__bytes_read.sum + dram__bytes_write.sum)
 ALL_GROUPS_DRAM_BYTES_PER_LAUNCH = 29_660_672 + 142_600_448
@@ -378,7 +378,7 @@ def roofline_entry(ms: float, updates: float, d_oct: int, s_bytes: int, peak: fl
 # (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture).  The
 # 320 MB of double partials (5 ordinate groups of 8 x 8 octants x 10^6 cells)
 # do not fit in L2, so most of it is their write-back.
-STREAMING_SWEEP_DRAM_BYTES = 36_372_224 + 437_900_032
+STREAMING_SWEEP_DRAM_BYTES = 30_568_960 + 346_246_912
 
 
 def streaming_leg(args, stream, flush):
