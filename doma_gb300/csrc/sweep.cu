@@ -772,9 +772,10 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
     const float * rlx_l = rlx - d;
     const bool ybound = active && jl == vy - 1;
     const bool zbound = DIMS == 3 && active && kl == vz - 1;
-    float * yout_g = A.yf + F.y(k0 + kl, i0) + nl;
-    float * zout_g = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl : nullptr;
-    float * P_lane = P + (PAIRS ? nl >> 1 : nl) * CELLS + ebase;
+    // store bases shifted by -d as well: step s stores at a constant offset
+    float * yout_l = A.yf + F.y(k0 + kl, i0) + nl - (ptrdiff_t)d * KG;
+    float * zout_l = DIMS == 3 ? A.zf + F.z(j0 + jl, i0) + nl - (ptrdiff_t)d * KG : nullptr;
+    float * P_l = P + (PAIRS ? nl >> 1 : nl) * CELLS + ebase - d;
     const float wgt = PAIRS ? wts[min(nl, KG - 1)] : 0.f;
     float x = xin_v, ysh = 0.f, zsh = 0.f;
     constexpr int STEPS = TX + PY + PZ - 2;
@@ -810,15 +811,15 @@ __device__ __forceinline__ void run_task_f32(const SweepArgs<float> & A, const T
         else psi = dd2_fast(qc.x, qc.y, hx, cy_t, xo, y);
       }
       x = valid ? xo : x;
-      st_global_if(yout_g + il * KG, y, valid && ybound);
-      if constexpr (DIMS == 3) st_global_if(zout_g + il * KG, z, valid && zbound);
+      st_global_if(yout_l + s * KG, y, valid && ybound);
+      if constexpr (DIMS == 3) st_global_if(zout_l + s * KG, z, valid && zbound);
       if constexpr (PAIRS) {
         // lanes l and l + 16 hold the same cell for ordinates nl and nl + 1
         const float wp = valid ? fM(wgt, psi) : 0.f;
         const float pair = fA(wp, __shfl_xor_sync(FULL, wp, 16));
-        st_shared_if(P_lane + il, pair, valid && lane < 16);
+        st_shared_if(P_l + s, pair, valid && lane < 16);
       } else {
-        st_shared_if(P_lane + il, psi, valid);
+        st_shared_if(P_l + s, psi, valid);
       }
       ysh = __shfl_up_sync(FULL, y, 1);
       if (DIMS == 3) zsh = __shfl_up_sync(FULL, z, PY);
