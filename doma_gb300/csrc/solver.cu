@@ -121,6 +121,13 @@ struct doma_solver {
   double * d_acc_partials = nullptr;                                  // [grid]
   unsigned * d_acc_ticket = nullptr;
   double * d_ref = nullptr;                                           // [G][N]
+  // a correction's kernels (per group: residual, input, U-Net forward,
+  // correction) captured as one graph after a first, eager correction
+  cudaGraph_t acc_graph = nullptr;
+  cudaGraphExec_t acc_exec = nullptr;
+  const doma_unet * acc_net = nullptr;   // the net and workspace it was captured over
+  unsigned long long acc_gen = 0;
+  bool acc_warm = false;
   double ref_norm2 = 0.0, ref_target = 0.0;
   doma_accel_stats stats{};
 
@@ -571,6 +578,8 @@ void release(doma_solver * s)
   if (s->h_k) cudaFreeHost(s->h_k);
   if (s->tr_exec) cudaGraphExecDestroy(s->tr_exec);
   if (s->tr_graph) cudaGraphDestroy(s->tr_graph);
+  if (s->acc_exec) cudaGraphExecDestroy(s->acc_exec);
+  if (s->acc_graph) cudaGraphDestroy(s->acc_graph);
   for (void * p : s->tr_allocs) cudaFree(p);
   if (s->h_dnps) cudaFreeHost(s->h_dnps);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -1213,7 +1222,8 @@ doma_status solve_multigroup(doma_solver * s, doma_report * r)
 
 // Network corrections for every group in order (y chain), then the next
 // sweep's source from delta + Delta.
-doma_status accel_correction(doma_solver * s, cudaStream_t st)
+// The kernels of one correction, in group order (the y chain).
+doma_status accel_correction_kernels(doma_solver * s, cudaStream_t st)
 {
   const size_t N = s->N;
   float * y_prev = nullptr;
@@ -1231,6 +1241,58 @@ doma_status accel_correction(doma_solver * s, cudaStream_t st)
     y_prev = ya;
     std::swap(ya, yb);
   }
+  return DOMA_OK;
+}
+
+// A correction is G U-Net forwards and 3G small kernels, about 250 short
+// launches: after a first, eager correction (which sizes the network's
+// workspace and configures its kernels) they are captured once as a graph and
+// replayed.  The graph is rebuilt when the net or its workspace changed.
+// DOMA_ACCEL_GRAPH=0 keeps the launches eager.
+doma_status accel_correction_launch(doma_solver * s, cudaStream_t st)
+{
+  const char * env = std::getenv("DOMA_ACCEL_GRAPH");
+  // (the legacy default stream cannot be captured)
+  const bool use_graph = !(env && std::string(env) == "0") && st != nullptr && st != cudaStreamLegacy;
+  const bool stale = s->acc_net != s->accel || s->acc_gen != s->accel->work_gen;
+  if (stale) {
+    if (s->acc_exec) cudaGraphExecDestroy(s->acc_exec);
+    if (s->acc_graph) cudaGraphDestroy(s->acc_graph);
+    s->acc_exec = nullptr;
+    s->acc_graph = nullptr;
+    s->acc_warm = false;
+  }
+  if (!use_graph || !s->acc_warm) {
+    DOMA_TRY(accel_correction_kernels(s, st));
+    s->acc_warm = true;
+    s->acc_net = s->accel;
+    s->acc_gen = s->accel->work_gen;
+    return DOMA_OK;
+  }
+  if (!s->acc_exec) {
+    DOMA_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const doma_status cst = accel_correction_kernels(s, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (cst != DOMA_OK) {
+      if (g) cudaGraphDestroy(g);
+      return cst;
+    }
+    DOMA_CUDA_TRY(e);
+    s->acc_graph = g;
+    DOMA_CUDA_TRY(cudaGraphInstantiate(&s->acc_exec, g, 0));
+    if (s->acc_gen != s->accel->work_gen) {   // the capture itself resized the workspace
+      set_error("the U-Net workspace changed while its correction graph was captured");
+      return DOMA_CUDA_ERROR;
+    }
+  }
+  DOMA_CUDA_TRY(cudaGraphLaunch(s->acc_exec, st));
+  return DOMA_OK;
+}
+
+doma_status accel_correction(doma_solver * s, cudaStream_t st)
+{
+  DOMA_TRY(accel_correction_launch(s, st));
   // a tensor-memory convolution whose bounded wait gave up leaves garbage in
   // the correction: report it instead of sweeping from it
   DOMA_CUDA_TRY(cudaStreamSynchronize(st));

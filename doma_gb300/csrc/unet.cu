@@ -67,6 +67,7 @@ doma_status ensure_work(doma_unet * n, int batch, int nz, int ny, int nx)
 {
   if (n->batch == batch && n->nz == nz && n->ny == ny && n->nx == nx) return DOMA_OK;
   free_work(n->work);
+  ++n->work_gen;   // graphs captured over the old workspace are stale
   n->batch = n->nz = n->ny = n->nx = 0;
   UnetWork & w = n->work;
   for (int l = 0; l < 4; ++l) {

@@ -57,6 +57,7 @@ struct doma_unet {
   double * d_loss = nullptr;
   int adam_step = 0;
   int batch = 0, nz = 0, ny = 0, nx = 0;
+  unsigned long long work_gen = 0;   // bumped whenever the workspace is reallocated
   doma::UnetWork work;
   cudaStream_t stream = nullptr;
 };

@@ -75,6 +75,36 @@ def test_guarded_corrections_keep_the_plain_fixed_point():
 
 
 @pytest.mark.gpu
+def test_captured_corrections_equal_eager_ones(monkeypatch):
+    """From the second correction on, a correction's launches (per group:
+    residual, input, U-Net forward, correction) replay as one captured graph;
+    DOMA_ACCEL_GRAPH=0 launches them one by one.  Same kernels in the same
+    order: the same bits, counts and guard decisions."""
+    from pathlib import Path
+
+    from doma_gb300.learned.net import UNet
+    from doma_gb300.solver import Solver
+    weights = Path(__file__).resolve().parents[1] / "doma_gb300" / "learned" / "weights" / "unet_c32.npz"
+    p = P.learned_problem(900003, n=16, groups=3, np_=2, na=2)
+    opts = P.make_options(scheme="dd", precision="fp32", fs_tol=1e-6, fs_max_it=20000,
+                          iteration="multigroup")
+    out = []
+    with UNet(seed=0) as net:
+        net.load(weights)
+        for graph in ("1", "0"):
+            monkeypatch.setenv("DOMA_ACCEL_GRAPH", graph)
+            with Solver(p, opts) as s:
+                s.set_accelerator(net, first=2, interval=3, max_corrections=6, guard=True)
+                rep = s.solve_fixed_source()
+                out.append((rep.si_iterations, s.accel_stats(), s.scalar_flux()))
+    (i1, st1, phi1), (i0, st0, phi0) = out
+    assert i1 == i0
+    assert (st1["accepted"], st1["rejected"]) == (st0["accepted"], st0["rejected"])
+    assert st1["accepted"] + st1["rejected"] >= 2   # the second one replays the graph
+    assert np.array_equal(phi1, phi0)
+
+
+@pytest.mark.gpu
 def test_batch_stepping_equals_the_graph_solve():
     from doma_gb300.solver import Batch
     ps = [P.learned_problem(i, n=16, groups=2, np_=2, na=2) for i in range(3)]
