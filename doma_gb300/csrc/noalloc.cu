@@ -207,7 +207,8 @@ extern "C" doma_status doma_sweep_noalloc(const doma_problem * p, uint32_t schem
   }
 
   // block shape and task list (level order) in static host storage
-  const int tx = sweep_tile_x(dims == 3 ? 8 : 32);
+  // the solver's block lengths (pick_tile): TW-DD 16, DD 16 with many tasks per level, else 8
+  const int tx = sweep_tile_x(dims == 3 ? (scheme == DOMA_SCHEME_TW_DD || ngroups >= 3 ? 16 : 8) : 32);
   const int py = dims == 3 ? 4 : 16, pz = dims == 3 ? 4 : 1;
   const int nbx = (nx + tx - 1) / tx, nby = (ny + py - 1) / py, nbz = (nz + pz - 1) / pz;
   const int levels = nbx + nby + nbz - 2;

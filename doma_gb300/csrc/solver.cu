@@ -233,20 +233,22 @@ doma_status validate(const doma_problem * p, const doma_options * o)
 // scheme) per task.
 void pick_tile(doma_solver * s, const doma_options * o)
 {
-  // measured on GB300 with the present bodies (3D): TW-DD 64^3 357, 266, 317 us
-  // for 8, 16, 32-cell blocks; DD 64^3 196, 194, 244 us; the DD 100^3 duct
-  // 1371 us at 8 and 1246 at 16; but DD 48^3 115 us at 8 and 121 at 16, and
-  // the FP64 DD 20^3 solve 38 ms at 8 and 47 at 16.  DD takes 16 from 64
-  // cells along x up, TW-DD always; 2D takes 32.
-  const bool dd_long = o->scheme == DOMA_SCHEME_DD && s->nx >= 64;
-  const int want = o->tile_x ? (int)o->tile_x
-                             : (s->dims == 3 ? (o->scheme == DOMA_SCHEME_TW_DD || dd_long ? 16 : 8) : 32);
-  s->sched.tx = sweep_tile_x(want);
-  s->sched.ty = s->dims == 3 ? 4 : 16;
-  s->sched.tz = s->dims == 3 ? 4 : 1;
   const int kg = ordinate_group((int)o->precision, (int)o->scheme);
   s->sched.ngroups = (s->d_oct + kg - 1) / kg;
   s->sched.gs = std::min(kg, s->d_oct);
+  // Measured on GB300 with the present bodies (3D): TW-DD 64^3 347, 261, 291 us
+  // for 8, 16, 32-cell blocks.  DD wants 8-cell blocks when a wavefront level
+  // holds few tasks (64^3 and 48^3 with 16 ordinates: 186 against 193 us, 110
+  // against 121 us) and 16 when it holds many (the 100^3 duct with 36
+  // ordinates: 1253 against 1312 us; the FP64 duct 0.96 against 1.21 s), the
+  // criterion of the register bodies (sweep_many_ctas, counted here with the
+  // mode's own ordinate groups).  2D takes 32.
+  const bool many = s->sched.ngroups * s->gif >= 3;
+  const int want3 = o->scheme == DOMA_SCHEME_TW_DD ? 16 : (many ? 16 : 8);
+  const int want = o->tile_x ? (int)o->tile_x : (s->dims == 3 ? want3 : 32);
+  s->sched.tx = sweep_tile_x(want);
+  s->sched.ty = s->dims == 3 ? 4 : 16;
+  s->sched.tz = s->dims == 3 ? 4 : 1;
 }
 
 void build_schedule(doma_solver * s)
