@@ -1942,6 +1942,14 @@ doma_status doma_solver_set_accelerator(doma_solver * s, doma_unet * net,
                                         const doma_accel_options * opts)
 {
   if (!s) return bad("null solver");
+  // a correction graph captured over the previous net is dropped (a new net
+  // may even reuse the old one's address)
+  if (s->acc_exec) cudaGraphExecDestroy(s->acc_exec);
+  if (s->acc_graph) cudaGraphDestroy(s->acc_graph);
+  s->acc_exec = nullptr;
+  s->acc_graph = nullptr;
+  s->acc_net = nullptr;
+  s->acc_warm = false;
   if (!net) {
     s->accel = nullptr;
     return DOMA_OK;
