@@ -163,7 +163,7 @@ class ClockSampler:
 # dram__bytes_write.sum from one ncu capture of sweep_persistent_kernel, FP32
 # TW-DD, 64^3, 128 directions).  Far below the algorithmic bytes: the sweep's
 # working set stays in L2.
-SWEEP_DRAM_BYTES_PER_LAUNCH = 2_480_896 + 274_688
+SWEEP_DRAM_BYTES_PER_LAUNCH = 2_709_504 + 924_160
 # the same kernel with all 8 groups in flight: mean of two captured launches
 # (dram__bytes_read.sum + dram__bytes_write.sum)
 ALL_GROUPS_DRAM_BYTES_PER_LAUNCH = 29_660_672 + 142_600_448

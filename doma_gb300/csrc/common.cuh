@@ -36,17 +36,17 @@ const char * get_error();
   } while (0)
 
 // Ordinates of one octant handled by one sweep task (two per warp), at most
-// kGroupMax.  FP32 DD runs groups of 8: twice the tasks per sweep, each half
-// as long, which shortens the dataflow's critical path (measured on GB300:
-// 100^3 with 36 ordinates per octant 1.73 -> 1.38 ms per sweep, 64^3 with 16
-// ordinates 229 -> 221 us).  FP32 TW-DD, whose cell solve keeps more values
-// live, was slower with 8 (271 -> 278 us at 64^3) and keeps 16, as does the
-// FP64 exact mode.  Every kernel of one (precision, scheme) uses the same
-// size, so single, batched and allocation-free sweeps give the same bits.
+// kGroupMax.  The FP32 modes run groups of 8: twice the tasks per sweep, each
+// half as long, which shortens the dataflow's critical path (measured on
+// GB300: the DD 100^3 duct with 36 ordinates per octant 1.73 -> 1.38 ms per
+// sweep; TW-DD 64^3 with 16 ordinates 258 -> 244 us once its partials were
+// summed on the FP32 pipes and its body given 5 CTAs per SM).  The FP64 exact
+// mode keeps 16.  Every kernel of one (precision, scheme) uses the same size,
+// so single, batched and allocation-free sweeps give the same bits.
 constexpr int kGroupMax = 16;
-__host__ __device__ constexpr int ordinate_group(int precision, int scheme)
+__host__ __device__ constexpr int ordinate_group(int precision, int /* scheme */)
 {
-  return precision == DOMA_PREC_FP32 && scheme == DOMA_SCHEME_DD ? 8 : kGroupMax;
+  return precision == DOMA_PREC_FP32 ? 8 : kGroupMax;
 }
 
 #ifdef __CUDACC__

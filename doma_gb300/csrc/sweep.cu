@@ -55,10 +55,10 @@
 #define DOMA_SWEEP_MIN_CTAS_FP64 1
 #endif
 #ifndef DOMA_SWEEP_MIN_CTAS
-#define DOMA_SWEEP_MIN_CTAS 2
+#define DOMA_SWEEP_MIN_CTAS 5
 #endif
 #ifndef DOMA_SWEEP_MIN_CTAS_MANY
-#define DOMA_SWEEP_MIN_CTAS_MANY 3
+#define DOMA_SWEEP_MIN_CTAS_MANY 6
 #endif
 
 namespace doma {
@@ -883,9 +883,10 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 //     groups: more independent tasks per wavefront level) is the other way
 //     round, 1542 against 1369 us, and so is the multigroup solve with eight
 //     groups in flight (415 against 374 ms).
-//   * FP32 TW-DD (256-thread CTAs), with more live values per cell: 2 per SM
-//     (128 registers) for one group in flight, 265 against 270 us at 3 (80
-//     registers, which spill 12 bytes); 3 per SM with many tasks per level.
+//   * FP32 TW-DD (128-thread CTAs), with more live values per cell: 5 per SM
+//     (at most 102 registers) for one group in flight: 244 us at 64^3, against
+//     246 us at 4 and 276 us at 6 (80 registers); 6 per SM with many tasks per
+//     level.
 //   * FP64: 1 (2 and 3 per SM were 19 % and 38 % slower; the FP64 pipe is the limit).
 // MANY selects the body for many tasks per wavefront level; solvers take it
 // from three (ordinate group, group in flight) slots per octant up

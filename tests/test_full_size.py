@@ -9,7 +9,7 @@
   and upscatter sources, the residuals and the failed-MG exit path.
 * Streaming duct: 100^3 cells, one group, 12 x 24 = 288 directions
   (np = na = 6: 36 ordinates per octant, split into ordinate groups of 16 in
-  the FP64 mode and of 8 in FP32 DD, the last one partial in both, and 298
+  the FP64 mode and of 8 in FP32, the last one partial in both, and 298
   wavefront planes per octant), DD, a near-void
   duct through an absorber.  It converges in about 20 source iterations, so
   it runs to DOMA's 1e-8 tolerance.

@@ -88,8 +88,8 @@ def test_fp64_matches_oracle_random(seed, scheme, dims):
 @pytest.mark.parametrize("scheme", ["tw_dd", "dd"])
 def test_block_shape_does_not_change_results(tile, precision, dims, scheme):
     """Every block length, with ragged edge blocks in every axis and a
-    partial ordinate group (9 ordinates per octant: one partial group of 16,
-    or in FP32 DD a full group of 8 and a partial one), gives the same bits."""
+    partial ordinate group (9 ordinates per octant: in FP32 a full group of 8
+    and a partial one, in FP64 one partial group of 16), gives the same bits."""
     p = P.random_problem(31, dims, 37, 19, 7, groups=2, np_=3, na=3, materials=3)
     base = P.make_options(scheme=scheme, precision=precision, fs_tol=1e-9, mg_tol=1e-9)
     ref_phi, _ = run(p, base)
@@ -103,7 +103,7 @@ def test_block_shape_does_not_change_results(tile, precision, dims, scheme):
 @pytest.mark.parametrize("dims", [2, 3])
 def test_both_register_bodies_give_the_same_bits(monkeypatch, dims, scheme):
     """Each FP32 scheme is compiled twice, for fewer and for more CTAs per SM
-    (DD 8 and 12, TW-DD 2 and 3); the solver picks one by the tasks a
+    (DD 8 and 12, TW-DD 5 and 6); the solver picks one by the tasks a
     wavefront level holds.  Both run the same arithmetic, so a solve gives the
     same bits and counts."""
     p = P.random_problem(17, dims, 21, 12, 8, groups=2, np_=3, na=3, materials=3)
