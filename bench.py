@@ -166,7 +166,7 @@ class ClockSampler:
 SWEEP_DRAM_BYTES_PER_LAUNCH = 2_709_504 + 924_160
 # the same kernel with all 8 groups in flight: mean of two captured launches
 # (dram__bytes_read.sum + dram__bytes_write.sum)
-ALL_GROUPS_DRAM_BYTES_PER_LAUNCH = 29_660_672 + 142_600_448
+ALL_GROUPS_DRAM_BYTES_PER_LAUNCH = 41_324_672 + 305_230_080
 
 
 def measured_peak_hbm():
