@@ -1,6 +1,7 @@
 """The C++ drop-in layer: deck reader, mesh, text output and (on a GPU) the
 TransportSolver3D/2D classes and the deck runner."""
 import json
+import os
 import subprocess
 from pathlib import Path
 
@@ -15,7 +16,9 @@ from doma_gb300.decks import read_deck_summary, write_deck
 ROOT = Path(__file__).resolve().parents[1]
 SRC = ROOT / "tests" / "cpp" / "host_check.cpp"
 EXE = ROOT / "tests" / "cpp" / "_build" / "host_check"
-REF_CASES = Path("/root/reference/cases")
+# DOMA's example decks, where its source tree is present ($DOMA_REFERENCE_TREE,
+# else a directory named `reference` beside this repository)
+REF_CASES = Path(os.environ.get("DOMA_REFERENCE_TREE", str(ROOT.parent / "reference"))) / "cases"
 
 
 @pytest.fixture(scope="module")
