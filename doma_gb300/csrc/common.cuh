@@ -41,12 +41,17 @@ const char * get_error();
 // GB300: the DD 100^3 duct with 36 ordinates per octant 1.73 -> 1.38 ms per
 // sweep; TW-DD 64^3 with 16 ordinates 258 -> 244 us once its partials were
 // summed on the FP32 pipes and its body given 5 CTAs per SM).  The FP64 exact
-// mode keeps 16.  Every kernel of one (precision, scheme) uses the same size,
-// so single, batched and allocation-free sweeps give the same bits.
+// mode, whose tasks are bound by the SM's small FP64 pipe, runs groups of 2
+// (one warp): 20^3 DD solve 37.0 -> 32.4 ms, 100^3 duct 957 -> 756 ms, against
+// groups of 16; its bits do not depend on the grouping (every ordinate's w psi
+// is kept and summed in DOMA's order).  Every kernel of one (precision,
+// scheme) uses the same size, so single, batched and allocation-free sweeps
+// give the same bits.
 constexpr int kGroupMax = 16;
+constexpr int kGroupExact = 2;   // the FP64 exact mode's group size
 __host__ __device__ constexpr int ordinate_group(int precision, int /* scheme */)
 {
-  return precision == DOMA_PREC_FP32 ? 8 : kGroupMax;
+  return precision == DOMA_PREC_FP32 ? 8 : kGroupExact;
 }
 
 #ifdef __CUDACC__

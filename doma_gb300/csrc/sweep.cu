@@ -392,7 +392,7 @@ template <int DIMS, int TX>
 struct TaskSmemExact {
   static constexpr int PY = Pencils<DIMS>::PY, PZ = Pencils<DIMS>::PZ;
   static constexpr int CELLS = TX * PY * PZ;
-  static constexpr int KG = kGroupMax;                      // ordinate_group(DOMA_PREC_FP64, *)
+  static constexpr int KG = kGroupExact;                    // ordinate_group(DOMA_PREC_FP64, *)
   static constexpr int YF = PZ * TX * KG;                  // y faces [PZ][TX][KG]
   static constexpr int ZF = DIMS == 3 ? PY * TX * KG : 0;  // z faces [PY][TX][KG]
   static constexpr int NT = 2 * YF + 2 * ZF + 2 * CELLS + TX + PY + PZ + KG * (TX + PY + PZ);
