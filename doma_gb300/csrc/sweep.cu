@@ -883,11 +883,13 @@ __device__ __forceinline__ void run_task(const SweepArgs<T> & A, const Task task
 //     groups: more independent tasks per wavefront level) is the other way
 //     round, 1542 against 1369 us, and so is the multigroup solve with eight
 //     groups in flight (415 against 374 ms).
-//   * FP32 TW-DD (128-thread CTAs), with more live values per cell: 5 per SM
-//     (at most 102 registers) for one group in flight: 244 us at 64^3, against
-//     246 us at 4 and 276 us at 6 (80 registers); 6 per SM with many tasks per
+//   * FP32 TW-DD (128-thread CTAs), with more live values per cell: compiled
+//     for 5 per SM (it takes 80 registers, so 6 fit) for one group in flight,
+//     244 us at 64^3 against 246 us compiled for 4; for 6 with many tasks per
 //     level.
-//   * FP64: 1 (2 and 3 per SM were 19 % and 38 % slower; the FP64 pipe is the limit).
+//   * FP64 (one-warp CTAs): 1, which leaves the registers to the compiler (154;
+//     12 CTAs fit).  With 256-thread CTAs, 2 and 3 per SM had been 19 % and
+//     38 % slower than 1: the FP64 pipe is the limit.
 // MANY selects the body for many tasks per wavefront level; solvers take it
 // from three (ordinate group, group in flight) slots per octant up
 // (sweep_many_ctas).  Both bodies of a scheme run the same instructions on the
